@@ -1,0 +1,255 @@
+/*
+ * kgpu.h — C ABI of the GB300 configuration-validity and proximity engine.
+ *
+ * This is the drop-in boundary for Klamp't's hot path: forward kinematics of
+ * a robot at configurations q, robot-vs-environment and robot self-collision
+ * over triangle-mesh BVHs, planner edge checks, and signed distance with its
+ * gradient.  Every entry point is `extern "C"`, takes plain pointers and
+ * sizes, returns a status code and never lets a C++ exception cross.  Query
+ * entry points take caller-owned DEVICE buffers and a CUDA stream and are
+ * asynchronous on that stream; the `_host` variants take host buffers and
+ * return when the results are in them.
+ *
+ * Each declaration names the reference interface it replaces (paths are
+ * relative to the Klamp't source tree).  The reference reaches these through
+ * KrisLibrary (UpdateFrames / AnyCollisionQuery / EpsilonEdgeChecker), which
+ * is not part of the Klamp't tree; the call sites cited below are where
+ * Klamp't binds them.
+ *
+ * Conventions
+ *   - Rigid transforms are 12 doubles (or floats): rotation row-major R[3*r+c]
+ *     then translation t.  (Klamp't's Python so3/se3 lists are column-major;
+ *     the Python layer converts.)
+ *   - A robot has one DOF per link, as a Klamp't RobotModel does: q has
+ *     num_links entries.
+ *   - Environment objects carry a group id.  Group 0 holds rigid objects and
+ *     group 1 terrains; others are free for the caller.  Each link has a
+ *     32-bit mask of the groups it is checked against.
+ */
+#ifndef KGPU_H
+#define KGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (Python/klampt/src/robotsim.i:41-53 maps the reference's
+ *      PyException to RuntimeError; these codes are what the Python layer
+ *      maps the same way) ---------------------------------------------------- */
+typedef int32_t kgpu_status;
+#define KGPU_OK 0
+#define KGPU_ERR_INVALID 1     /* bad argument: null handle, size, index        */
+#define KGPU_ERR_CUDA 2        /* a CUDA runtime call failed                     */
+#define KGPU_ERR_OOM 3         /* device or pinned allocation failed             */
+#define KGPU_ERR_OVERFLOW 4    /* traversal stack spill area exhausted           */
+#define KGPU_ERR_TIMEOUT 5     /* a bounded device-side wait ran out             */
+#define KGPU_ERR_NOT_FINITE 6  /* NaN/Inf (or |q| >= 1e6) in a configuration     */
+#define KGPU_ERR_EMPTY 7       /* query on empty geometry (robotsim.cpp:1786-1787) */
+#define KGPU_ERR_UNSUPPORTED 8 /* feature not available for this input           */
+
+#define KGPU_GROUP_RIGID_OBJECT 0
+#define KGPU_GROUP_TERRAIN 1
+
+#define KGPU_JOINT_REVOLUTE 0
+#define KGPU_JOINT_PRISMATIC 1
+#define KGPU_JOINT_WELD 2
+
+#define KGPU_MAX_LINKS 32
+
+typedef struct kgpu_robot_s* kgpu_robot;
+typedef struct kgpu_env_s* kgpu_env;
+typedef struct kgpu_world_s* kgpu_world;
+typedef struct kgpu_edge_plan_s* kgpu_edge_plan;
+typedef void* kgpu_stream; /* cudaStream_t; NULL selects the legacy default stream */
+
+/* Robot model: links in topological order (parent index < link index, -1 =
+ * attached to the world), Cpp/docs/Manual-Modeling.md:59,107.  Replaces the
+ * model that Klampt::RobotModel::LoadRob builds (Cpp/Modeling/Robot.cpp:216,
+ * T0_Parent/axes/types at :961-973, geommargin :1048-1051, self-collision
+ * pairs :1275-1380). */
+typedef struct {
+  int32_t num_links;          /* 1..KGPU_MAX_LINKS                              */
+  const int32_t* parents;     /* [num_links]                                    */
+  const int32_t* joint_types; /* [num_links] KGPU_JOINT_*                       */
+  const double* T0_parent;    /* [num_links*12] link frame in parent frame      */
+  const double* axes;         /* [num_links*3] unit joint axis (link frame)     */
+  const double* qmin;         /* [num_links]                                    */
+  const double* qmax;         /* [num_links]                                    */
+  const int32_t* vert_offset; /* [num_links+1] into verts (vertex units)        */
+  const double* verts;        /* link-local vertex coordinates, 3 per vertex    */
+  const int32_t* tri_offset;  /* [num_links+1] into tris (triangle units)       */
+  const int32_t* tris;        /* 3 vertex indices per triangle, local to link   */
+  const double* margins;     /* [num_links] collision margin, or NULL (= 0)     */
+  const uint8_t* self_mask;  /* [num_links*num_links], entry [i*n+j] (i<j) != 0
+                                enables pair (i,j); NULL = every pair except
+                                link-parent (Cpp/docs/Manual-FileTypes.md:212) */
+} kgpu_robot_desc;
+
+/* Static environment: rigid objects and terrains, vertices in world frame.
+ * Replaces the geometry that WorldModel::InitCollisions hands to the
+ * collision queries (Cpp/Modeling/World.cpp:266-274). */
+typedef struct {
+  int32_t num_objects;
+  const int32_t* vert_offset; /* [num_objects+1] */
+  const double* verts;        /* world-frame coordinates */
+  const int32_t* tri_offset;  /* [num_objects+1] */
+  const int32_t* tris;        /* per-object vertex indices */
+  const int32_t* groups;      /* [num_objects] in 0..31, or NULL (= 0) */
+  const uint8_t* convex;      /* [num_objects] 1 = closed convex mesh (enables
+                                 signed distance), or NULL (= none) */
+  const double* margins;      /* [num_objects] or NULL (= 0) */
+} kgpu_env_desc;
+
+typedef struct {
+  uint64_t items;          /* configurations (or edge steps) examined          */
+  uint64_t node_pairs;     /* BVH node pairs tested in FP32                     */
+  uint64_t tri_pairs;      /* triangle pairs tested in FP32                     */
+  uint64_t band_pairs;     /* triangle pairs re-tested in FP64                  */
+  uint64_t spills;         /* traversal stack spills to global memory           */
+} kgpu_stats;
+
+/* ---- model construction --------------------------------------------------- */
+
+/* Builds link BVHs on the host and uploads them.  Replaces RobotModel
+ * construction + InitCollisions for the robot's links
+ * (Python/klampt/src/robotsim.cpp:4118-4165). */
+kgpu_status kgpu_robot_create(const kgpu_robot_desc* desc, kgpu_robot* out);
+kgpu_status kgpu_robot_destroy(kgpu_robot robot);
+
+/* Builds the environment BVHs (one per object group, plus per-object trees
+ * for distance queries) and uploads them.  Replaces WorldModel geometry
+ * initialisation (Cpp/Modeling/World.cpp:266-284). */
+kgpu_status kgpu_env_create(const kgpu_env_desc* desc, kgpu_env* out);
+kgpu_status kgpu_env_destroy(kgpu_env env);
+
+/* Joins an environment and robots.  Collision masks start at Klamp't's
+ * defaults: WorldPlannerSettings::InitializeDefault
+ * (Cpp/Planning/PlannerSettings.cpp:16-42) — every link against every rigid
+ * object, links whose parent is -1 not against terrains, self pairs as in the
+ * robot description.  The world keeps references; destroy it before its
+ * robots and environment. */
+kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t num_robots,
+                              kgpu_world* out);
+kgpu_status kgpu_world_destroy(kgpu_world world);
+
+/* Per-link group mask, the analogue of WorldPlannerSettings::collisionEnabled
+ * rows (PlannerSettings.cpp:16-42) and WorldCollider.ignoreCollision
+ * (Python/klampt/model/collide.py:314-362). */
+kgpu_status kgpu_world_set_link_env_mask(kgpu_world world, int32_t robot, int32_t link,
+                                         uint32_t group_mask);
+/* Enables or disables self-collision testing of link pair (i,j), as
+ * RobotModel::enableSelfCollision (robotsim.cpp:5513-5527). */
+kgpu_status kgpu_world_enable_self_pair(kgpu_world world, int32_t robot, int32_t i, int32_t j,
+                                        int32_t enabled);
+
+/* Named tuning options: "eps_band" (m), "warps_per_block", "blocks_per_sm",
+ * "dist_band" (m).  Unknown names are KGPU_ERR_INVALID. */
+kgpu_status kgpu_world_set_option(kgpu_world world, const char* name, double value);
+kgpu_status kgpu_world_get_option(kgpu_world world, const char* name, double* value);
+
+/* Waits for the stream, then returns (and clears) the status word that the
+ * world's kernels set on the device (overflow, non-finite input, timeout). */
+kgpu_status kgpu_world_sync(kgpu_world world, kgpu_stream stream);
+kgpu_status kgpu_world_get_stats(kgpu_world world, kgpu_stats* out);
+kgpu_status kgpu_world_reset_stats(kgpu_world world);
+
+/* ---- queries (device buffers, asynchronous on `stream`) ------------------- */
+
+/* Forward kinematics.  Replaces RobotModel::setConfig -> UpdateFrames
+ * (Python/klampt/src/robotsim.cpp:5311-5321).  q: [B*num_links] float,
+ * T_out: [B*num_links*12] float world transforms. */
+kgpu_status kgpu_fk(kgpu_world world, int32_t robot, const float* q, int32_t B, float* T_out,
+                    kgpu_stream stream);
+
+/* Environment and self collision verdicts of B configurations, FP32 BVH
+ * traversal with the FP64 band re-test.  Replaces, per configuration,
+ * WorldPlannerSettings::CheckCollision(world, {robot}, others)
+ * (PlannerSettings.cpp:269-331) and RobotModel::selfCollides
+ * (robotsim.cpp:5529-5539).  env_hit/self_hit: [B] bytes (0/1); either may be
+ * NULL to skip that test. */
+kgpu_status kgpu_check_configs(kgpu_world world, int32_t robot, const float* q, int32_t B,
+                               uint8_t* env_hit, uint8_t* self_hit, kgpu_stream stream);
+
+/* Heterogeneous batch: configuration b belongs to robot robot_ids[b] and its
+ * joint values start at q + b*q_stride.  One launch for all robots. */
+kgpu_status kgpu_check_configs_multi(kgpu_world world, const int32_t* robot_ids, const float* q,
+                                     int32_t q_stride, int32_t B, uint8_t* env_hit,
+                                     uint8_t* self_hit, kgpu_stream stream);
+
+/* Feasibility: joint limits, then environment, then self collision, as
+ * SingleRobotCSpace::IsFeasible (Cpp/Planning/RobotCSpace.cpp:786-823).
+ * feasible: [B] bytes. */
+kgpu_status kgpu_is_feasible(kgpu_world world, int32_t robot, const float* q, int32_t B,
+                             uint8_t* feasible, kgpu_stream stream);
+
+/* Straight-line edge checks: edge e is discretised into configurations
+ * q_k = qa + (k/n)(qb-qa), k = 0..n (n = nsteps[e] >= 1), and first_hit[e] is
+ * the smallest k whose configuration is infeasible (-1 when all are
+ * feasible).  Replaces EpsilonEdgeChecker / BisectionEpsilonEdgePlanner
+ * visibility tests (Cpp/Planning/RobotCSpace.cpp:835-840,
+ * Python/klampt/src/motionplanning.cpp:383-400) with interpolation as
+ * Cpp/Modeling/Interpolate.cpp:10-14.  One persistent launch over all steps
+ * of all edges. */
+kgpu_status kgpu_check_edges(kgpu_world world, int32_t robot, const float* qa, const float* qb,
+                             const int32_t* nsteps, int32_t E, int32_t* first_hit,
+                             kgpu_stream stream);
+
+/* The same outputs computed by the plain FP64 method: one thread per
+ * configuration, FP64 forward kinematics, FP64 traversal and triangle tests,
+ * no batching machinery.  The comparison baseline for the engine. */
+kgpu_status kgpu_check_configs_plain64(kgpu_world world, int32_t robot, const float* q, int32_t B,
+                                       uint8_t* env_hit, uint8_t* self_hit, kgpu_stream stream);
+kgpu_status kgpu_check_edges_plain64(kgpu_world world, int32_t robot, const float* qa,
+                                     const float* qb, const int32_t* nsteps, int32_t E,
+                                     int32_t* first_hit, kgpu_stream stream);
+
+/* Minimum signed link-obstacle distance per configuration, clamped at
+ * `cutoff`, with its gradient d/dq.  Replaces the per-pair
+ * Geometry3D::distance_ext loop (robotsim.cpp:1782-1819, settings
+ * upperBound = cutoff) and WorldPlannerSettings::DistanceLowerBound
+ * (PlannerSettings.cpp:372-483).  d: [B] (cutoff when nothing is closer),
+ * pair: [B*2] (link, object) or (-1,-1), cp: [B*6] closest points in world
+ * frame (link side, object side), grad: [B*num_links] (may be NULL). */
+kgpu_status kgpu_distance(kgpu_world world, int32_t robot, const float* q, int32_t B,
+                          double cutoff, double* d, int32_t* pair, double* cp, float* grad,
+                          kgpu_stream stream);
+
+/* Soft-min over all (waypoint, link, object) pairs of a trajectory of the
+ * signed distance, L = -tau * log sum exp(-d/tau), and dL/dq by the adjoint
+ * kernel.  Replaces geometry_ad.MinDistance + pytorch.ADModule backward
+ * (Python/klampt/math/autodiff/geometry_ad.py:613-814,
+ * Python/klampt/math/autodiff/pytorch.py:72-115).  q: [T*W*num_links],
+ * L: [T], dLdq: [T*W*num_links] (may be NULL). */
+kgpu_status kgpu_softmin_grad(kgpu_world world, int32_t robot, const float* q, int32_t T,
+                              int32_t W, double tau, double* L, float* dLdq, kgpu_stream stream);
+
+/* ---- host-buffer variants (pinned staging inside; synchronous) ------------ */
+kgpu_status kgpu_check_configs_host(kgpu_world world, int32_t robot, const float* q, int32_t B,
+                                    uint8_t* env_hit, uint8_t* self_hit);
+kgpu_status kgpu_check_edges_host(kgpu_world world, int32_t robot, const float* qa,
+                                  const float* qb, const int32_t* nsteps, int32_t E,
+                                  int32_t* first_hit);
+
+/* ---- captured edge-check plans (CUDA-graph replay) ------------------------ */
+/* Records the whole edge-check pipeline for fixed device buffers into a CUDA
+ * graph; each launch replays it on `stream`. */
+kgpu_status kgpu_edge_plan_create(kgpu_world world, int32_t robot, const float* qa,
+                                  const float* qb, const int32_t* nsteps, int32_t E,
+                                  int32_t* first_hit, kgpu_edge_plan* out);
+kgpu_status kgpu_edge_plan_launch(kgpu_edge_plan plan, kgpu_stream stream);
+kgpu_status kgpu_edge_plan_destroy(kgpu_edge_plan plan);
+
+/* ---- diagnostics ------------------------------------------------------------ */
+/* Last error message of the calling thread ("" when none). */
+const char* kgpu_last_error(void);
+/* Library version string. */
+const char* kgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* KGPU_H */

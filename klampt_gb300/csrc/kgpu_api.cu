@@ -1,0 +1,913 @@
+// kgpu_api.cu — the C ABI of include/kgpu.h: handle construction (host BVH
+// build + upload), argument validation, launches, device status words,
+// host-buffer variants and CUDA-graph edge plans.
+//
+// Error behaviour mirrors the reference's binding layer: where Klamp't throws
+// PyException (mapped to RuntimeError by Python/klampt/src/robotsim.i:41-53),
+// e.g. a configuration of the wrong size (robotsim.cpp:5314-5316), these
+// functions return a status code and record a message for kgpu_last_error().
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "../../include/kgpu_exact.h"
+#include "kgpu_internal.h"
+
+using namespace kgpu;
+
+namespace kgpu {
+cudaError_t engine_init();
+size_t engine_smem_per_warp();
+}
+
+namespace {
+
+thread_local std::string g_err;
+
+kgpu_status fail(kgpu_status code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
+kgpu_status fail(kgpu_status code, const char* fmt, ...)
+{
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return code;
+}
+
+kgpu_status cuda_fail(cudaError_t e, const char* what)
+{
+  return fail(e == cudaErrorMemoryAllocation ? KGPU_ERR_OOM : KGPU_ERR_CUDA, "%s: %s", what,
+              cudaGetErrorString(e));
+}
+
+#define CK(call)                                   \
+  do {                                             \
+    cudaError_t _e = (call);                       \
+    if (_e != cudaSuccess) return cuda_fail(_e, #call); \
+  } while (0)
+
+template <class T>
+cudaError_t upload(T** dst, const T* src, size_t n)
+{
+  *dst = nullptr;
+  if (n == 0) return cudaSuccess;
+  cudaError_t e = cudaMalloc((void**)dst, n * sizeof(T));
+  if (e != cudaSuccess) return e;
+  return cudaMemcpy(*dst, src, n * sizeof(T), cudaMemcpyHostToDevice);
+}
+
+template <class T>
+void dfree(T*& p)
+{
+  if (p) cudaFree((void*)p);
+  p = nullptr;
+}
+
+inline float round_up_f(double x)
+{
+  float f = (float)x;
+  if ((double)f < x) f = std::nextafter(f, 1e30f);
+  return f;
+}
+
+inline float as_float(int i)
+{
+  float f;
+  memcpy(&f, &i, 4);
+  return f;
+}
+inline int as_int(float f)
+{
+  int i;
+  memcpy(&i, &f, 4);
+  return i;
+}
+
+// appends `b` to the concatenated arrays with node/triangle index shifts
+void append_bvh(const HostBvh& b, int node_base, int tri_base, std::vector<KNode>& nodes,
+                std::vector<double>& node64)
+{
+  for (size_t k = 0; k < b.nodes.size(); ++k) {
+    KNode n = b.nodes[k];
+    int cnt = as_int(n.b.w), idx = as_int(n.a.w);
+    n.a.w = as_float(cnt > 0 ? idx + tri_base : idx + node_base);
+    nodes.push_back(n);
+    for (int i = 0; i < 3; ++i) node64.push_back(b.node_c64[3 * k + i]);
+    for (int i = 0; i < 3; ++i) node64.push_back(b.node_h64[3 * k + i]);
+  }
+}
+
+void free_world_device(kgpu_world w)
+{
+  dfree(w->d_robots);
+  dfree(w->d_queries);
+  dfree(w->d_lnodes);
+  dfree(w->d_ltri32);
+  dfree(w->d_ltri64);
+  dfree(w->d_lnode64);
+  dfree(w->d_status);
+  dfree(w->d_stats);
+  dfree(w->scratch.spill);
+  dfree(w->scratch.counters);
+  dfree(w->scratch.edge_hist);
+  dfree(w->scratch.edge_round_off);
+  dfree(w->scratch.edge_perm);
+  dfree(w->scratch.edge_meta);
+  if (w->pinned) cudaFreeHost(w->pinned);
+  w->pinned = nullptr;
+  dfree(w->dstage);
+  if (w->host_stream) cudaStreamDestroy(w->host_stream);
+  w->host_stream = nullptr;
+}
+
+// (re)builds the per-robot device tables and query lists
+kgpu_status refresh_tables(kgpu_world w)
+{
+  if (!w->tables_dirty) return KGPU_OK;
+  std::vector<KRobotDev> rd(w->robots.size());
+  std::vector<uint32_t> queries;
+  kgpu_env env = w->env;
+  for (size_t r = 0; r < w->robots.size(); ++r) {
+    kgpu_robot R = w->robots[r];
+    KRobotDev& d = rd[r];
+    memset(&d, 0, sizeof d);
+    d.nlinks = R->nlinks;
+    int node_base = w->robot_node_base[r];
+    int depth_max = 0;
+    for (int i = 0; i < R->nlinks; ++i) {
+      d.parents[i] = R->parents[i];
+      d.jtype[i] = R->jtypes[i];
+      d.link_root[i] = R->bvh[i].nodes.empty() ? -1 : node_base;
+      node_base += (int)R->bvh[i].nodes.size();
+      int dep = 0;
+      for (int j = i; j >= 0; j = R->parents[j]) ++dep;
+      d.link_depth[i] = dep;
+      depth_max = dep > depth_max ? dep : depth_max;
+      d.env_mask[i] = w->env_mask[r][i];
+      d.link_margin[i] = round_up_f(R->margins[i]);
+      d.link_margin64[i] = R->margins[i];
+      d.qmin[i] = (float)R->qmin[i];
+      d.qmax[i] = (float)R->qmax[i];
+      d.qmin64[i] = R->qmin[i];
+      d.qmax64[i] = R->qmax[i];
+      for (int k = 0; k < 12; ++k) {
+        d.T0P[i][k] = (float)R->T0P[12 * i + k];
+        d.T0P64[i][k] = R->T0P[12 * i + k];
+      }
+      for (int k = 0; k < 3; ++k) {
+        d.axis[i][k] = (float)R->axes[3 * i + k];
+        d.axis64[i][k] = R->axes[3 * i + k];
+      }
+    }
+    d.query_off = (int)queries.size();
+    for (int i = 0; i < R->nlinks; ++i) {
+      if (d.link_root[i] < 0) continue;
+      for (int g = 0; g < kMaxGroups; ++g)
+        if (((d.env_mask[i] >> g) & 1u) && env && env->group_root[g] >= 0) {
+          queries.push_back((uint32_t)i | ((uint32_t)(32 + g) << 8));
+          d.nqueries_env++;
+        }
+    }
+    for (int i = 0; i < R->nlinks; ++i)
+      for (int j = i + 1; j < R->nlinks; ++j)
+        if (w->self_enabled[r][i * R->nlinks + j] && d.link_root[i] >= 0 && d.link_root[j] >= 0) {
+          queries.push_back((uint32_t)i | ((uint32_t)j << 8));
+          d.nqueries_self++;
+        }
+  }
+  dfree(w->d_robots);
+  dfree(w->d_queries);
+  CK(upload(&w->d_robots, rd.data(), rd.size()));
+  if (queries.empty()) queries.push_back(0);
+  CK(upload(&w->d_queries, queries.data(), queries.size()));
+  w->dev.robots = w->d_robots;
+  w->dev.queries = w->d_queries;
+  w->tables_dirty = false;
+  return KGPU_OK;
+}
+
+int grid_blocks(kgpu_world w) { return w->num_sms * w->blocks_per_sm; }
+
+kgpu_status ensure_edge_scratch(kgpu_world w, int E)
+{
+  if ((size_t)E <= w->scratch.edge_cap) return KGPU_OK;
+  dfree(w->scratch.edge_perm);
+  size_t cap = (size_t)E < 1024 ? 1024 : (size_t)E;
+  CK(cudaMalloc((void**)&w->scratch.edge_perm, cap * sizeof(int)));
+  w->scratch.edge_cap = cap;
+  return KGPU_OK;
+}
+
+kgpu_status check_world(kgpu_world w, int robot)
+{
+  if (!w) return fail(KGPU_ERR_INVALID, "null world");
+  if (robot < 0 || robot >= (int)w->robots.size())
+    return fail(KGPU_ERR_INVALID, "robot index %d out of range [0,%d)", robot, (int)w->robots.size());
+  return refresh_tables(w);
+}
+
+kgpu_status launch_status(cudaError_t e, const char* what)
+{
+  if (e != cudaSuccess) return cuda_fail(e, what);
+  return KGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* kgpu_last_error(void) { return g_err.c_str(); }
+const char* kgpu_version(void) { return "kgpu 0.1 (sm_103a)"; }
+
+kgpu_status kgpu_robot_create(const kgpu_robot_desc* d, kgpu_robot* out)
+{
+  if (!d || !out) return fail(KGPU_ERR_INVALID, "null argument");
+  *out = nullptr;
+  int L = d->num_links;
+  if (L < 1 || L > KGPU_MAX_LINKS)
+    return fail(KGPU_ERR_INVALID, "num_links %d outside [1,%d]", L, KGPU_MAX_LINKS);
+  if (!d->parents || !d->joint_types || !d->T0_parent || !d->axes || !d->qmin || !d->qmax ||
+      !d->vert_offset || !d->tri_offset)
+    return fail(KGPU_ERR_INVALID, "robot description has a null array");
+  kgpu_robot R = new (std::nothrow) kgpu_robot_s();
+  if (!R) return fail(KGPU_ERR_OOM, "host allocation");
+  R->nlinks = L;
+  R->parents.assign(d->parents, d->parents + L);
+  R->jtypes.assign(d->joint_types, d->joint_types + L);
+  R->T0P.assign(d->T0_parent, d->T0_parent + 12 * L);
+  R->axes.assign(d->axes, d->axes + 3 * L);
+  R->qmin.assign(d->qmin, d->qmin + L);
+  R->qmax.assign(d->qmax, d->qmax + L);
+  R->margins.assign(L, 0.0);
+  if (d->margins) R->margins.assign(d->margins, d->margins + L);
+  for (int i = 0; i < L; ++i) {
+    if (R->parents[i] >= i || R->parents[i] < -1) {
+      delete R;
+      return fail(KGPU_ERR_INVALID, "link %d: parent %d must be -1 or a smaller index", i, R->parents[i]);
+    }
+    if (R->jtypes[i] < 0 || R->jtypes[i] > 2) {
+      delete R;
+      return fail(KGPU_ERR_INVALID, "link %d: joint type %d unknown", i, R->jtypes[i]);
+    }
+    double n2 = R->axes[3 * i] * R->axes[3 * i] + R->axes[3 * i + 1] * R->axes[3 * i + 1] +
+                R->axes[3 * i + 2] * R->axes[3 * i + 2];
+    if (R->jtypes[i] != KGPU_JOINT_WELD && std::fabs(n2 - 1.0) > 1e-9) {
+      delete R;
+      return fail(KGPU_ERR_INVALID, "link %d: joint axis is not a unit vector", i);
+    }
+    if (!(R->qmin[i] <= R->qmax[i]) || R->margins[i] < 0) {
+      delete R;
+      return fail(KGPU_ERR_INVALID, "link %d: bad joint limits or negative margin", i);
+    }
+  }
+  R->self_mask.assign(L * L, 0);
+  for (int i = 0; i < L; ++i)
+    for (int j = i + 1; j < L; ++j) {
+      if (d->self_mask) R->self_mask[i * L + j] = d->self_mask[i * L + j] ? 1 : 0;
+      else R->self_mask[i * L + j] = (R->parents[j] != i && R->parents[i] != j) ? 1 : 0;
+    }
+  R->bvh.resize(L);
+  R->tri64.resize(L);
+  R->link_tri_count.assign(L, 0);
+  double reach_link = 0.0;
+  for (int l = 0; l < L; ++l) {
+    int v0 = d->vert_offset[l], v1 = d->vert_offset[l + 1];
+    int t0 = d->tri_offset[l], t1 = d->tri_offset[l + 1];
+    if (v1 < v0 || t1 < t0 || (t1 > t0 && (!d->verts || !d->tris))) {
+      delete R;
+      return fail(KGPU_ERR_INVALID, "link %d: bad mesh offsets", l);
+    }
+    int nt = t1 - t0, nv = v1 - v0;
+    std::vector<double> tri(9 * (size_t)nt);
+    for (int t = 0; t < nt; ++t)
+      for (int v = 0; v < 3; ++v) {
+        int vi = d->tris[3 * (size_t)(t0 + t) + v];
+        if (vi < 0 || vi >= nv) {
+          delete R;
+          return fail(KGPU_ERR_INVALID, "link %d triangle %d: vertex index %d out of range", l, t, vi);
+        }
+        for (int i = 0; i < 3; ++i) {
+          double x = d->verts[3 * (size_t)(v0 + vi) + i];
+          if (!std::isfinite(x)) {
+            delete R;
+            return fail(KGPU_ERR_NOT_FINITE, "link %d: non-finite vertex", l);
+          }
+          tri[9 * (size_t)t + 3 * v + i] = x;
+        }
+      }
+    for (size_t k = 0; k < tri.size(); k += 3) {
+      double r = std::sqrt(tri[k] * tri[k] + tri[k + 1] * tri[k + 1] + tri[k + 2] * tri[k + 2]);
+      reach_link = std::max(reach_link, r);
+    }
+    std::vector<int> ids(nt);
+    for (int t = 0; t < nt; ++t) ids[t] = t;
+    build_bvh(tri, ids, nullptr, R->bvh[l]);
+    R->tri64[l].resize(9 * (size_t)nt);
+    for (int k = 0; k < nt; ++k)
+      for (int i = 0; i < 9; ++i) R->tri64[l][9 * (size_t)k + i] = tri[9 * (size_t)R->bvh[l].order[k] + i];
+    R->link_tri_count[l] = nt;
+  }
+  double chain = 0.0;
+  for (int i = 0; i < L; ++i)
+    chain += std::sqrt(R->T0P[12 * i + 9] * R->T0P[12 * i + 9] + R->T0P[12 * i + 10] * R->T0P[12 * i + 10] +
+                       R->T0P[12 * i + 11] * R->T0P[12 * i + 11]);
+  R->reach = chain + reach_link;
+  *out = R;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_robot_destroy(kgpu_robot r)
+{
+  delete r;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_env_create(const kgpu_env_desc* d, kgpu_env* out)
+{
+  if (!d || !out) return fail(KGPU_ERR_INVALID, "null argument");
+  *out = nullptr;
+  int N = d->num_objects;
+  if (N < 0 || (N > 0 && (!d->vert_offset || !d->tri_offset)))
+    return fail(KGPU_ERR_INVALID, "bad environment description");
+  kgpu_env E = new (std::nothrow) kgpu_env_s();
+  if (!E) return fail(KGPU_ERR_OOM, "host allocation");
+  E->nobj = N;
+  E->groups.assign(N, 0);
+  if (d->groups) E->groups.assign(d->groups, d->groups + N);
+  E->convex.assign(N, 0);
+  if (d->convex) E->convex.assign(d->convex, d->convex + N);
+  E->margins.assign(N, 0.0);
+  if (d->margins) E->margins.assign(d->margins, d->margins + N);
+  size_t ntot = N > 0 ? (size_t)d->tri_offset[N] : 0;
+  E->tri64.resize(9 * ntot);
+  E->tri_obj.resize(ntot);
+  for (int o = 0; o < N; ++o) {
+    if (E->groups[o] < 0 || E->groups[o] >= kMaxGroups || E->margins[o] < 0) {
+      delete E;
+      return fail(KGPU_ERR_INVALID, "object %d: bad group or margin", o);
+    }
+    int v0 = d->vert_offset[o], v1 = d->vert_offset[o + 1];
+    int nv = v1 - v0;
+    for (int t = d->tri_offset[o]; t < d->tri_offset[o + 1]; ++t) {
+      E->tri_obj[t] = o;
+      for (int v = 0; v < 3; ++v) {
+        int vi = d->tris[3 * (size_t)t + v];
+        if (vi < 0 || vi >= nv) {
+          delete E;
+          return fail(KGPU_ERR_INVALID, "object %d: vertex index out of range", o);
+        }
+        for (int i = 0; i < 3; ++i) {
+          double x = d->verts[3 * ((size_t)v0 + vi) + i];
+          if (!std::isfinite(x)) {
+            delete E;
+            return fail(KGPU_ERR_NOT_FINITE, "object %d: non-finite vertex", o);
+          }
+          E->tri64[9 * (size_t)t + 3 * v + i] = x;
+          E->extent = std::max(E->extent, std::fabs(x));
+        }
+      }
+    }
+  }
+  // per-group object-aware trees, concatenated
+  std::vector<KNode> nodes;
+  std::vector<double> node64;
+  std::vector<int> node_obj, leaf_tris;
+  std::vector<int> obj_root(N, -1);
+  for (int g = 0; g < kMaxGroups; ++g) {
+    E->group_root[g] = -1;
+    E->group_margin[g] = 0.f;
+    std::vector<int> ids;
+    double gm = 0.0;
+    for (int o = 0; o < N; ++o)
+      if (E->groups[o] == g) {
+        gm = std::max(gm, E->margins[o]);
+        for (int t = d->tri_offset[o]; t < d->tri_offset[o + 1]; ++t) ids.push_back(t);
+      }
+    if (ids.empty()) continue;
+    HostBvh& b = E->gbvh[g];
+    build_bvh(E->tri64, ids, &E->tri_obj, b);
+    int node_base = (int)nodes.size(), tri_base = (int)leaf_tris.size();
+    append_bvh(b, node_base, tri_base, nodes, node64);
+    for (size_t k = 0; k < b.nodes.size(); ++k) {
+      int o = b.node_obj[k];
+      node_obj.push_back(o);
+      // the first (shallowest) node owned by an object is its root: nodes are
+      // appended parent-before-child, so the first occurrence wins
+      if (o >= 0 && obj_root[o] < 0) obj_root[o] = node_base + (int)k;
+    }
+    for (int t : b.order) leaf_tris.push_back(t);
+    E->group_root[g] = node_base;
+    E->group_margin[g] = round_up_f(gm);
+  }
+  E->n_nodes = nodes.size();
+  E->n_tris = leaf_tris.size();
+  std::vector<float4> tri32(3 * leaf_tris.size());
+  std::vector<double> tri64l(9 * leaf_tris.size());
+  std::vector<int> tobj(leaf_tris.size());
+  for (size_t k = 0; k < leaf_tris.size(); ++k) {
+    int t = leaf_tris[k];
+    for (int v = 0; v < 3; ++v)
+      tri32[3 * k + v] = make_float4((float)E->tri64[9 * (size_t)t + 3 * v], (float)E->tri64[9 * (size_t)t + 3 * v + 1],
+                                     (float)E->tri64[9 * (size_t)t + 3 * v + 2], 0.f);
+    for (int i = 0; i < 9; ++i) tri64l[9 * k + i] = E->tri64[9 * (size_t)t + i];
+    tobj[k] = E->tri_obj[t];
+  }
+  std::vector<float> om(N);
+  std::vector<double> om64(N);
+  for (int o = 0; o < N; ++o) {
+    om[o] = round_up_f(E->margins[o]);
+    om64[o] = E->margins[o];
+  }
+  cudaError_t e = cudaSuccess;
+  if (e == cudaSuccess) e = upload(&E->d_nodes, nodes.data(), nodes.size());
+  if (e == cudaSuccess) e = upload(&E->d_node64, node64.data(), node64.size());
+  if (e == cudaSuccess) e = upload(&E->d_tri32, tri32.data(), tri32.size());
+  if (e == cudaSuccess) e = upload(&E->d_tri64, tri64l.data(), tri64l.size());
+  if (e == cudaSuccess) e = upload(&E->d_tri_obj, tobj.data(), tobj.size());
+  if (e == cudaSuccess) e = upload(&E->d_obj_margin, om.data(), om.size());
+  if (e == cudaSuccess) e = upload(&E->d_obj_margin64, om64.data(), om64.size());
+  if (e == cudaSuccess) e = upload(&E->d_obj_root, obj_root.data(), obj_root.size());
+  if (e == cudaSuccess) e = upload(&E->d_obj_group, E->groups.data(), E->groups.size());
+  if (e == cudaSuccess) e = upload(&E->d_obj_convex, E->convex.data(), E->convex.size());
+  if (e == cudaSuccess) e = upload(&E->d_node_obj, node_obj.data(), node_obj.size());
+  if (e != cudaSuccess) {
+    kgpu_env_destroy(E);
+    return cuda_fail(e, "environment upload");
+  }
+  *out = E;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_env_destroy(kgpu_env E)
+{
+  if (!E) return KGPU_OK;
+  dfree(E->d_nodes);
+  dfree(E->d_node64);
+  dfree(E->d_tri32);
+  dfree(E->d_tri64);
+  dfree(E->d_tri_obj);
+  dfree(E->d_obj_margin);
+  dfree(E->d_obj_margin64);
+  dfree(E->d_obj_root);
+  dfree(E->d_obj_group);
+  dfree(E->d_obj_convex);
+  dfree(E->d_node_obj);
+  delete E;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n, kgpu_world* out)
+{
+  if (!out || n < 0 || (n > 0 && !robots)) return fail(KGPU_ERR_INVALID, "bad arguments");
+  *out = nullptr;
+  for (int r = 0; r < n; ++r)
+    if (!robots[r]) return fail(KGPU_ERR_INVALID, "null robot %d", r);
+  kgpu_world w = new (std::nothrow) kgpu_world_s();
+  if (!w) return fail(KGPU_ERR_OOM, "host allocation");
+  w->env = env;
+  w->robots.assign(robots, robots + n);
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&w->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = engine_init();
+  if (e != cudaSuccess) {
+    delete w;
+    return cuda_fail(e, "device query");
+  }
+  // link BVHs of every robot, concatenated
+  std::vector<KNode> nodes;
+  std::vector<double> node64, tri64;
+  std::vector<float4> tri32;
+  double reach = 0.0;
+  for (int r = 0; r < n; ++r) {
+    kgpu_robot R = robots[r];
+    w->robot_node_base.push_back((int)nodes.size());
+    w->robot_tri_base.push_back((int)(tri32.size() / 3));
+    for (int l = 0; l < R->nlinks; ++l) {
+      append_bvh(R->bvh[l], (int)nodes.size(), (int)(tri32.size() / 3), nodes, node64);
+      for (size_t k = 0; k < R->tri64[l].size(); k += 3)
+        tri32.push_back(make_float4((float)R->tri64[l][k], (float)R->tri64[l][k + 1], (float)R->tri64[l][k + 2], 0.f));
+      tri64.insert(tri64.end(), R->tri64[l].begin(), R->tri64[l].end());
+    }
+    reach = std::max(reach, R->reach);
+    std::vector<uint32_t> mask(R->nlinks, 0xffffffffu);
+    for (int l = 0; l < R->nlinks; ++l)
+      if (R->parents[l] < 0) mask[l] &= ~(1u << KGPU_GROUP_TERRAIN);
+    w->env_mask.push_back(mask);
+    w->self_enabled.push_back(R->self_mask);
+  }
+  if (nodes.size() >= (1u << 20) || tri32.size() / 3 >= (1u << 28)) {
+    delete w;
+    return fail(KGPU_ERR_UNSUPPORTED, "link BVHs exceed 2^20 nodes");
+  }
+  if (nodes.empty()) nodes.push_back(KNode());
+  if (tri32.empty()) tri32.resize(3);
+  if (tri64.empty()) tri64.resize(9);
+  if (node64.empty()) node64.resize(6);
+  e = cudaSuccess;
+  if (e == cudaSuccess) e = upload(&w->d_lnodes, nodes.data(), nodes.size());
+  if (e == cudaSuccess) e = upload(&w->d_lnode64, node64.data(), node64.size());
+  if (e == cudaSuccess) e = upload(&w->d_ltri32, tri32.data(), tri32.size());
+  if (e == cudaSuccess) e = upload(&w->d_ltri64, tri64.data(), tri64.size());
+  if (e == cudaSuccess) e = cudaMalloc((void**)&w->d_status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(w->d_status, 0, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&w->d_stats, 8 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(w->d_stats, 0, 8 * sizeof(unsigned long long));
+  // scratch: per-warp spill stacks, queue heads, edge ordering tables
+  Scratch& S = w->scratch;
+  S.max_warps = w->num_sms * 4 * 16;  // up to 4 blocks/SM of 16 warps
+  S.spill_per_warp = 8192;
+  if (e == cudaSuccess) e = cudaMalloc((void**)&S.spill, (size_t)S.max_warps * S.spill_per_warp * sizeof(uint2));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&S.counters, 64 * sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_hist, (kMaxSteps + 2) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_round_off, (kMaxSteps + 2) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_meta, (4 + kMaxSteps + 2) * sizeof(int));
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w->host_stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) {
+    free_world_device(w);
+    delete w;
+    return cuda_fail(e, "world allocation");
+  }
+  // eps_band: bound on |FP32 - FP64| world coordinates (chain depth x
+  // coordinate magnitude x float epsilon, with a large safety factor)
+  double mag = std::max(reach, env ? env->extent : 0.0) + 1.0;
+  int depth = 1;
+  for (int r = 0; r < n; ++r)
+    for (int l = 0; l < robots[r]->nlinks; ++l) {
+      int dep = 0;
+      for (int j = l; j >= 0; j = robots[r]->parents[j]) ++dep;
+      depth = std::max(depth, dep);
+    }
+  w->eps_band = std::max(1e-5, 64.0 * 5.9604644775390625e-08 * (depth + 4) * mag);
+  KWorldDev& D = w->dev;
+  memset(&D, 0, sizeof D);
+  D.lnodes = w->d_lnodes;
+  D.ltri32 = w->d_ltri32;
+  D.ltri64 = w->d_ltri64;
+  D.lnode64 = w->d_lnode64;
+  if (env) {
+    D.enodes = env->d_nodes;
+    D.etri32 = env->d_tri32;
+    D.etri64 = env->d_tri64;
+    D.enode64 = env->d_node64;
+    D.etri_obj = env->d_tri_obj;
+    D.obj_margin = env->d_obj_margin;
+    D.obj_margin64 = env->d_obj_margin64;
+    D.obj_root = env->d_obj_root;
+    D.obj_group = env->d_obj_group;
+    D.obj_convex = env->d_obj_convex;
+    D.node_obj = env->d_node_obj;
+    D.num_objects = env->nobj;
+    for (int g = 0; g < kMaxGroups; ++g) {
+      D.group_root[g] = env->group_root[g];
+      D.group_margin[g] = env->group_margin[g];
+    }
+  } else {
+    for (int g = 0; g < kMaxGroups; ++g) D.group_root[g] = -1;
+  }
+  D.eps_band = (float)w->eps_band;
+  D.status = w->d_status;
+  D.stats = w->d_stats;
+  w->tables_dirty = true;
+  kgpu_status st = refresh_tables(w);
+  if (st != KGPU_OK) {
+    free_world_device(w);
+    delete w;
+    return st;
+  }
+  *out = w;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_world_destroy(kgpu_world w)
+{
+  if (!w) return KGPU_OK;
+  free_world_device(w);
+  delete w;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_world_set_link_env_mask(kgpu_world w, int32_t robot, int32_t link, uint32_t mask)
+{
+  if (!w || robot < 0 || robot >= (int)w->robots.size()) return fail(KGPU_ERR_INVALID, "bad robot");
+  if (link < 0 || link >= w->robots[robot]->nlinks) return fail(KGPU_ERR_INVALID, "bad link %d", link);
+  w->env_mask[robot][link] = mask;
+  w->tables_dirty = true;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_world_enable_self_pair(kgpu_world w, int32_t robot, int32_t i, int32_t j,
+                                        int32_t enabled)
+{
+  if (!w || robot < 0 || robot >= (int)w->robots.size()) return fail(KGPU_ERR_INVALID, "bad robot");
+  int L = w->robots[robot]->nlinks;
+  if (i < 0 || j < 0 || i >= L || j >= L || i == j) return fail(KGPU_ERR_INVALID, "bad link pair");
+  if (i > j) std::swap(i, j);
+  w->self_enabled[robot][i * L + j] = enabled ? 1 : 0;
+  w->tables_dirty = true;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_world_set_option(kgpu_world w, const char* name, double v)
+{
+  if (!w || !name) return fail(KGPU_ERR_INVALID, "null argument");
+  if (!strcmp(name, "eps_band")) {
+    if (!(v > 0 && v < 1)) return fail(KGPU_ERR_INVALID, "eps_band must be in (0,1)");
+    w->eps_band = v;
+    w->dev.eps_band = (float)v;
+  } else if (!strcmp(name, "warps_per_block")) {
+    int k = (int)v;
+    if (k != 4 && k != 8 && k != 16) return fail(KGPU_ERR_INVALID, "warps_per_block must be 4, 8 or 16");
+    w->warps_per_block = k;
+  } else if (!strcmp(name, "blocks_per_sm")) {
+    int k = (int)v;
+    if (k < 1 || k * w->warps_per_block > 64 || k > 4) return fail(KGPU_ERR_INVALID, "blocks_per_sm out of range");
+    w->blocks_per_sm = k;
+  } else {
+    return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
+  }
+  if (w->num_sms * w->blocks_per_sm * w->warps_per_block > w->scratch.max_warps)
+    return fail(KGPU_ERR_INVALID, "launch shape exceeds the scratch sized at creation");
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_world_get_option(kgpu_world w, const char* name, double* v)
+{
+  if (!w || !name || !v) return fail(KGPU_ERR_INVALID, "null argument");
+  if (!strcmp(name, "eps_band")) *v = w->eps_band;
+  else if (!strcmp(name, "warps_per_block")) *v = w->warps_per_block;
+  else if (!strcmp(name, "blocks_per_sm")) *v = w->blocks_per_sm;
+  else if (!strcmp(name, "num_sms")) *v = w->num_sms;
+  else return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_world_sync(kgpu_world w, kgpu_stream stream)
+{
+  if (!w) return fail(KGPU_ERR_INVALID, "null world");
+  CK(cudaStreamSynchronize((cudaStream_t)stream));
+  int st = 0;
+  CK(cudaMemcpy(&st, w->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st != 0) {
+    CK(cudaMemset(w->d_status, 0, sizeof(int)));
+    const char* what = st == KGPU_ERR_NOT_FINITE ? "non-finite or out-of-range configuration value"
+                       : st == KGPU_ERR_OVERFLOW ? "traversal stack spill area exhausted"
+                       : st == KGPU_ERR_INVALID  ? "invalid step count (must be 1..65535)"
+                       : st == KGPU_ERR_TIMEOUT  ? "bounded device wait ran out"
+                                                 : "device error";
+    return fail(st, "device status: %s", what);
+  }
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_world_get_stats(kgpu_world w, kgpu_stats* out)
+{
+  if (!w || !out) return fail(KGPU_ERR_INVALID, "null argument");
+  unsigned long long s[8];
+  CK(cudaMemcpy(s, w->d_stats, sizeof s, cudaMemcpyDeviceToHost));
+  out->items = s[0];
+  out->node_pairs = s[1];
+  out->tri_pairs = s[2];
+  out->band_pairs = s[3];
+  out->spills = s[4];
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_world_reset_stats(kgpu_world w)
+{
+  if (!w) return fail(KGPU_ERR_INVALID, "null world");
+  CK(cudaMemset(w->d_stats, 0, 8 * sizeof(unsigned long long)));
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_fk(kgpu_world w, int32_t robot, const float* q, int32_t B, float* T, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && (!q || !T))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  return launch_status(launch_fk(w->dev, robot, q, B, T, (cudaStream_t)s), "kgpu_fk");
+}
+
+kgpu_status kgpu_check_configs(kgpu_world w, int32_t robot, const float* q, int32_t B,
+                               uint8_t* env_hit, uint8_t* self_hit, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && !q)) return fail(KGPU_ERR_INVALID, "bad buffers");
+  if (!env_hit && !self_hit) return KGPU_OK;
+  return launch_status(launch_check_configs(w->dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
+                                            env_hit, self_hit, nullptr, grid_blocks(w), w->warps_per_block,
+                                            (cudaStream_t)s),
+                       "kgpu_check_configs");
+}
+
+kgpu_status kgpu_check_configs_multi(kgpu_world w, const int32_t* robot_ids, const float* q,
+                                     int32_t q_stride, int32_t B, uint8_t* env_hit, uint8_t* self_hit,
+                                     kgpu_stream s)
+{
+  if (!w) return fail(KGPU_ERR_INVALID, "null world");
+  kgpu_status st = refresh_tables(w);
+  if (st) return st;
+  int maxl = 0;
+  for (auto R : w->robots) maxl = std::max(maxl, R->nlinks);
+  if (B < 0 || (B > 0 && (!q || !robot_ids)) || q_stride < maxl)
+    return fail(KGPU_ERR_INVALID, "bad buffers or q_stride %d < max links %d", q_stride, maxl);
+  if (!env_hit && !self_hit) return KGPU_OK;
+  return launch_status(launch_check_configs(w->dev, w->scratch, -1, robot_ids, q, q_stride, B, env_hit, self_hit,
+                                            nullptr, grid_blocks(w), w->warps_per_block, (cudaStream_t)s),
+                       "kgpu_check_configs_multi");
+}
+
+kgpu_status kgpu_is_feasible(kgpu_world w, int32_t robot, const float* q, int32_t B, uint8_t* feasible,
+                             kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && (!q || !feasible))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  return launch_status(launch_check_configs(w->dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
+                                            nullptr, nullptr, feasible, grid_blocks(w), w->warps_per_block,
+                                            (cudaStream_t)s),
+                       "kgpu_is_feasible");
+}
+
+kgpu_status kgpu_check_edges(kgpu_world w, int32_t robot, const float* qa, const float* qb,
+                             const int32_t* nsteps, int32_t E, int32_t* first_hit, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (E < 0 || (E > 0 && (!qa || !qb || !nsteps || !first_hit))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  if ((st = ensure_edge_scratch(w, E))) return st;
+  return launch_status(launch_check_edges(w->dev, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
+                                          w->warps_per_block, (cudaStream_t)s),
+                       "kgpu_check_edges");
+}
+
+kgpu_status kgpu_check_configs_plain64(kgpu_world w, int32_t robot, const float* q, int32_t B,
+                                       uint8_t* env_hit, uint8_t* self_hit, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && !q)) return fail(KGPU_ERR_INVALID, "bad buffers");
+  return launch_status(launch_plain64_configs(w->dev, robot, q, B, env_hit, self_hit, (cudaStream_t)s),
+                       "kgpu_check_configs_plain64");
+}
+
+kgpu_status kgpu_check_edges_plain64(kgpu_world w, int32_t robot, const float* qa, const float* qb,
+                                     const int32_t* nsteps, int32_t E, int32_t* first_hit, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (E < 0 || (E > 0 && (!qa || !qb || !nsteps || !first_hit))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  return launch_status(launch_plain64_edges(w->dev, robot, qa, qb, nsteps, E, first_hit, (cudaStream_t)s),
+                       "kgpu_check_edges_plain64");
+}
+
+kgpu_status kgpu_distance(kgpu_world w, int32_t robot, const float* q, int32_t B, double cutoff, double* d,
+                          int32_t* pair, double* cp, float* grad, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && (!q || !d || !pair || !cp))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  if (!(cutoff > 0)) return fail(KGPU_ERR_INVALID, "cutoff must be positive");
+  return launch_status(launch_distance(w->dev, w->scratch, robot, q, B, cutoff, d, pair, cp, grad, grid_blocks(w),
+                                       w->warps_per_block, (cudaStream_t)s),
+                       "kgpu_distance");
+}
+
+kgpu_status kgpu_softmin_grad(kgpu_world w, int32_t robot, const float* q, int32_t T, int32_t Wn, double tau,
+                              double* L, float* dLdq, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (T < 0 || Wn < 1 || (T > 0 && (!q || !L))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  if (!(tau > 0)) return fail(KGPU_ERR_INVALID, "tau must be positive");
+  return launch_status(launch_softmin(w->dev, w->scratch, robot, q, T, Wn, tau, L, dLdq, grid_blocks(w),
+                                      w->warps_per_block, (cudaStream_t)s),
+                       "kgpu_softmin_grad");
+}
+
+// ---- host-buffer variants ----------------------------------------------------
+static kgpu_status ensure_stage(kgpu_world w, size_t bytes)
+{
+  if (bytes <= w->pinned_bytes && bytes <= w->dstage_bytes) return KGPU_OK;
+  size_t cap = bytes < ((size_t)1 << 20) ? ((size_t)1 << 20) : bytes;
+  if (w->pinned) cudaFreeHost(w->pinned);
+  w->pinned = nullptr;
+  w->pinned_bytes = 0;
+  dfree(w->dstage);
+  w->dstage_bytes = 0;
+  CK(cudaMallocHost(&w->pinned, cap));
+  w->pinned_bytes = cap;
+  CK(cudaMalloc(&w->dstage, cap));
+  w->dstage_bytes = cap;
+  return KGPU_OK;
+}
+
+static size_t al(size_t x) { return (x + 255) & ~(size_t)255; }
+
+kgpu_status kgpu_check_configs_host(kgpu_world w, int32_t robot, const float* q, int32_t B, uint8_t* env_hit,
+                                    uint8_t* self_hit)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && !q)) return fail(KGPU_ERR_INVALID, "bad buffers");
+  int L = w->robots[robot]->nlinks;
+  size_t qb = al((size_t)B * L * sizeof(float)), ob = al((size_t)B);
+  if ((st = ensure_stage(w, qb + 2 * ob))) return st;
+  char* hp = (char*)w->pinned;
+  char* dp = (char*)w->dstage;
+  cudaStream_t s = w->host_stream;
+  memcpy(hp, q, (size_t)B * L * sizeof(float));
+  CK(cudaMemcpyAsync(dp, hp, (size_t)B * L * sizeof(float), cudaMemcpyHostToDevice, s));
+  st = kgpu_check_configs(w, robot, (const float*)dp, B, env_hit ? (uint8_t*)(dp + qb) : nullptr,
+                          self_hit ? (uint8_t*)(dp + qb + ob) : nullptr, s);
+  if (st) return st;
+  if (env_hit) CK(cudaMemcpyAsync(hp + qb, dp + qb, B, cudaMemcpyDeviceToHost, s));
+  if (self_hit) CK(cudaMemcpyAsync(hp + qb + ob, dp + qb + ob, B, cudaMemcpyDeviceToHost, s));
+  if ((st = kgpu_world_sync(w, s))) return st;
+  if (env_hit) memcpy(env_hit, hp + qb, B);
+  if (self_hit) memcpy(self_hit, hp + qb + ob, B);
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_check_edges_host(kgpu_world w, int32_t robot, const float* qa, const float* qbuf,
+                                  const int32_t* nsteps, int32_t E, int32_t* first_hit)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (E < 0 || (E > 0 && (!qa || !qbuf || !nsteps || !first_hit))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  int L = w->robots[robot]->nlinks;
+  size_t qbytes = (size_t)E * L * sizeof(float);
+  size_t o1 = al(qbytes), o2 = o1 + al(qbytes), o3 = o2 + al((size_t)E * 4);
+  size_t total = o3 + al((size_t)E * 4);
+  if ((st = ensure_stage(w, total))) return st;
+  char* hp = (char*)w->pinned;
+  char* dp = (char*)w->dstage;
+  cudaStream_t s = w->host_stream;
+  memcpy(hp, qa, qbytes);
+  memcpy(hp + o1, qbuf, qbytes);
+  memcpy(hp + o2, nsteps, (size_t)E * 4);
+  CK(cudaMemcpyAsync(dp, hp, o3, cudaMemcpyHostToDevice, s));
+  st = kgpu_check_edges(w, robot, (const float*)dp, (const float*)(dp + o1), (const int32_t*)(dp + o2), E,
+                        (int32_t*)(dp + o3), s);
+  if (st) return st;
+  CK(cudaMemcpyAsync(hp + o3, dp + o3, (size_t)E * 4, cudaMemcpyDeviceToHost, s));
+  if ((st = kgpu_world_sync(w, s))) return st;
+  memcpy(first_hit, hp + o3, (size_t)E * 4);
+  return KGPU_OK;
+}
+
+// ---- CUDA-graph edge plans ----------------------------------------------------
+kgpu_status kgpu_edge_plan_create(kgpu_world w, int32_t robot, const float* qa, const float* qb,
+                                  const int32_t* nsteps, int32_t E, int32_t* first_hit, kgpu_edge_plan* out)
+{
+  if (!out) return fail(KGPU_ERR_INVALID, "null argument");
+  *out = nullptr;
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (E <= 0 || !qa || !qb || !nsteps || !first_hit) return fail(KGPU_ERR_INVALID, "bad buffers");
+  if ((st = ensure_edge_scratch(w, E))) return st;
+  cudaStream_t cs;
+  CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  kgpu_edge_plan p = new kgpu_edge_plan_s();
+  p->world = w;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t le = launch_check_edges(w->dev, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
+                                        w->warps_per_block, cs);
+    e = cudaStreamEndCapture(cs, &p->graph);
+    if (e == cudaSuccess && le != cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    kgpu_edge_plan_destroy(p);
+    return cuda_fail(e, "edge plan capture");
+  }
+  *out = p;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_edge_plan_launch(kgpu_edge_plan p, kgpu_stream s)
+{
+  if (!p || !p->exec) return fail(KGPU_ERR_INVALID, "null plan");
+  CK(cudaGraphLaunch(p->exec, (cudaStream_t)s));
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_edge_plan_destroy(kgpu_edge_plan p)
+{
+  if (!p) return KGPU_OK;
+  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->graph) cudaGraphDestroy(p->graph);
+  delete p;
+  return KGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,636 @@
+// kgpu_collide.cu — batched collision engine: configuration checks, feasibility
+// and planner edge checks in one persistent launch.
+//
+// Replaces, per configuration, the reference's serial chain
+//   SingleRobotCSpace::IsFeasible -> CheckJointLimits -> UpdateConfig (FK)
+//   -> WorldPlannerSettings::CheckCollision(robot, others) (env)
+//   -> WorldPlannerSettings::CheckCollision(robot) (self)
+// (Cpp/Planning/RobotCSpace.cpp:610-630,786-823,
+//  Cpp/Planning/PlannerSettings.cpp:241-331) and, per edge, the epsilon edge
+// checker loop over interpolated configurations
+// (Cpp/Planning/RobotCSpace.cpp:835-840, Cpp/Modeling/Interpolate.cpp:10-14).
+//
+// Execution model
+//   * One warp processes one work item (a configuration or an edge step) at
+//     a time and pulls items from a device work queue (persistent grid sized
+//     to the SM count).  Edge steps are ordered step-major across edges, so
+//     every edge's early steps run first and a step beyond an edge's first
+//     collision is skipped.
+//   * FK: lane i owns link i (warp_fk32); transforms go to shared memory.
+//   * All queries of the item — (link, env group) and (link, link) pairs —
+//     share one warp stack of BVH node pairs tagged with their query, so the
+//     32 lanes stay busy across queries.  Lanes pop 32 pairs, test them, and
+//     push children with ballot/popc compaction; leaf/leaf pairs become
+//     triangle-pair jobs that are expanded one triangle pair per lane.
+//   * A triangle pair the FP32 filter cannot separate is re-tested in FP64
+//     by the lane that holds it (band_retest); the first confirmed contact
+//     ends the query set.
+//   * The shared-memory stack spills its lower half to a per-warp region of
+//     global scratch when full; exhausting that region sets
+//     KGPU_ERR_OVERFLOW instead of dropping work.
+#include <climits>
+
+#include "kgpu_device.cuh"
+
+namespace kgpu {
+
+namespace {
+
+constexpr int kStackCap = 512;
+constexpr int kJobCap = 96;
+constexpr int kGrab = 2;  // items taken from the queue per atomic
+
+enum Mode { MODE_CONFIGS = 0, MODE_FEASIBLE = 1, MODE_EDGES = 2 };
+
+struct __align__(16) WarpSmem {
+  uint2 stack[kStackCap];
+  uint32_t jobA[kJobCap];
+  uint32_t jobB[kJobCap];
+  uint32_t jobM[kJobCap];
+  uint32_t jobOff[kJobCap + 1];
+  float T[kMaxLinks][12];
+  double q64[kMaxLinks];
+  double T64[kMaxLinks][12];  // FP64 link transforms, computed on first band pair
+};
+
+struct EngineArgs {
+  int mode;
+  int robot;             // fixed robot, or -1 with robot_ids
+  const int* robot_ids;
+  const float* q;
+  int q_stride;
+  int B;
+  uint8_t* env_hit;
+  uint8_t* self_hit;
+  uint8_t* feasible;
+  // edges
+  const float* qa;
+  const float* qb;
+  const int* nsteps;
+  int E;
+  int* first_hit;
+  const int* round_off;
+  const int* perm;
+  const int* meta;       // [0] max n, [1] total items
+  // queue / scratch
+  unsigned int* head;
+  uint2* spill;
+  int spill_per_warp;
+};
+
+struct Cnt {
+  unsigned long long items = 0, node_pairs = 0, tri_pairs = 0, band = 0, spills = 0;
+};
+
+// Result of one query set.
+enum { TR_FREE = 0, TR_HIT = 1, TR_OVERFLOW = 2 };
+
+__device__ __forceinline__ uint2 make_entry(int nodeA, int la, int tgt, int nodeB)
+{
+  return make_uint2((uint32_t)nodeB, (uint32_t)nodeA | ((uint32_t)la << 20) | ((uint32_t)tgt << 25));
+}
+
+// Tests the triangle-pair jobs of the warp, one triangle pair per lane;
+// returns true on a confirmed contact.  Per pair: FP32 separating-axis filter
+// (separated beyond the band: done), FP32 intersection certificate (crossing
+// beyond the band: contact), otherwise the FP64 re-test on transforms
+// computed once per configuration (fk64 tracks whether S.T64 is valid).
+__device__ bool run_jobs(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, int njobs, int lane,
+                         int& fk64, Cnt& cnt)
+{
+  // exclusive prefix over job sizes
+  uint32_t carry = 0;
+  for (int b = 0; b < njobs; b += 32) {
+    int j = b + lane;
+    uint32_t c = 0;
+    if (j < njobs) {
+      uint32_t ca = (S.jobA[j] >> 28) + 1;
+      uint32_t cb = ((S.jobM[j] >> 16) & 3u) + 1;
+      c = ca * cb;
+    }
+    uint32_t incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (j < njobs) S.jobOff[j] = carry + incl - c;
+    carry += __shfl_sync(0xffffffffu, incl, 31);
+  }
+  if (lane == 0) S.jobOff[njobs] = carry;
+  __syncwarp();
+  const uint32_t total = carry;
+  const float eps = W.eps_band;
+  for (uint32_t base = 0; base < total; base += 32) {
+    uint32_t p = base + lane;
+    bool band = false, certain = false;
+    int la = 0, tgt = 0, tA = 0, tB = 0;
+    if (p < total) {
+      // job holding p: largest j with jobOff[j] <= p
+      int lo = 0, hi = njobs - 1;
+      while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (S.jobOff[mid] <= p) lo = mid; else hi = mid - 1;
+      }
+      int j = lo;
+      uint32_t r = p - S.jobOff[j];
+      uint32_t jm = S.jobM[j];
+      uint32_t cb = ((jm >> 16) & 3u) + 1;
+      la = jm & 0xff;
+      tgt = (jm >> 8) & 0xff;
+      tA = (int)(S.jobA[j] & 0x0fffffffu) + (int)(r / cb);
+      tB = (int)S.jobB[j] + (int)(r % cb);
+      float3 P[3], Q[3];
+      const float* TA = S.T[la];
+#pragma unroll
+      for (int v = 0; v < 3; ++v) {
+        float4 x = __ldg(W.ltri32 + 3 * (size_t)tA + v);
+        P[v] = xform32(TA, make_float3(x.x, x.y, x.z));
+      }
+      float margin = R.link_margin[la];
+      if (tgt < 32) {
+        const float* TB = S.T[tgt];
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+          float4 x = __ldg(W.ltri32 + 3 * (size_t)tB + v);
+          Q[v] = xform32(TB, make_float3(x.x, x.y, x.z));
+        }
+        margin += R.link_margin[tgt];
+      } else {
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+          float4 x = __ldg(W.etri32 + 3 * (size_t)tB + v);
+          Q[v] = make_float3(x.x, x.y, x.z);
+        }
+        margin += W.group_margin[tgt - 32];
+      }
+      band = !tri_separated32(P, Q, eps, margin);
+      if (band && margin == 0.f) certain = tri_certain_hit32(P, Q, eps);
+    }
+    cnt.tri_pairs += (p < total) ? 1 : 0;
+    if (__any_sync(0xffffffffu, certain)) return true;
+    bool need64 = band && !certain;
+    if (__any_sync(0xffffffffu, need64)) {
+      if (!fk64) {
+        warp_fk64(R, S.q64, S.T64, lane);
+        fk64 = 1;
+      }
+      int hit = 0;
+      if (need64) {
+        cnt.band++;
+        hit = band_retest(W, R, S.T64, la, tA, tgt, tB);
+      }
+      if (__any_sync(0xffffffffu, hit)) return true;
+    }
+  }
+  return false;
+}
+
+// Traverses queries [qbase, qbase+qcount) of robot R for the configuration
+// whose FP32 link transforms are in S.T.  Warp-uniform control flow.
+__device__ int traverse(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, int qbase, int qcount,
+                        int lane, uint2* spill, int spill_cap, int& fk64, Cnt& cnt)
+{
+  const float eps = W.eps_band;
+  int top = 0, njobs = 0, spill_top = 0;
+
+  auto spill_out = [&]() -> bool {
+    const int H = kStackCap / 2;
+    if (spill_top + H > spill_cap) return false;
+    for (int k = lane; k < H; k += 32) spill[spill_top + k] = S.stack[k];
+    __syncwarp();
+    for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];
+    __syncwarp();
+    spill_top += H;
+    top -= H;
+    cnt.spills++;
+    return true;
+  };
+
+  // root pairs of every query, tested in parallel
+  for (int qb = 0; qb < qcount; qb += 32) {
+    if (top > kStackCap - 32) {
+      if (!spill_out()) return TR_OVERFLOW;
+    }
+    int qi = qb + lane;
+    bool push = false;
+    uint2 ent = make_uint2(0, 0);
+    if (qi < qcount) {
+      uint32_t qw = __ldg(W.queries + qbase + qi);
+      int a = qw & 0xff, tgt = (qw >> 8) & 0xff;
+      int ra = R.link_root[a];
+      int rb = tgt < 32 ? R.link_root[tgt] : W.group_root[tgt - 32];
+      if (ra >= 0 && rb >= 0) {
+        KNode na = W.lnodes[ra];
+        Box32 A = xform_box(S.T[a], na.a, na.b);
+        Box32 Bx;
+        float m = R.link_margin[a];
+        if (tgt < 32) {
+          KNode nb = W.lnodes[rb];
+          Bx = xform_box(S.T[tgt], nb.a, nb.b);
+          m += R.link_margin[tgt];
+        } else {
+          KNode nb = W.enodes[rb];
+          Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z);
+          Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z);
+          m += W.group_margin[tgt - 32];
+        }
+        cnt.node_pairs++;
+        if (boxes_overlap(A, Bx, eps + m)) {
+          push = true;
+          ent = make_entry(ra, a, tgt, rb);
+        }
+      }
+    }
+    unsigned mp = __ballot_sync(0xffffffffu, push);
+    if (push) S.stack[top + __popc(mp & lanemask_lt())] = ent;
+    top += __popc(mp);
+    __syncwarp();
+  }
+
+  for (;;) {
+    if (top == 0) {
+      if (spill_top > 0) {
+        int n = min(kStackCap / 2, spill_top);
+        for (int k = lane; k < n; k += 32) S.stack[k] = spill[spill_top - n + k];
+        __syncwarp();
+        spill_top -= n;
+        top = n;
+      } else if (njobs == 0) {
+        return TR_FREE;
+      }
+    }
+    if (njobs > kJobCap - 32 || (top == 0 && njobs > 0)) {
+      bool hit = run_jobs(S, W, R, njobs, lane, fk64, cnt);
+      __syncwarp();
+      njobs = 0;
+      if (hit) return TR_HIT;
+      continue;
+    }
+    if (top > kStackCap - 32) {
+      if (!spill_out()) return TR_OVERFLOW;
+    }
+    int n = min(top, 32);
+    bool have = lane < n;
+    uint2 e = make_uint2(0, 0);
+    if (have) e = S.stack[top - 1 - lane];
+    __syncwarp();
+    top -= n;
+    int outcome = 0;  // 1: two children, 2: leaf job
+    uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
+    uint32_t jA = 0, jB = 0, jM = 0;
+    if (have) {
+      int nodeA = e.y & 0xfffff;
+      int la = (e.y >> 20) & 31;
+      int tgt = (e.y >> 25) & 63;
+      int nodeB = (int)e.x;
+      KNode na = W.lnodes[nodeA];
+      KNode nb = tgt < 32 ? W.lnodes[nodeB] : W.enodes[nodeB];
+      Box32 A = xform_box(S.T[la], na.a, na.b);
+      Box32 Bx;
+      float m = R.link_margin[la];
+      if (tgt < 32) {
+        Bx = xform_box(S.T[tgt], nb.a, nb.b);
+        m += R.link_margin[tgt];
+      } else {
+        Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z);
+        Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z);
+        m += W.group_margin[tgt - 32];
+      }
+      if (boxes_overlap(A, Bx, eps + m)) {
+        int cntA = f2i(na.b.w), cntB = f2i(nb.b.w);
+        int ia = f2i(na.a.w), ib = f2i(nb.a.w);
+        if (cntA > 0 && cntB > 0) {
+          outcome = 2;
+          jA = (uint32_t)ia | ((uint32_t)(cntA - 1) << 28);
+          jB = (uint32_t)ib;
+          jM = (uint32_t)la | ((uint32_t)tgt << 8) | ((uint32_t)(cntB - 1) << 16);
+        } else {
+          outcome = 1;
+          bool splitB = cntA > 0 ||
+                        (cntB == 0 && (nb.b.x + nb.b.y + nb.b.z) > (na.b.x + na.b.y + na.b.z));
+          if (splitB) {
+            c0 = make_entry(nodeA, la, tgt, ib);
+            c1 = make_entry(nodeA, la, tgt, ib + 1);
+          } else {
+            c0 = make_entry(ia, la, tgt, nodeB);
+            c1 = make_entry(ia + 1, la, tgt, nodeB);
+          }
+        }
+      }
+    }
+    cnt.node_pairs += have ? 1 : 0;
+    unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
+    unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
+    unsigned lt = lanemask_lt();
+    if (outcome == 1) {
+      int r = top + 2 * __popc(m1 & lt);
+      S.stack[r] = c1;
+      S.stack[r + 1] = c0;
+    } else if (outcome == 2) {
+      int r = njobs + __popc(m2 & lt);
+      S.jobA[r] = jA;
+      S.jobB[r] = jB;
+      S.jobM[r] = jM;
+    }
+    top += 2 * __popc(m1);
+    njobs += __popc(m2);
+    __syncwarp();
+  }
+}
+
+template <int WARPS>
+__global__ void __launch_bounds__(WARPS * 32, 16 / WARPS) k_engine(KWorldDev W, EngineArgs A)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpSmem* all = reinterpret_cast<WarpSmem*>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WarpSmem& S = all[warp];
+  const int gwarp = blockIdx.x * WARPS + warp;
+  uint2* spill = A.spill + (size_t)gwarp * A.spill_per_warp;
+  Cnt cnt;
+  int total = A.mode == MODE_EDGES ? A.meta[1] : A.B;
+  int maxn = A.mode == MODE_EDGES ? A.meta[0] : 0;
+
+  for (;;) {
+    unsigned int base = 0;
+    if (lane == 0) base = atomicAdd(A.head, kGrab);
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (base >= (unsigned)total) break;
+    for (unsigned it = base; it < base + kGrab && it < (unsigned)total; ++it) {
+      // ---- decode the item
+      int rid = A.robot;
+      int b = (int)it, e = 0, k = 0, n = 0;
+      if (A.mode == MODE_EDGES) {
+        int lo = 0, hi = maxn;
+        while (lo < hi) {
+          int mid = (lo + hi + 1) >> 1;
+          if (__ldg(A.round_off + mid) <= (int)it) lo = mid; else hi = mid - 1;
+        }
+        k = lo;
+        e = __ldg(A.perm + ((int)it - __ldg(A.round_off + k)));
+        int fh = 0;
+        if (lane == 0) fh = *((volatile int*)(A.first_hit + e));
+        fh = __shfl_sync(0xffffffffu, fh, 0);
+        if (fh < k) continue;  // an earlier step of this edge already hit
+        n = __ldg(A.nsteps + e);
+      } else if (rid < 0) {
+        rid = __ldg(A.robot_ids + b);
+      }
+      const KRobotDev& R = W.robots[rid];
+      const int nl = R.nlinks;
+      double q64 = 0.0;
+      if (lane < nl) {
+        if (A.mode == MODE_EDGES)
+          q64 = kx_interp((double)__ldg(A.qa + (size_t)e * nl + lane),
+                          (double)__ldg(A.qb + (size_t)e * nl + lane), k, n);
+        else
+          q64 = (double)__ldg(A.q + (size_t)b * A.q_stride + lane);
+        S.q64[lane] = q64;
+      }
+      cnt.items++;
+      bool viol = lane < nl && (q64 < R.qmin64[lane] || q64 > R.qmax64[lane]);
+      bool limit_bad = __any_sync(0xffffffffu, viol);
+      bool nonfinite = __any_sync(0xffffffffu, lane < nl && !(fabs(q64) < 1.0e6));
+      if (nonfinite) {
+        if (lane == 0) set_status(W, KGPU_ERR_NOT_FINITE);
+        continue;
+      }
+      if (A.mode != MODE_CONFIGS && limit_bad) {
+        if (lane == 0) {
+          if (A.mode == MODE_EDGES) atomicMin(A.first_hit + e, k);
+          else A.feasible[b] = 0;
+        }
+        continue;
+      }
+      float P[12];
+      warp_fk32(R, lane, (float)q64, P);
+      if (lane < nl) {
+#pragma unroll
+        for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
+      }
+      __syncwarp();
+      int env_res = TR_FREE, self_res = TR_FREE;
+      int fk64 = 0;
+      bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
+      bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
+      if (want_env && R.nqueries_env > 0)
+        env_res = traverse(S, W, R, R.query_off, R.nqueries_env, lane, spill, A.spill_per_warp, fk64, cnt);
+      bool stop = A.mode != MODE_CONFIGS && env_res != TR_FREE;
+      if (!stop && want_self && R.nqueries_self > 0)
+        self_res = traverse(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill,
+                            A.spill_per_warp, fk64, cnt);
+      if (env_res == TR_OVERFLOW || self_res == TR_OVERFLOW) {
+        if (lane == 0) set_status(W, KGPU_ERR_OVERFLOW);
+        continue;
+      }
+      if (lane == 0) {
+        if (A.mode == MODE_CONFIGS) {
+          if (A.env_hit) A.env_hit[b] = env_res == TR_HIT;
+          if (A.self_hit) A.self_hit[b] = self_res == TR_HIT;
+        } else if (A.mode == MODE_FEASIBLE) {
+          A.feasible[b] = (env_res == TR_FREE && self_res == TR_FREE) ? 1 : 0;
+        } else if (env_res == TR_HIT || self_res == TR_HIT) {
+          atomicMin(A.first_hit + e, k);
+        }
+      }
+      __syncwarp();
+    }
+  }
+  if (lane == 0 && W.stats) {
+    atomicAdd(W.stats + 0, cnt.items);
+  }
+  // per-lane counters
+  unsigned long long np = cnt.node_pairs, tp = cnt.tri_pairs, bd = cnt.band;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    np += __shfl_down_sync(0xffffffffu, np, o);
+    tp += __shfl_down_sync(0xffffffffu, tp, o);
+    bd += __shfl_down_sync(0xffffffffu, bd, o);
+  }
+  if (lane == 0 && W.stats) {
+    atomicAdd(W.stats + 1, np);
+    atomicAdd(W.stats + 2, tp);
+    atomicAdd(W.stats + 3, bd);
+    atomicAdd(W.stats + 4, cnt.spills);
+  }
+}
+
+// ---- edge preparation ------------------------------------------------------
+__global__ void k_edges_prep1(const int* nsteps, int E, int* hist, int* meta, int* first_hit,
+                              int* status)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  int n = nsteps[e];
+  first_hit[e] = INT_MAX;
+  if (n < 1 || n > kMaxSteps) {
+    atomicCAS(status, 0, KGPU_ERR_INVALID);
+    n = 0;  // treated as a single configuration
+  }
+  atomicAdd(hist + n, 1);
+  atomicMax(meta + 0, n);
+}
+
+// hist[v] -> base position of edges with n == v in the descending order;
+// round_off[k] = number of items in rounds < k; meta[1] = total items.
+__global__ void k_edges_prep2(int* hist, int* round_off, int* meta)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int maxn = meta[0];
+  long long count = 0;  // edges with n > v
+  for (int v = maxn; v >= 0; --v) {
+    int h = hist[v];
+    hist[v] = (int)count;  // base
+    count += h;
+    round_off[v + 1] = (int)count;  // temporarily: count_ge[v]
+  }
+  long long acc = 0;
+  round_off[0] = 0;
+  for (int k = 0; k <= maxn; ++k) {
+    long long c = round_off[k + 1];
+    round_off[k + 1] = (int)(acc + c);
+    acc += c;
+  }
+  meta[1] = acc > INT_MAX ? INT_MAX : (int)acc;
+}
+
+__global__ void k_edges_prep3(const int* nsteps, int E, const int* base, int* fill, int* perm)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  int n = nsteps[e];
+  if (n < 1 || n > kMaxSteps) n = 0;
+  perm[base[n] + atomicAdd(fill + n, 1)] = e;
+}
+
+__global__ void k_edges_finalize(int* first_hit, int E)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e < E && first_hit[e] == INT_MAX) first_hit[e] = -1;
+}
+
+__global__ void k_fk(const KWorldDev W, int robot, const float* q, int B, float* T)
+{
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= B) return;
+  const KRobotDev& R = W.robots[robot];
+  int nl = R.nlinks;
+  float qv = lane < nl ? q[(size_t)warp * nl + lane] : 0.f;
+  float P[12];
+  warp_fk32(R, lane, qv, P);
+  if (lane < nl)
+    for (int i = 0; i < 12; ++i) T[((size_t)warp * nl + lane) * 12 + i] = P[i];
+}
+
+template <int WARPS>
+cudaError_t init_engine()
+{
+  return cudaFuncSetAttribute(k_engine<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(sizeof(WarpSmem) * WARPS));
+}
+
+// the shared-memory attribute is set once per process by engine_init(), so
+// that launches can be captured into CUDA graphs
+template <int WARPS>
+cudaError_t launch_engine(const KWorldDev& W, const EngineArgs& A, int blocks, cudaStream_t s)
+{
+  size_t smem = sizeof(WarpSmem) * WARPS;
+  k_engine<WARPS><<<blocks, WARPS * 32, smem, s>>>(W, A);
+  return cudaGetLastError();
+}
+
+cudaError_t dispatch_engine(const KWorldDev& W, const EngineArgs& A, int blocks, int warps,
+                            cudaStream_t s)
+{
+  switch (warps) {
+    case 4: return launch_engine<4>(W, A, blocks, s);
+    case 16: return launch_engine<16>(W, A, blocks, s);
+    default: return launch_engine<8>(W, A, blocks, s);
+  }
+}
+
+}  // namespace
+
+size_t engine_smem_per_warp() { return sizeof(WarpSmem); }
+
+cudaError_t engine_init()
+{
+  cudaError_t e = init_engine<4>();
+  if (e == cudaSuccess) e = init_engine<8>();
+  if (e == cudaSuccess) e = init_engine<16>();
+  return e;
+}
+
+cudaError_t launch_fk(const KWorldDev& W, int robot, const float* q, int B, float* T,
+                      cudaStream_t s)
+{
+  if (B <= 0) return cudaSuccess;
+  int threads = 256;
+  long long warps = B;
+  int blocks = (int)((warps * 32 + threads - 1) / threads);
+  k_fk<<<blocks, threads, 0, s>>>(W, robot, q, B, T);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_check_configs(const KWorldDev& W, const Scratch& S, int robot,
+                                 const int* robot_ids, const float* q, int q_stride, int B,
+                                 uint8_t* env_hit, uint8_t* self_hit, uint8_t* feasible,
+                                 int blocks, int warps_per_block, cudaStream_t s)
+{
+  if (B <= 0) return cudaSuccess;
+  cudaError_t err = cudaMemsetAsync(S.counters, 0, sizeof(unsigned int), s);
+  if (err != cudaSuccess) return err;
+  EngineArgs A = {};
+  A.mode = feasible ? MODE_FEASIBLE : MODE_CONFIGS;
+  A.robot = robot;
+  A.robot_ids = robot_ids;
+  A.q = q;
+  A.q_stride = q_stride;
+  A.B = B;
+  A.env_hit = env_hit;
+  A.self_hit = self_hit;
+  A.feasible = feasible;
+  A.head = S.counters;
+  A.spill = S.spill;
+  A.spill_per_warp = (int)S.spill_per_warp;
+  return dispatch_engine(W, A, blocks, warps_per_block, s);
+}
+
+cudaError_t launch_check_edges(const KWorldDev& W, const Scratch& S, int robot, const float* qa,
+                               const float* qb, const int* nsteps, int E, int* first_hit,
+                               int blocks, int warps_per_block, cudaStream_t s)
+{
+  if (E <= 0) return cudaSuccess;
+  cudaError_t err;
+  if ((err = cudaMemsetAsync(S.counters, 0, sizeof(unsigned int), s)) != cudaSuccess) return err;
+  if ((err = cudaMemsetAsync(S.edge_hist, 0, sizeof(int) * (kMaxSteps + 2), s)) != cudaSuccess) return err;
+  if ((err = cudaMemsetAsync(S.edge_meta, 0, sizeof(int) * 4, s)) != cudaSuccess) return err;
+  int* fill = S.edge_meta + 4;  // kMaxSteps+2 ints after the meta words
+  if ((err = cudaMemsetAsync(fill, 0, sizeof(int) * (kMaxSteps + 2), s)) != cudaSuccess) return err;
+  int tb = 256, gb = (E + tb - 1) / tb;
+  k_edges_prep1<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, S.edge_meta, first_hit, W.status);
+  k_edges_prep2<<<1, 32, 0, s>>>(S.edge_hist, S.edge_round_off, S.edge_meta);
+  k_edges_prep3<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, fill, S.edge_perm);
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  EngineArgs A = {};
+  A.mode = MODE_EDGES;
+  A.robot = robot;
+  A.qa = qa;
+  A.qb = qb;
+  A.nsteps = nsteps;
+  A.E = E;
+  A.first_hit = first_hit;
+  A.round_off = S.edge_round_off;
+  A.perm = S.edge_perm;
+  A.meta = S.edge_meta;
+  A.head = S.counters;
+  A.spill = S.spill;
+  A.spill_per_warp = (int)S.spill_per_warp;
+  if ((err = dispatch_engine(W, A, blocks, warps_per_block, s)) != cudaSuccess) return err;
+  k_edges_finalize<<<gb, tb, 0, s>>>(first_hit, E);
+  return cudaGetLastError();
+}
+
+}  // namespace kgpu

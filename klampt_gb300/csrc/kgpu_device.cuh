@@ -1,0 +1,321 @@
+// kgpu_device.cuh — device helpers shared by the engine kernels.
+//
+// FP32 side: forward kinematics, link-node boxes in world frame, and a
+// conservative triangle/triangle separating-axis filter.  "Conservative"
+// means: when the filter reports separation, the canonical FP64 triangles
+// (include/kgpu_exact.h, evaluated on the FP64 forward kinematics) are
+// separated too.  Every FP32 comparison therefore carries an inflation
+// eps (world option "eps_band", default 1e-4 m) that bounds the difference
+// between FP32 and FP64 world coordinates plus the FP32 rounding of the test
+// itself.  Pairs the filter cannot separate form the "band" and are decided
+// by the FP64 re-test, so verdicts equal the FP64 ones bit for bit.
+#pragma once
+
+#include "../../include/kgpu_exact.h"
+#include "kgpu_internal.h"
+
+namespace kgpu {
+
+__device__ __forceinline__ int f2i(float f) { return __float_as_int(f); }
+
+__device__ __forceinline__ unsigned lanemask_lt()
+{
+  unsigned m;
+  asm volatile("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// ---- FP32 rigid transforms (R row-major, then t) -------------------------
+__device__ __forceinline__ void compose32(const float* A, const float* B, float* o)
+{
+#pragma unroll
+  for (int r = 0; r < 3; ++r) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      o[3 * r + c] = fmaf(A[3 * r + 0], B[c], fmaf(A[3 * r + 1], B[3 + c], A[3 * r + 2] * B[6 + c]));
+    o[9 + r] = fmaf(A[3 * r + 0], B[9], fmaf(A[3 * r + 1], B[10], fmaf(A[3 * r + 2], B[11], A[9 + r])));
+  }
+}
+
+__device__ __forceinline__ float3 xform32(const float* T, float3 v)
+{
+  return make_float3(fmaf(T[0], v.x, fmaf(T[1], v.y, fmaf(T[2], v.z, T[9]))),
+                     fmaf(T[3], v.x, fmaf(T[4], v.y, fmaf(T[5], v.z, T[10]))),
+                     fmaf(T[6], v.x, fmaf(T[7], v.y, fmaf(T[8], v.z, T[11]))));
+}
+
+// local transform T0_Parent * J(q) of link i in FP32
+__device__ __forceinline__ void joint_local32(const KRobotDev& R, int i, float q, float* L)
+{
+  const float* T0 = R.T0P[i];
+  int jt = R.jtype[i];
+  if (jt == KX_JOINT_REVOLUTE) {
+    float s, c;
+    sincosf(q, &s, &c);
+    float wx = R.axis[i][0], wy = R.axis[i][1], wz = R.axis[i][2];
+    float v = 1.f - c;
+    float J[12];
+    J[0] = c + wx * wx * v;  J[1] = wx * wy * v - wz * s; J[2] = wx * wz * v + wy * s;
+    J[3] = wy * wx * v + wz * s; J[4] = c + wy * wy * v;  J[5] = wy * wz * v - wx * s;
+    J[6] = wz * wx * v - wy * s; J[7] = wz * wy * v + wx * s; J[8] = c + wz * wz * v;
+    J[9] = 0.f; J[10] = 0.f; J[11] = 0.f;
+    compose32(T0, J, L);
+  } else if (jt == KX_JOINT_PRISMATIC) {
+    float J[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
+    J[9] = R.axis[i][0] * q; J[10] = R.axis[i][1] * q; J[11] = R.axis[i][2] * q;
+    compose32(T0, J, L);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 12; ++k) L[k] = T0[k];
+  }
+}
+
+// Warp-cooperative forward kinematics: lane i < nlinks owns link i.  Local
+// transforms are formed in parallel and chained to the root by pointer
+// jumping (ceil(log2(depth)) rounds of shuffles), which handles serial
+// chains and trees alike.  Result: world transform of link `lane` in P.
+__device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, float q, float* P)
+{
+  int nl = R.nlinks;
+  int anc = -1;
+  if (lane < nl) {
+    joint_local32(R, lane, q, P);
+    anc = R.parents[lane];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 12; ++k) P[k] = 0.f;
+  }
+  while (__any_sync(0xffffffffu, anc >= 0)) {
+    int src = anc >= 0 ? anc : lane;
+    float Pa[12];
+#pragma unroll
+    for (int k = 0; k < 12; ++k) Pa[k] = __shfl_sync(0xffffffffu, P[k], src);
+    int anc2 = __shfl_sync(0xffffffffu, anc, src);
+    if (anc >= 0) {
+      float o[12];
+      compose32(Pa, P, o);
+#pragma unroll
+      for (int k = 0; k < 12; ++k) P[k] = o[k];
+      anc = anc2;
+    }
+  }
+}
+
+// ---- boxes -------------------------------------------------------------
+struct Box32 {
+  float3 c, h;
+};
+
+__device__ __forceinline__ Box32 xform_box(const float* T, float4 a, float4 b)
+{
+  Box32 o;
+  o.c = xform32(T, make_float3(a.x, a.y, a.z));
+  o.h = make_float3(fabsf(T[0]) * b.x + fabsf(T[1]) * b.y + fabsf(T[2]) * b.z,
+                    fabsf(T[3]) * b.x + fabsf(T[4]) * b.y + fabsf(T[5]) * b.z,
+                    fabsf(T[6]) * b.x + fabsf(T[7]) * b.y + fabsf(T[8]) * b.z);
+  return o;
+}
+
+__device__ __forceinline__ bool boxes_overlap(const Box32& A, const Box32& B, float eps)
+{
+  return fabsf(A.c.x - B.c.x) <= A.h.x + B.h.x + eps &&
+         fabsf(A.c.y - B.c.y) <= A.h.y + B.h.y + eps &&
+         fabsf(A.c.z - B.c.z) <= A.h.z + B.h.z + eps;
+}
+
+// ---- FP32 triangle filter ------------------------------------------------
+__device__ __forceinline__ float3 sub3(float3 a, float3 b) { return make_float3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b)
+{
+  return make_float3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float l1(float3 a) { return fabsf(a.x) + fabsf(a.y) + fabsf(a.z); }
+
+// true if axis a separates p and q by more than the tolerance
+__device__ __forceinline__ bool sep_axis32(float3 a, const float3* p, const float3* q, float eps,
+                                           float margin)
+{
+  float p0 = dot3(a, p[0]), p1 = dot3(a, p[1]), p2 = dot3(a, p[2]);
+  float q0 = dot3(a, q[0]), q1 = dot3(a, q[1]), q2 = dot3(a, q[2]);
+  float pmin = fminf(p0, fminf(p1, p2)), pmax = fmaxf(p0, fmaxf(p1, p2));
+  float qmin = fminf(q0, fminf(q1, q2)), qmax = fmaxf(q0, fmaxf(q1, q2));
+  float gap = fmaxf(qmin - pmax, pmin - qmax);
+  float tol = l1(a) * eps;
+  if (margin > 0.f) tol += margin * sqrtf(dot3(a, a));
+  return gap > tol;
+}
+
+// Conservative separation of world-frame triangles P and Q (FP32).
+__device__ __forceinline__ bool tri_separated32(const float3* P, const float3* Q, float eps,
+                                                float margin)
+{
+  // box pre-test
+  float3 pmn = make_float3(fminf(P[0].x, fminf(P[1].x, P[2].x)), fminf(P[0].y, fminf(P[1].y, P[2].y)),
+                           fminf(P[0].z, fminf(P[1].z, P[2].z)));
+  float3 pmx = make_float3(fmaxf(P[0].x, fmaxf(P[1].x, P[2].x)), fmaxf(P[0].y, fmaxf(P[1].y, P[2].y)),
+                           fmaxf(P[0].z, fmaxf(P[1].z, P[2].z)));
+  float3 qmn = make_float3(fminf(Q[0].x, fminf(Q[1].x, Q[2].x)), fminf(Q[0].y, fminf(Q[1].y, Q[2].y)),
+                           fminf(Q[0].z, fminf(Q[1].z, Q[2].z)));
+  float3 qmx = make_float3(fmaxf(Q[0].x, fmaxf(Q[1].x, Q[2].x)), fmaxf(Q[0].y, fmaxf(Q[1].y, Q[2].y)),
+                           fmaxf(Q[0].z, fmaxf(Q[1].z, Q[2].z)));
+  float bt = eps + margin;
+  if (qmn.x - pmx.x > bt || pmn.x - qmx.x > bt || qmn.y - pmx.y > bt || pmn.y - qmx.y > bt ||
+      qmn.z - pmx.z > bt || pmn.z - qmx.z > bt)
+    return true;
+  float3 p[3], q[3];
+  p[0] = make_float3(0.f, 0.f, 0.f);
+  p[1] = sub3(P[1], P[0]);
+  p[2] = sub3(P[2], P[0]);
+  q[0] = sub3(Q[0], P[0]);
+  q[1] = sub3(Q[1], P[0]);
+  q[2] = sub3(Q[2], P[0]);
+  float3 ep[3] = {sub3(p[1], p[0]), sub3(p[2], p[1]), sub3(p[0], p[2])};
+  float3 eq[3] = {sub3(q[1], q[0]), sub3(q[2], q[1]), sub3(q[0], q[2])};
+  float3 np = cross3(ep[0], ep[1]);
+  float3 nq = cross3(eq[0], eq[1]);
+  if (sep_axis32(np, p, q, eps, margin)) return true;
+  if (sep_axis32(nq, p, q, eps, margin)) return true;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      if (sep_axis32(cross3(ep[i], eq[j]), p, q, eps, margin)) return true;
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    if (sep_axis32(cross3(np, ep[i]), p, q, eps, margin)) return true;
+    if (sep_axis32(cross3(nq, eq[i]), p, q, eps, margin)) return true;
+  }
+  return false;
+}
+
+// orient3d(a,b,c,d) = (a-d) . ((b-d) x (c-d))
+__device__ __forceinline__ float orient32(float3 a, float3 b, float3 c, float3 d)
+{
+  return dot3(sub3(a, d), cross3(sub3(b, d), sub3(c, d)));
+}
+
+__device__ __forceinline__ int rsign(float x, float B) { return x > B ? 1 : (x < -B ? -1 : 0); }
+
+// Certain intersection of world-frame triangles P and Q despite vertex
+// errors of up to `delta` (Euclidean) per vertex.  An edge of one triangle
+// crossing the other's interior is decided by orientation determinants: its
+// endpoints lie on opposite sides of the other triangle's plane and the three
+// edge-edge orientations agree in sign.  Each determinant's sign is trusted
+// only beyond the bound B = 6 delta L^2 + 12 delta^2 L + 16 u L^3 (vertex
+// perturbation + FP32 rounding, L the diameter of the six vertices), so a
+// "true" here holds for the exact FP64 triangles as well, and the canonical
+// FP64 test then reports the same contact.  Pairs it cannot certify go to the
+// FP64 re-test.
+__device__ __forceinline__ bool tri_certain_hit32(const float3* P, const float3* Q, float delta)
+{
+  float3 lo = P[0], hi = P[0];
+#pragma unroll
+  for (int k = 1; k < 6; ++k) {
+    float3 v = k < 3 ? P[k] : Q[k - 3];
+    lo = make_float3(fminf(lo.x, v.x), fminf(lo.y, v.y), fminf(lo.z, v.z));
+    hi = make_float3(fmaxf(hi.x, v.x), fmaxf(hi.y, v.y), fmaxf(hi.z, v.z));
+  }
+  float3 dg = sub3(hi, lo);
+  float L = sqrtf(dot3(dg, dg)) * 1.0001f;
+  float B = 6.f * delta * L * L + 12.f * delta * delta * L + 16.f * 5.9604645e-08f * L * L * L;
+  // plane sides
+  int sq[3], sp[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    sq[k] = rsign(orient32(Q[0], Q[1], Q[2], P[k]), B);
+    sp[k] = rsign(orient32(P[0], P[1], P[2], Q[k]), B);
+  }
+  int E[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      E[i][j] = rsign(orient32(P[i], P[(i + 1) % 3], Q[j], Q[(j + 1) % 3]), B);
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    // edge i of P through the interior of Q
+    if (sq[i] * sq[(i + 1) % 3] == -1 && E[i][0] != 0 && E[i][0] == E[i][1] && E[i][1] == E[i][2])
+      return true;
+    // edge i of Q through the interior of P
+    if (sp[i] * sp[(i + 1) % 3] == -1 && E[0][i] != 0 && E[0][i] == E[1][i] && E[1][i] == E[2][i])
+      return true;
+  }
+  return false;
+}
+
+// ---- FP64 side (canonical arithmetic) ------------------------------------
+// World transform of link l at q64 by the sequential chain root -> l, the
+// same operation sequence as the oracle's forward kinematics.
+__device__ __forceinline__ void chain64(const KRobotDev& R, const double* q64, int l, double* T)
+{
+  int path[kMaxLinks];
+  int n = 0;
+  for (int j = l; j >= 0; j = R.parents[j]) path[n++] = j;
+  double A[12], Lc[12];
+  int j = path[n - 1];
+  kx_joint_local(R.T0P64[j], R.axis64[j], R.jtype[j], q64[j], A);
+  for (int k = n - 2; k >= 0; --k) {
+    j = path[k];
+    kx_joint_local(R.T0P64[j], R.axis64[j], R.jtype[j], q64[j], Lc);
+    kx_compose(A, Lc, T);
+#pragma unroll
+    for (int i = 0; i < 12; ++i) A[i] = T[i];
+  }
+#pragma unroll
+  for (int i = 0; i < 12; ++i) T[i] = A[i];
+}
+
+// Warp-cooperative FP64 forward kinematics into T64[link][12]: the local
+// transforms are formed in parallel (lane i, link i), then composed by lane 0
+// in link order exactly as the oracle does (T[i] = T[parent] * L_i), so the
+// result is bit-identical to the sequential chain.
+__device__ __forceinline__ void warp_fk64(const KRobotDev& R, const double* q64, double (*T64)[12],
+                                          int lane)
+{
+  int nl = R.nlinks;
+  if (lane < nl) kx_joint_local(R.T0P64[lane], R.axis64[lane], R.jtype[lane], q64[lane], T64[lane]);
+  __syncwarp();
+  if (lane == 0) {
+    for (int i = 0; i < nl; ++i) {
+      int p = R.parents[i];
+      if (p < 0) continue;
+      double o[12];
+      kx_compose(T64[p], T64[i], o);
+      for (int k = 0; k < 12; ++k) T64[i][k] = o[k];
+    }
+  }
+  __syncwarp();
+}
+
+// FP64 re-test of one band pair: link triangle tA of link la against link
+// triangle tB of link tgt (tgt < 32) or environment triangle tB, with the
+// link transforms T64 of the configuration.  Returns 1 if the canonical
+// predicate reports collision.
+static __device__ __noinline__ int band_retest(const KWorldDev& W, const KRobotDev& R,
+                                               const double (*T64)[12], int la, int tA, int tgt, int tB)
+{
+  double P[9], Q[9];
+  const double* pa = W.ltri64 + 9 * (size_t)tA;
+  for (int v = 0; v < 3; ++v) kx_xform_point(T64[la], pa + 3 * v, P + 3 * v);
+  double m = R.link_margin64[la];
+  if (tgt < 32) {
+    const double* pb = W.ltri64 + 9 * (size_t)tB;
+    for (int v = 0; v < 3; ++v) kx_xform_point(T64[tgt], pb + 3 * v, Q + 3 * v);
+    m = kx_add(m, R.link_margin64[tgt]);
+  } else {
+    const double* pb = W.etri64 + 9 * (size_t)tB;
+    for (int i = 0; i < 9; ++i) Q[i] = pb[i];
+    m = kx_add(m, W.obj_margin64[W.etri_obj[tB]]);
+  }
+  if (m == 0.0) return kx_tri_tri_overlap(P, Q);
+  double cp[3], cq[3];
+  return kx_tri_tri_dist2(P, Q, cp, cq) <= kx_mul(m, m);
+}
+
+__device__ __forceinline__ void set_status(const KWorldDev& W, int code)
+{
+  atomicCAS(W.status, 0, code);
+}
+
+}  // namespace kgpu

@@ -1,0 +1,221 @@
+// kgpu_internal.h — device data layouts and host-side objects of the engine.
+//
+// HBM layout (all arrays are device-resident for the life of the handles):
+//   link BVH nodes    KNode[] for every link of every robot, concatenated;
+//                     child/leaf indices are global into the same array
+//   link triangles    float4[3] per triangle (FP32, link frame) in BVH leaf
+//                     order, plus double[9] per triangle (FP64 copy for the
+//                     band re-test)
+//   env BVH nodes     KNode[] for every object group; each group tree is
+//                     object-aware: its top levels split objects, and every
+//                     object owns a subtree (its root is obj_root[o])
+//   env triangles     float4[3] + double[9] per triangle (world frame), and
+//                     the owning object of each triangle
+// A node is 32 bytes (two float4): (center.xyz, index) and (half.xyz, count);
+// count == 0 marks an internal node whose children are index and index+1, a
+// leaf holds triangles [index, index+count).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/kgpu.h"
+
+namespace kgpu {
+
+constexpr int kMaxLinks = KGPU_MAX_LINKS;
+constexpr int kMaxGroups = 32;
+constexpr int kLeafSize = 4;
+constexpr int kMaxSteps = 65535;
+
+struct KNode {
+  float4 a;  // center.xyz, index (int bits)
+  float4 b;  // half.xyz, count (int bits)
+};
+
+// Host-side BVH result in the device layout.
+struct HostBvh {
+  std::vector<KNode> nodes;          // local indices (root = 0)
+  std::vector<double> node_c64;      // 3 per node, FP64 center
+  std::vector<double> node_h64;      // 3 per node, FP64 half extent
+  std::vector<int> order;            // triangle ids in leaf order
+  std::vector<int> node_obj;         // object owning each node (-1 above objects)
+};
+
+// Builds a BVH over triangles `ids` (tri: 9 doubles per triangle id).  When
+// tri_obj is given, the top levels split whole objects so that every object
+// owns one subtree.  Median split on the widest centroid axis, leaves of at
+// most kLeafSize triangles, children adjacent.
+void build_bvh(const std::vector<double>& tri, const std::vector<int>& ids,
+               const std::vector<int>* tri_obj, HostBvh& out);
+
+// Device tables of one robot (read through the read-only cache).
+struct KRobotDev {
+  int nlinks;
+  int nqueries_env;   // (link, group) queries
+  int nqueries_self;  // (link, link) queries
+  int query_off;      // into KWorldDev::queries (env queries first)
+  int parents[kMaxLinks];
+  int jtype[kMaxLinks];
+  int link_root[kMaxLinks];  // global node index or -1
+  int link_depth[kMaxLinks];
+  uint32_t env_mask[kMaxLinks];
+  float link_margin[kMaxLinks];
+  float qmin[kMaxLinks], qmax[kMaxLinks];
+  float T0P[kMaxLinks][12];
+  float axis[kMaxLinks][3];
+  double T0P64[kMaxLinks][12];
+  double axis64[kMaxLinks][3];
+  double qmin64[kMaxLinks], qmax64[kMaxLinks];
+  double link_margin64[kMaxLinks];
+};
+
+struct KWorldDev {
+  // robots
+  const KRobotDev* robots;
+  const uint32_t* queries;   // a | tgt << 8 ; tgt < 32: link, tgt >= 32: env group tgt-32
+  const KNode* lnodes;
+  const float4* ltri32;      // 3 per tri
+  const double* ltri64;      // 9 per tri
+  const double* lnode64;     // 6 per node (c, h) FP64 (plain kernel)
+  // environment
+  const KNode* enodes;
+  const float4* etri32;
+  const double* etri64;
+  const double* enode64;     // 6 per node
+  const int* etri_obj;
+  const float* obj_margin;
+  const double* obj_margin64;
+  const int* obj_root;       // per object: node index of its subtree root
+  const int* obj_group;
+  const uint8_t* obj_convex;
+  const int* node_obj;       // per env node
+  int group_root[kMaxGroups];
+  float group_margin[kMaxGroups];
+  int num_objects;
+  // options
+  float eps_band;            // FP32 conservative inflation (m)
+  // diagnostics
+  int* status;               // device status word
+  unsigned long long* stats; // kgpu_stats counters
+};
+
+// scratch owned by the world (allocated at creation, grown on demand)
+struct Scratch {
+  uint2* spill = nullptr;          // per-warp spill stacks
+  size_t spill_per_warp = 0;
+  int max_warps = 0;
+  unsigned int* counters = nullptr;  // work-queue heads
+  int* edge_hist = nullptr;          // kMaxSteps+2
+  int* edge_round_off = nullptr;     // kMaxSteps+2
+  int* edge_perm = nullptr;
+  int* edge_meta = nullptr;          // [0] max n, [1] total items
+  size_t edge_cap = 0;
+};
+
+}  // namespace kgpu
+
+// ---- host objects -----------------------------------------------------------
+struct kgpu_robot_s {
+  int nlinks = 0;
+  std::vector<int> parents, jtypes;
+  std::vector<double> T0P, axes, qmin, qmax, margins;
+  std::vector<uint8_t> self_mask;   // [L*L] upper triangle
+  std::vector<int> link_tri_count;
+  // device arrays of this robot's links (local indices per link)
+  std::vector<kgpu::HostBvh> bvh;
+  std::vector<std::vector<double>> tri64;  // per link, leaf order, 9 per tri
+  double reach = 0.0;                      // bound on |world coordinate| of any link point
+};
+
+struct kgpu_env_s {
+  int nobj = 0;
+  std::vector<int> groups;
+  std::vector<uint8_t> convex;
+  std::vector<double> margins;
+  std::vector<int> tri_off;
+  // per group BVH (object-aware) over global triangle ids
+  kgpu::HostBvh gbvh[kgpu::kMaxGroups];
+  std::vector<double> tri64;   // global, original order, 9 per tri
+  std::vector<int> tri_obj;
+  double extent = 0.0;
+  // device
+  kgpu::KNode* d_nodes = nullptr;
+  float4* d_tri32 = nullptr;
+  double* d_tri64 = nullptr;
+  double* d_node64 = nullptr;
+  int* d_tri_obj = nullptr;
+  float* d_obj_margin = nullptr;
+  double* d_obj_margin64 = nullptr;
+  int* d_obj_root = nullptr;
+  int* d_obj_group = nullptr;
+  uint8_t* d_obj_convex = nullptr;
+  int* d_node_obj = nullptr;
+  int group_root[kgpu::kMaxGroups];
+  float group_margin[kgpu::kMaxGroups];
+  size_t n_nodes = 0, n_tris = 0;
+};
+
+struct kgpu_world_s {
+  kgpu_env env = nullptr;
+  std::vector<kgpu_robot> robots;
+  std::vector<std::vector<uint32_t>> env_mask;     // per robot per link
+  std::vector<std::vector<uint8_t>> self_enabled;  // per robot [L*L]
+  // device copies
+  kgpu::KRobotDev* d_robots = nullptr;
+  uint32_t* d_queries = nullptr;
+  kgpu::KNode* d_lnodes = nullptr;
+  float4* d_ltri32 = nullptr;
+  double* d_ltri64 = nullptr;
+  double* d_lnode64 = nullptr;
+  int* d_status = nullptr;
+  unsigned long long* d_stats = nullptr;
+  std::vector<int> robot_node_base, robot_tri_base;
+  kgpu::KWorldDev dev;
+  kgpu::Scratch scratch;
+  // options
+  double eps_band = 1e-4;
+  int warps_per_block = 8;
+  int blocks_per_sm = 2;
+  int num_sms = 0;
+  bool tables_dirty = true;
+  // pinned staging for the host-buffer entry points
+  void* pinned = nullptr;
+  size_t pinned_bytes = 0;
+  void* dstage = nullptr;
+  size_t dstage_bytes = 0;
+  cudaStream_t host_stream = nullptr;
+};
+
+struct kgpu_edge_plan_s {
+  kgpu_world world = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+namespace kgpu {
+// launchers implemented in the .cu files (return a CUDA error code)
+cudaError_t launch_fk(const KWorldDev& W, int robot, const float* q, int B, float* T,
+                      cudaStream_t s);
+cudaError_t launch_check_configs(const KWorldDev& W, const Scratch& S, int robot,
+                                 const int* robot_ids, const float* q, int q_stride, int B,
+                                 uint8_t* env_hit, uint8_t* self_hit, uint8_t* feasible,
+                                 int blocks, int warps_per_block, cudaStream_t s);
+cudaError_t launch_check_edges(const KWorldDev& W, const Scratch& S, int robot, const float* qa,
+                               const float* qb, const int* nsteps, int E, int* first_hit,
+                               int blocks, int warps_per_block, cudaStream_t s);
+cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q, int B,
+                                   uint8_t* env_hit, uint8_t* self_hit, cudaStream_t s);
+cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,
+                                 const float* qb, const int* nsteps, int E, int* first_hit,
+                                 cudaStream_t s);
+cudaError_t launch_distance(const KWorldDev& W, const Scratch& S, int robot, const float* q,
+                            int B, double cutoff, double* d, int* pair, double* cp, float* grad,
+                            int blocks, int warps_per_block, cudaStream_t s);
+cudaError_t launch_softmin(const KWorldDev& W, const Scratch& S, int robot, const float* q, int T,
+                           int Wn, double tau, double* L, float* dLdq, int blocks,
+                           int warps_per_block, cudaStream_t s);
+}  // namespace kgpu

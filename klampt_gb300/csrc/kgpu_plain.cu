@@ -1,0 +1,202 @@
+// kgpu_plain.cu — the plain FP64 GPU method, kept as the comparison baseline
+// for the batched engine.
+//
+// One thread per configuration (or per edge, stepping through its
+// configurations in order), FP64 forward kinematics, FP64 BVH-vs-BVH
+// traversal with a per-thread stack, and the canonical FP64 triangle test on
+// every candidate pair.  No warp cooperation, no FP32 filter, no work queue:
+// this is the straightforward port of the reference's serial loops
+// (Cpp/Planning/RobotCSpace.cpp:786-823, PlannerSettings.cpp:241-331) to one
+// thread each.  Its verdicts equal the oracle's by construction.
+#include <climits>
+
+#include "kgpu_device.cuh"
+
+namespace kgpu {
+
+namespace {
+
+constexpr int kPlainStack = 128;
+
+__device__ __forceinline__ void box64_world(const double* T, const double* n, double* c, double* h)
+{
+  for (int r = 0; r < 3; ++r) {
+    c[r] = T[3 * r] * n[0] + T[3 * r + 1] * n[1] + T[3 * r + 2] * n[2] + T[9 + r];
+    h[r] = fabs(T[3 * r]) * n[3] + fabs(T[3 * r + 1]) * n[4] + fabs(T[3 * r + 2]) * n[5];
+  }
+}
+
+// 0 free, 1 hit, 2 stack overflow
+__device__ int plain_query(const KWorldDev& W, const KRobotDev& R, const double (*T)[12], int la,
+                           int tgt)
+{
+  int ra = R.link_root[la];
+  int rb = tgt < 32 ? R.link_root[tgt] : W.group_root[tgt - 32];
+  if (ra < 0 || rb < 0) return 0;
+  double mA = R.link_margin64[la];
+  double mB = tgt < 32 ? R.link_margin64[tgt] : (double)W.group_margin[tgt - 32];
+  double tol = 1e-9 + mA + mB;
+  int2 st[kPlainStack];
+  int top = 0;
+  st[top++] = make_int2(ra, rb);
+  while (top > 0) {
+    int2 pr = st[--top];
+    const double* na = W.lnode64 + 6 * (size_t)pr.x;
+    const double* nb = tgt < 32 ? W.lnode64 + 6 * (size_t)pr.y : W.enode64 + 6 * (size_t)pr.y;
+    double ca[3], ha[3], cb[3], hb[3];
+    box64_world(T[la], na, ca, ha);
+    if (tgt < 32) box64_world(T[tgt], nb, cb, hb);
+    else for (int i = 0; i < 3; ++i) { cb[i] = nb[i]; hb[i] = nb[3 + i]; }
+    bool sep = false;
+    for (int i = 0; i < 3; ++i)
+      if (fabs(ca[i] - cb[i]) > ha[i] + hb[i] + tol) sep = true;
+    if (sep) continue;
+    KNode ka = W.lnodes[pr.x];
+    KNode kb = tgt < 32 ? W.lnodes[pr.y] : W.enodes[pr.y];
+    int cntA = f2i(ka.b.w), cntB = f2i(kb.b.w);
+    int ia = f2i(ka.a.w), ib = f2i(kb.a.w);
+    if (cntA > 0 && cntB > 0) {
+      for (int i = 0; i < cntA; ++i) {
+        double P[9];
+        const double* pa = W.ltri64 + 9 * (size_t)(ia + i);
+        for (int v = 0; v < 3; ++v) kx_xform_point(T[la], pa + 3 * v, P + 3 * v);
+        for (int j = 0; j < cntB; ++j) {
+          double Q[9];
+          double m;
+          if (tgt < 32) {
+            const double* pb = W.ltri64 + 9 * (size_t)(ib + j);
+            for (int v = 0; v < 3; ++v) kx_xform_point(T[tgt], pb + 3 * v, Q + 3 * v);
+            m = kx_add(mA, mB);
+          } else {
+            const double* pb = W.etri64 + 9 * (size_t)(ib + j);
+            for (int k = 0; k < 9; ++k) Q[k] = pb[k];
+            m = kx_add(mA, W.obj_margin64[W.etri_obj[ib + j]]);
+          }
+          int hit;
+          if (m == 0.0) hit = kx_tri_tri_overlap(P, Q);
+          else {
+            double cp[3], cq[3];
+            hit = kx_tri_tri_dist2(P, Q, cp, cq) <= kx_mul(m, m);
+          }
+          if (hit) return 1;
+        }
+      }
+    } else {
+      if (top + 2 > kPlainStack) return 2;
+      bool splitB = cntA > 0 || (cntB == 0 && (kb.b.x + kb.b.y + kb.b.z) > (ka.b.x + ka.b.y + ka.b.z));
+      if (splitB) {
+        st[top++] = make_int2(pr.x, ib + 1);
+        st[top++] = make_int2(pr.x, ib);
+      } else {
+        st[top++] = make_int2(ia + 1, pr.y);
+        st[top++] = make_int2(ia, pr.y);
+      }
+    }
+  }
+  return 0;
+}
+
+__device__ void fk64_all(const KRobotDev& R, const double* q, double (*T)[12])
+{
+  for (int i = 0; i < R.nlinks; ++i) {
+    double Lc[12];
+    kx_joint_local(R.T0P64[i], R.axis64[i], R.jtype[i], q[i], Lc);
+    int p = R.parents[i];
+    if (p < 0) for (int k = 0; k < 12; ++k) T[i][k] = Lc[k];
+    else kx_compose(T[p], Lc, T[i]);
+  }
+}
+
+// returns bit 0 env hit, bit 1 self hit, bit 2 overflow
+__device__ int plain_config(const KWorldDev& W, const KRobotDev& R, const double (*T)[12],
+                            bool do_env, bool do_self, bool stop_any)
+{
+  int res = 0;
+  if (do_env) {
+    for (int k = 0; k < R.nqueries_env; ++k) {
+      uint32_t qw = W.queries[R.query_off + k];
+      int r = plain_query(W, R, T, qw & 0xff, (qw >> 8) & 0xff);
+      if (r == 2) return 4;
+      if (r == 1) { res |= 1; break; }
+    }
+  }
+  if (stop_any && res) return res;
+  if (do_self) {
+    for (int k = 0; k < R.nqueries_self; ++k) {
+      uint32_t qw = W.queries[R.query_off + R.nqueries_env + k];
+      int r = plain_query(W, R, T, qw & 0xff, (qw >> 8) & 0xff);
+      if (r == 2) return 4;
+      if (r == 1) { res |= 2; break; }
+    }
+  }
+  return res;
+}
+
+__global__ void k_plain_configs(KWorldDev W, int robot, const float* q, int B, uint8_t* env_hit,
+                                uint8_t* self_hit)
+{
+  int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const KRobotDev& R = W.robots[robot];
+  double qd[kMaxLinks];
+  for (int i = 0; i < R.nlinks; ++i) {
+    qd[i] = (double)q[(size_t)b * R.nlinks + i];
+    if (!(fabs(qd[i]) < 1.0e6)) { set_status(W, KGPU_ERR_NOT_FINITE); return; }
+  }
+  double T[kMaxLinks][12];
+  fk64_all(R, qd, T);
+  int r = plain_config(W, R, T, env_hit != nullptr, self_hit != nullptr, false);
+  if (r & 4) { set_status(W, KGPU_ERR_OVERFLOW); return; }
+  if (env_hit) env_hit[b] = (r & 1) ? 1 : 0;
+  if (self_hit) self_hit[b] = (r & 2) ? 1 : 0;
+}
+
+__global__ void k_plain_edges(KWorldDev W, int robot, const float* qa, const float* qb,
+                              const int* nsteps, int E, int* first_hit)
+{
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const KRobotDev& R = W.robots[robot];
+  int nl = R.nlinks;
+  int n = nsteps[e];
+  if (n < 1 || n > kMaxSteps) { set_status(W, KGPU_ERR_INVALID); first_hit[e] = -1; return; }
+  int hit = -1;
+  double qd[kMaxLinks];
+  double T[kMaxLinks][12];
+  for (int k = 0; k <= n && hit < 0; ++k) {
+    bool ok = true;
+    for (int i = 0; i < nl; ++i) {
+      qd[i] = kx_interp((double)qa[(size_t)e * nl + i], (double)qb[(size_t)e * nl + i], k, n);
+      if (!(fabs(qd[i]) < 1.0e6)) { set_status(W, KGPU_ERR_NOT_FINITE); first_hit[e] = -1; return; }
+      if (qd[i] < R.qmin64[i] || qd[i] > R.qmax64[i]) ok = false;
+    }
+    if (!ok) { hit = k; break; }
+    fk64_all(R, qd, T);
+    int r = plain_config(W, R, T, true, true, true);
+    if (r & 4) { set_status(W, KGPU_ERR_OVERFLOW); first_hit[e] = -1; return; }
+    if (r) hit = k;
+  }
+  first_hit[e] = hit;
+}
+
+}  // namespace
+
+cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q, int B,
+                                   uint8_t* env_hit, uint8_t* self_hit, cudaStream_t s)
+{
+  if (B <= 0) return cudaSuccess;
+  int tb = 64;
+  k_plain_configs<<<(B + tb - 1) / tb, tb, 0, s>>>(W, robot, q, B, env_hit, self_hit);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa, const float* qb,
+                                 const int* nsteps, int E, int* first_hit, cudaStream_t s)
+{
+  if (E <= 0) return cudaSuccess;
+  int tb = 64;
+  k_plain_edges<<<(E + tb - 1) / tb, tb, 0, s>>>(W, robot, qa, qb, nsteps, E, first_hit);
+  return cudaGetLastError();
+}
+
+}  // namespace kgpu

@@ -1,0 +1,293 @@
+"""World handle over the C ABI: batched FK, collision verdicts, feasibility,
+edge checks, signed distance and soft-min gradients on one GPU.
+
+Device buffers are torch tensors (torch is used for device memory and streams
+only); every query goes through libkgpu.so.  Inputs may be numpy arrays
+(copied to the device) or CUDA tensors (used in place).
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import List, Optional, Sequence
+
+import numpy as np
+import torch
+
+from . import _kgpu
+from ._kgpu import check, lib
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _dptr(t: Optional[torch.Tensor]):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dev(x, dtype) -> torch.Tensor:
+    if isinstance(x, torch.Tensor):
+        t = x.to(device="cuda", dtype=dtype)
+    else:
+        t = torch.as_tensor(np.ascontiguousarray(x), dtype=dtype).cuda()
+    return t.contiguous()
+
+
+class Robot:
+    """Robot handle built from a scenes.RobotSpec-like object (links, parents,
+    T0_parent, axes, joint types, limits, link meshes, margins, self mask)."""
+
+    def __init__(self, spec):
+        self.spec = spec
+        self.num_links = spec.num_links
+        p = spec.packed()
+        self._arrays = p
+        d = _kgpu.RobotDesc(
+            num_links=self.num_links, parents=_ptr(p["parents"]), joint_types=_ptr(p["joint_types"]),
+            T0_parent=_ptr(p["T0_parent"]), axes=_ptr(p["axes"]), qmin=_ptr(p["qmin"]), qmax=_ptr(p["qmax"]),
+            vert_offset=_ptr(p["vert_offset"]), verts=_ptr(p["verts"]), tri_offset=_ptr(p["tri_offset"]),
+            tris=_ptr(p["tris"]), margins=_ptr(p["margins"]), self_mask=_ptr(p["self_mask"]))
+        h = ctypes.c_void_p()
+        check(lib().kgpu_robot_create(ctypes.byref(d), ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().kgpu_robot_destroy(self.handle)
+            self.handle = None
+
+
+class Environment:
+    """Static environment handle from a scenes.EnvSpec-like object."""
+
+    def __init__(self, spec):
+        self.spec = spec
+        p = spec.packed()
+        self._arrays = p
+        d = _kgpu.EnvDesc(num_objects=spec.num_objects, vert_offset=_ptr(p["vert_offset"]),
+                          verts=_ptr(p["verts"]), tri_offset=_ptr(p["tri_offset"]), tris=_ptr(p["tris"]),
+                          groups=_ptr(p["groups"]), convex=_ptr(p["convex"]), margins=_ptr(p["margins"]))
+        h = ctypes.c_void_p()
+        check(lib().kgpu_env_create(ctypes.byref(d), ctypes.byref(h)))
+        self.handle = h
+
+    def close(self):
+        if self.handle:
+            lib().kgpu_env_destroy(self.handle)
+            self.handle = None
+
+
+class EdgePlan:
+    """A captured CUDA graph of one edge-check batch over fixed device buffers."""
+
+    def __init__(self, world: "World", robot: int, qa: torch.Tensor, qb: torch.Tensor, nsteps: torch.Tensor,
+                 first_hit: torch.Tensor):
+        self.world = world
+        self._keep = (qa, qb, nsteps, first_hit)
+        h = ctypes.c_void_p()
+        check(lib().kgpu_edge_plan_create(world.handle, robot, _dptr(qa), _dptr(qb), _dptr(nsteps), qa.shape[0],
+                                          _dptr(first_hit), ctypes.byref(h)))
+        self.handle = h
+
+    def launch(self):
+        check(lib().kgpu_edge_plan_launch(self.handle, _stream()))
+
+    def close(self):
+        if self.handle:
+            lib().kgpu_edge_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class World:
+    """An environment plus robots on the current CUDA device."""
+
+    def __init__(self, env_spec, robot_specs: Sequence):
+        self.env = Environment(env_spec) if env_spec is not None else None
+        self.robots: List[Robot] = [Robot(s) for s in robot_specs]
+        arr = (ctypes.c_void_p * len(self.robots))(*[r.handle.value for r in self.robots])
+        h = ctypes.c_void_p()
+        check(lib().kgpu_world_create(self.env.handle if self.env else None, arr, len(self.robots),
+                                      ctypes.byref(h)))
+        self.handle = h
+
+    # ---- lifetime --------------------------------------------------------
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().kgpu_world_destroy(self.handle)
+            self.handle = None
+        for r in getattr(self, "robots", []):
+            r.close()
+        if getattr(self, "env", None):
+            self.env.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # ---- settings ----------------------------------------------------------
+    def set_option(self, name: str, value: float):
+        check(lib().kgpu_world_set_option(self.handle, name.encode(), float(value)))
+
+    def get_option(self, name: str) -> float:
+        v = ctypes.c_double()
+        check(lib().kgpu_world_get_option(self.handle, name.encode(), ctypes.byref(v)))
+        return v.value
+
+    def set_link_env_mask(self, robot: int, link: int, mask: int):
+        check(lib().kgpu_world_set_link_env_mask(self.handle, robot, link, ctypes.c_uint32(mask & 0xFFFFFFFF)))
+
+    def enable_self_pair(self, robot: int, i: int, j: int, enabled: bool):
+        check(lib().kgpu_world_enable_self_pair(self.handle, robot, i, j, 1 if enabled else 0))
+
+    def sync(self):
+        check(lib().kgpu_world_sync(self.handle, _stream()))
+
+    def stats(self) -> dict:
+        s = _kgpu.Stats()
+        check(lib().kgpu_world_get_stats(self.handle, ctypes.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in _kgpu.Stats._fields_}
+
+    def reset_stats(self):
+        check(lib().kgpu_world_reset_stats(self.handle))
+
+    # ---- queries (device) ----------------------------------------------------
+    def fk(self, q, robot: int = 0, sync: bool = True) -> torch.Tensor:
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L)
+        T = torch.empty((qd.shape[0], L, 12), dtype=torch.float32, device="cuda")
+        check(lib().kgpu_fk(self.handle, robot, _dptr(qd), qd.shape[0], _dptr(T), _stream()))
+        if sync:
+            self.sync()
+        return T
+
+    def check_configs(self, q, robot: int = 0, env: bool = True, self_collision: bool = True,
+                      sync: bool = True):
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L)
+        B = qd.shape[0]
+        eh = torch.zeros(B, dtype=torch.uint8, device="cuda") if env else None
+        sh = torch.zeros(B, dtype=torch.uint8, device="cuda") if self_collision else None
+        check(lib().kgpu_check_configs(self.handle, robot, _dptr(qd), B, _dptr(eh), _dptr(sh), _stream()))
+        if sync:
+            self.sync()
+        return eh, sh
+
+    def check_configs_multi(self, robot_ids, q, sync: bool = True):
+        ids = _dev(robot_ids, torch.int32).reshape(-1)
+        qd = _dev(q, torch.float32)
+        B = ids.shape[0]
+        qd = qd.reshape(B, -1)
+        eh = torch.zeros(B, dtype=torch.uint8, device="cuda")
+        sh = torch.zeros(B, dtype=torch.uint8, device="cuda")
+        check(lib().kgpu_check_configs_multi(self.handle, _dptr(ids), _dptr(qd), qd.shape[1], B, _dptr(eh),
+                                             _dptr(sh), _stream()))
+        if sync:
+            self.sync()
+        return eh, sh
+
+    def is_feasible(self, q, robot: int = 0, sync: bool = True) -> torch.Tensor:
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L)
+        out = torch.zeros(qd.shape[0], dtype=torch.uint8, device="cuda")
+        check(lib().kgpu_is_feasible(self.handle, robot, _dptr(qd), qd.shape[0], _dptr(out), _stream()))
+        if sync:
+            self.sync()
+        return out
+
+    def check_edges(self, qa, qb, nsteps, robot: int = 0, sync: bool = True) -> torch.Tensor:
+        L = self.robots[robot].num_links
+        a = _dev(qa, torch.float32).reshape(-1, L)
+        b = _dev(qb, torch.float32).reshape(-1, L)
+        n = _dev(nsteps, torch.int32).reshape(-1)
+        out = torch.empty(a.shape[0], dtype=torch.int32, device="cuda")
+        check(lib().kgpu_check_edges(self.handle, robot, _dptr(a), _dptr(b), _dptr(n), a.shape[0], _dptr(out),
+                                     _stream()))
+        if sync:
+            self.sync()
+        return out
+
+    def check_configs_plain64(self, q, robot: int = 0, sync: bool = True):
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L)
+        B = qd.shape[0]
+        eh = torch.zeros(B, dtype=torch.uint8, device="cuda")
+        sh = torch.zeros(B, dtype=torch.uint8, device="cuda")
+        check(lib().kgpu_check_configs_plain64(self.handle, robot, _dptr(qd), B, _dptr(eh), _dptr(sh), _stream()))
+        if sync:
+            self.sync()
+        return eh, sh
+
+    def check_edges_plain64(self, qa, qb, nsteps, robot: int = 0, sync: bool = True) -> torch.Tensor:
+        L = self.robots[robot].num_links
+        a = _dev(qa, torch.float32).reshape(-1, L)
+        b = _dev(qb, torch.float32).reshape(-1, L)
+        n = _dev(nsteps, torch.int32).reshape(-1)
+        out = torch.empty(a.shape[0], dtype=torch.int32, device="cuda")
+        check(lib().kgpu_check_edges_plain64(self.handle, robot, _dptr(a), _dptr(b), _dptr(n), a.shape[0],
+                                             _dptr(out), _stream()))
+        if sync:
+            self.sync()
+        return out
+
+    def edge_plan(self, qa: torch.Tensor, qb: torch.Tensor, nsteps: torch.Tensor, first_hit: torch.Tensor,
+                  robot: int = 0) -> EdgePlan:
+        return EdgePlan(self, robot, qa, qb, nsteps, first_hit)
+
+    def distance(self, q, cutoff: float, robot: int = 0, want_grad: bool = True, sync: bool = True):
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L)
+        B = qd.shape[0]
+        d = torch.empty(B, dtype=torch.float64, device="cuda")
+        pair = torch.empty((B, 2), dtype=torch.int32, device="cuda")
+        cp = torch.empty((B, 6), dtype=torch.float64, device="cuda")
+        g = torch.empty((B, L), dtype=torch.float32, device="cuda") if want_grad else None
+        check(lib().kgpu_distance(self.handle, robot, _dptr(qd), B, float(cutoff), _dptr(d), _dptr(pair), _dptr(cp),
+                                  _dptr(g), _stream()))
+        if sync:
+            self.sync()
+        return d, pair, cp, g
+
+    def softmin(self, q, tau: float, robot: int = 0, want_grad: bool = True, sync: bool = True):
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32)
+        T, W = qd.shape[0], qd.shape[1]
+        qd = qd.reshape(T, W, L).contiguous()
+        out = torch.empty(T, dtype=torch.float64, device="cuda")
+        g = torch.empty((T, W, L), dtype=torch.float32, device="cuda") if want_grad else None
+        check(lib().kgpu_softmin_grad(self.handle, robot, _dptr(qd), T, W, float(tau), _dptr(out), _dptr(g),
+                                      _stream()))
+        if sync:
+            self.sync()
+        return out, g
+
+    # ---- queries (host buffers, through the C ABI's pinned staging) -----------
+    def check_configs_host(self, q: np.ndarray, robot: int = 0):
+        L = self.robots[robot].num_links
+        q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, L)
+        B = q.shape[0]
+        eh = np.zeros(B, np.uint8)
+        sh = np.zeros(B, np.uint8)
+        check(lib().kgpu_check_configs_host(self.handle, robot, _ptr(q), B, _ptr(eh), _ptr(sh)))
+        return eh, sh
+
+    def check_edges_host(self, qa: np.ndarray, qb: np.ndarray, nsteps: np.ndarray, robot: int = 0) -> np.ndarray:
+        L = self.robots[robot].num_links
+        qa = np.ascontiguousarray(qa, dtype=np.float32).reshape(-1, L)
+        qb = np.ascontiguousarray(qb, dtype=np.float32).reshape(-1, L)
+        n = np.ascontiguousarray(nsteps, dtype=np.int32).reshape(-1)
+        out = np.zeros(qa.shape[0], np.int32)
+        check(lib().kgpu_check_edges_host(self.handle, robot, _ptr(qa), _ptr(qb), _ptr(n), qa.shape[0], _ptr(out)))
+        return out

@@ -1,0 +1,196 @@
+"""ctypes driver of the FP64 CPU oracle (oracle/oracle.cpp).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, by ``__graft_entry__.smoke()``
+and by the CPU-baseline leg of ``bench.py`` as the checker.  The engine never
+imports this module.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+from typing import Optional
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "liboracle.so")
+
+_lib = None
+
+
+def build(force: bool = False) -> str:
+    """Compiles the oracle (make in oracle/); returns the library path."""
+    src = os.path.join(HERE, "oracle.cpp")
+    hdr = os.path.join(HERE, "..", "include", "kgpu_exact.h")
+    stale = (not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
+        os.path.getmtime(src), os.path.getmtime(hdr)))
+    if force or stale:
+        subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "all"], check=True)
+    return LIB_PATH
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = ctypes.CDLL(LIB_PATH)
+        P = ctypes.c_void_p
+        L.orc_robot_create.restype = P
+        L.orc_env_create.restype = P
+        for name in ("orc_check_configs", "orc_check_edges", "orc_is_feasible", "orc_pair_distance",
+                     "orc_min_distance", "orc_softmin", "orc_tri_tri"):
+            getattr(L, name).restype = ctypes.c_int
+        L.orc_robot_destroy.argtypes = [P]
+        L.orc_env_destroy.argtypes = [P]
+        _lib = L
+    return _lib
+
+
+def _p(a: Optional[np.ndarray]):
+    if a is None:
+        return None
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def default_masks(robot_spec, env_spec) -> np.ndarray:
+    """Klamp't default masks (PlannerSettings.cpp:16-42): every link against
+    rigid objects (group 0) and other groups, links with parent -1 not
+    against terrains (group 1)."""
+    L = robot_spec.num_links
+    m = np.full(ORC_MAXL, 0xFFFFFFFF, dtype=np.uint32)
+    for i in range(L):
+        if int(robot_spec.parents[i]) < 0:
+            m[i] &= np.uint32(~(1 << 1) & 0xFFFFFFFF)
+    return m
+
+
+ORC_MAXL = 32
+
+
+class Oracle:
+    """FP64 oracle over one robot and one environment."""
+
+    def __init__(self, robot_spec, env_spec, masks: Optional[np.ndarray] = None):
+        L = lib()
+        self.robot_spec = robot_spec
+        self.env_spec = env_spec
+        self.nl = robot_spec.num_links
+        r = robot_spec.packed()
+        self._keep = [r]
+        self.robot = L.orc_robot_create(
+            ctypes.c_int(self.nl), _p(r["parents"]), _p(r["joint_types"]), _p(r["T0_parent"]),
+            _p(r["axes"]), _p(r["qmin"]), _p(r["qmax"]), _p(r["vert_offset"]), _p(r["verts"]),
+            _p(r["tri_offset"]), _p(r["tris"]), _p(r["margins"]), _p(r["self_mask"]))
+        self.env = None
+        if env_spec is not None:
+            e = env_spec.packed()
+            self._keep.append(e)
+            self.env = L.orc_env_create(
+                ctypes.c_int(env_spec.num_objects), _p(e["vert_offset"]), _p(e["verts"]),
+                _p(e["tri_offset"]), _p(e["tris"]), _p(e["groups"]), _p(e["convex"]),
+                _p(e["margins"]))
+        self.masks = np.ascontiguousarray(
+            masks if masks is not None else default_masks(robot_spec, env_spec), dtype=np.uint32)
+
+    def close(self):
+        L = lib()
+        if self.robot:
+            L.orc_robot_destroy(ctypes.c_void_p(self.robot))
+            self.robot = None
+        if self.env:
+            L.orc_env_destroy(ctypes.c_void_p(self.env))
+            self.env = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def fk(self, q) -> np.ndarray:
+        q = np.ascontiguousarray(q, dtype=np.float64)
+        T = np.empty((self.nl, 12), np.float64)
+        lib().orc_fk(ctypes.c_void_p(self.robot), _p(q), _p(T))
+        return T
+
+    def check_configs(self, q, nthreads: int = 1, want_env=True, want_self=True):
+        q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, self.nl)
+        B = q.shape[0]
+        env_hit = np.zeros(B, np.uint8) if want_env else None
+        self_hit = np.zeros(B, np.uint8) if want_self else None
+        cnt = np.zeros(3, np.int64)
+        lib().orc_check_configs(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(self.masks),
+                                _p(q), ctypes.c_int(B), _p(env_hit), _p(self_hit),
+                                ctypes.c_int(nthreads), _p(cnt))
+        return env_hit, self_hit, cnt
+
+    def is_feasible(self, q, nthreads: int = 1) -> np.ndarray:
+        q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, self.nl)
+        out = np.zeros(q.shape[0], np.uint8)
+        lib().orc_is_feasible(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(self.masks),
+                              _p(q), ctypes.c_int(q.shape[0]), _p(out), ctypes.c_int(nthreads))
+        return out
+
+    def check_edges(self, qa, qb, nsteps, nthreads: int = 1):
+        qa = np.ascontiguousarray(qa, dtype=np.float32).reshape(-1, self.nl)
+        qb = np.ascontiguousarray(qb, dtype=np.float32).reshape(-1, self.nl)
+        ns = np.ascontiguousarray(nsteps, dtype=np.int32)
+        E = qa.shape[0]
+        out = np.zeros(E, np.int32)
+        cnt = np.zeros(3, np.int64)
+        lib().orc_check_edges(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(self.masks),
+                              _p(qa), _p(qb), _p(ns), ctypes.c_int(E), _p(out),
+                              ctypes.c_int(nthreads), _p(cnt))
+        return out, cnt
+
+    def pair_distance(self, q, link: int, obj: int, bound: float = 1e300):
+        q = np.ascontiguousarray(q, dtype=np.float32).reshape(self.nl)
+        out = np.zeros(10, np.float64)
+        feat = np.zeros(3, np.int32)
+        found = lib().orc_pair_distance(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(q),
+                                        ctypes.c_int(link), ctypes.c_int(obj), ctypes.c_double(bound),
+                                        _p(out), _p(feat))
+        return dict(found=bool(found), d=out[0], cp=out[1:4], cq=out[4:7], dir=out[7:10],
+                    feat=feat[:2].copy(), signed=bool(feat[2]))
+
+    def min_distance(self, q, cutoff: float, nthreads: int = 1, want_grad=True):
+        q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, self.nl)
+        B = q.shape[0]
+        d = np.zeros(B, np.float64)
+        pair = np.zeros((B, 2), np.int32)
+        cp = np.zeros((B, 6), np.float64)
+        grad = np.zeros((B, self.nl), np.float64) if want_grad else None
+        lib().orc_min_distance(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(self.masks),
+                               _p(q), ctypes.c_int(B), ctypes.c_double(cutoff), _p(d), _p(pair),
+                               _p(cp), _p(grad), ctypes.c_int(nthreads))
+        return d, pair, cp, grad
+
+    def softmin(self, q, tau: float, nthreads: int = 1, want_grad=True):
+        q = np.ascontiguousarray(q, dtype=np.float32)
+        T, W = q.shape[0], q.shape[1]
+        Lout = np.zeros(T, np.float64)
+        grad = np.zeros((T, W, self.nl), np.float64) if want_grad else None
+        lib().orc_softmin(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(self.masks),
+                          _p(q), ctypes.c_int(T), ctypes.c_int(W), ctypes.c_double(tau),
+                          _p(Lout), _p(grad), ctypes.c_int(nthreads))
+        return Lout, grad
+
+
+def sincos(x) -> tuple:
+    x = np.ascontiguousarray(x, dtype=np.float64)
+    s = np.empty_like(x)
+    c = np.empty_like(x)
+    lib().orc_sincos(_p(x), ctypes.c_int(x.size), _p(s), _p(c))
+    return s, c
+
+
+def tri_tri(P, Q):
+    P = np.ascontiguousarray(P, dtype=np.float64).reshape(9)
+    Q = np.ascontiguousarray(Q, dtype=np.float64).reshape(9)
+    d2 = np.zeros(1, np.float64)
+    cp = np.zeros(3, np.float64)
+    cq = np.zeros(3, np.float64)
+    hit = lib().orc_tri_tri(_p(P), _p(Q), _p(d2), _p(cp), _p(cq))
+    return bool(hit), float(d2[0]), cp, cq

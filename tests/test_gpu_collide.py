@@ -1,0 +1,187 @@
+"""GPU parity of the collision engine against the FP64 oracle (bit-exact
+booleans / indices), through the C ABI."""
+
+import os
+
+import numpy as np
+import pytest
+
+from klampt_gb300 import scenes as sc
+
+pytestmark = pytest.mark.gpu
+
+NT = os.cpu_count() or 4
+
+
+@pytest.fixture(scope="module")
+def built():
+    from klampt_gb300 import build
+    build.build()
+    from oracle import oracle_py
+    oracle_py.build()
+    return True
+
+
+@pytest.fixture(scope="module")
+def cfg0(built):
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robot, env, q = sc.scene_cfg0()
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    yield robot, env, q, w, o
+    w.close()
+
+
+@pytest.fixture(scope="module")
+def cfg1(built):
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robot, env, (qa, qb, ns) = sc.scene_cfg1(n_edges=2048)
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    yield robot, env, (qa, qb, ns), w, o
+    w.close()
+
+
+def test_fk_error_within_band(cfg0):
+    """FP32 forward kinematics stays far inside the inflation band."""
+    robot, env, q, w, o = cfg0
+    T = w.fk(q[:256]).cpu().numpy().astype(np.float64)
+    eps = w.get_option("eps_band")
+    worst = 0.0
+    for b in range(256):
+        T64 = o.fk(q[b].astype(np.float64))
+        # compare where a point at the link's far end lands (lever 0.3 m)
+        for l in range(robot.num_links):
+            R32, t32 = T[b, l, :9].reshape(3, 3), T[b, l, 9:]
+            R64, t64 = T64[l, :9].reshape(3, 3), T64[l, 9:]
+            p = np.array([0.05, 0.05, 0.3])
+            worst = max(worst, np.abs(R32 @ p + t32 - (R64 @ p + t64)).max())
+    assert worst < eps / 8, (worst, eps)
+
+
+def test_cfg0_verdicts_bit_exact(cfg0):
+    robot, env, q, w, o = cfg0
+    eh_o, sh_o, _ = o.check_configs(q, nthreads=NT)
+    eh, sh = w.check_configs(q)
+    eh, sh = eh.cpu().numpy(), sh.cpu().numpy()
+    assert np.array_equal(eh, eh_o), np.flatnonzero(eh != eh_o)[:10]
+    assert np.array_equal(sh, sh_o), np.flatnonzero(sh != sh_o)[:10]
+    assert 0.1 < eh.mean() < 0.9 and 0.1 < sh.mean() < 0.9
+
+
+def test_cfg0_plain64_bit_exact(cfg0):
+    robot, env, q, w, o = cfg0
+    eh_o, sh_o, _ = o.check_configs(q[:1024], nthreads=NT)
+    eh, sh = w.check_configs_plain64(q[:1024])
+    assert np.array_equal(eh.cpu().numpy(), eh_o)
+    assert np.array_equal(sh.cpu().numpy(), sh_o)
+
+
+def test_cfg0_env_only_and_self_only(cfg0):
+    robot, env, q, w, o = cfg0
+    eh_o, sh_o, _ = o.check_configs(q[:512], nthreads=NT)
+    eh, sh = w.check_configs(q[:512], env=True, self_collision=False)
+    assert sh is None and np.array_equal(eh.cpu().numpy(), eh_o)
+    eh, sh = w.check_configs(q[:512], env=False, self_collision=True)
+    assert eh is None and np.array_equal(sh.cpu().numpy(), sh_o)
+
+
+def test_cfg0_host_buffers(cfg0):
+    robot, env, q, w, o = cfg0
+    eh_d, sh_d = w.check_configs(q[:1000])
+    eh_h, sh_h = w.check_configs_host(q[:1000])
+    assert np.array_equal(eh_h, eh_d.cpu().numpy()) and np.array_equal(sh_h, sh_d.cpu().numpy())
+
+
+def test_feasibility_matches_oracle(cfg0):
+    robot, env, q, w, o = cfg0
+    qq = q[:1024].copy()
+    qq[::7, 2] = 3.5  # outside the joint limits
+    f_o = o.is_feasible(qq, nthreads=NT)
+    f = w.is_feasible(qq).cpu().numpy()
+    assert np.array_equal(f, f_o)
+    assert f[::7].sum() == 0
+
+
+def test_cfg1_configs_bit_exact(cfg1):
+    robot, env, (qa, qb, ns), w, o = cfg1
+    q = sc.uniform_configs(robot, 2048, np.random.default_rng(7))
+    eh_o, sh_o, _ = o.check_configs(q, nthreads=NT)
+    eh, sh = w.check_configs(q)
+    assert np.array_equal(eh.cpu().numpy(), eh_o)
+    assert np.array_equal(sh.cpu().numpy(), sh_o)
+
+
+def test_cfg1_edges_first_hit_exact(cfg1):
+    robot, env, (qa, qb, ns), w, o = cfg1
+    fh_o, _ = o.check_edges(qa, qb, ns, nthreads=NT)
+    fh = w.check_edges(qa, qb, ns).cpu().numpy()
+    bad = np.flatnonzero(fh != fh_o)
+    assert bad.size == 0, (bad[:10], fh[bad[:10]], fh_o[bad[:10]])
+    assert (fh_o < 0).any() and (fh_o > 0).any()
+
+
+def test_cfg1_edges_plain64_exact(cfg1):
+    robot, env, (qa, qb, ns), w, o = cfg1
+    sel = slice(0, 512)
+    fh_o, _ = o.check_edges(qa[sel], qb[sel], ns[sel], nthreads=NT)
+    fh = w.check_edges_plain64(qa[sel], qb[sel], ns[sel]).cpu().numpy()
+    assert np.array_equal(fh, fh_o)
+
+
+def test_cfg1_edges_host_and_graph(cfg1):
+    import torch
+    robot, env, (qa, qb, ns), w, o = cfg1
+    ref = w.check_edges(qa, qb, ns).cpu().numpy()
+    host = w.check_edges_host(qa, qb, ns)
+    assert np.array_equal(host, ref)
+    a = torch.as_tensor(qa).cuda()
+    b = torch.as_tensor(qb).cuda()
+    n = torch.as_tensor(ns).cuda()
+    out = torch.empty(len(ns), dtype=torch.int32, device="cuda")
+    plan = w.edge_plan(a, b, n, out)
+    for _ in range(3):
+        out.fill_(-7)
+        plan.launch()
+        w.sync()
+        assert np.array_equal(out.cpu().numpy(), ref)
+    plan.close()
+
+
+def test_edges_single_step_and_limits(cfg1):
+    """n = 1 edges (two configurations) and an edge leaving the limits."""
+    robot, env, (qa, qb, ns), w, o = cfg1
+    a = qa[:64].copy()
+    b = qb[:64].copy()
+    n = np.ones(64, np.int32)
+    b[5, 1] = 3.3  # endpoint outside [-pi, pi]
+    fh_o, _ = o.check_edges(a, b, n, nthreads=NT)
+    fh = w.check_edges(a, b, n).cpu().numpy()
+    assert np.array_equal(fh, fh_o)
+    assert fh[5] in (0, 1)
+
+
+def test_bad_step_count_reports_error(cfg1):
+    from klampt_gb300._kgpu import KgpuError, KGPU_ERR_INVALID
+    robot, env, (qa, qb, ns), w, o = cfg1
+    n = ns[:8].copy()
+    n[3] = 0
+    with pytest.raises(KgpuError) as ei:
+        w.check_edges(qa[:8], qb[:8], n)
+    assert ei.value.code == KGPU_ERR_INVALID
+    # the world stays usable afterwards
+    fh = w.check_edges(qa[:8], qb[:8], ns[:8]).cpu().numpy()
+    fh_o, _ = o.check_edges(qa[:8], qb[:8], ns[:8])
+    assert np.array_equal(fh, fh_o)
+
+
+def test_nonfinite_config_reports_error(cfg0):
+    from klampt_gb300._kgpu import KgpuError, KGPU_ERR_NOT_FINITE
+    robot, env, q, w, o = cfg0
+    qq = q[:16].copy()
+    qq[4, 0] = np.nan
+    with pytest.raises(KgpuError) as ei:
+        w.check_configs(qq)
+    assert ei.value.code == KGPU_ERR_NOT_FINITE
