@@ -109,6 +109,8 @@ typedef struct {
   uint64_t tri_pairs;      /* triangle pairs tested in FP32                     */
   uint64_t band_pairs;     /* triangle pairs re-tested in FP64                  */
   uint64_t spills;         /* traversal stack spills to global memory           */
+  uint64_t certified;      /* contacts certified in FP32 (no FP64 needed)       */
+  uint64_t fp64_hits;      /* contacts confirmed by the FP64 re-test            */
 } kgpu_stats;
 
 /* ---- model construction --------------------------------------------------- */

@@ -107,6 +107,7 @@ void free_world_device(kgpu_world w)
 {
   dfree(w->d_robots);
   dfree(w->d_queries);
+  dfree(w->d_dev);
   dfree(w->d_lnodes);
   dfree(w->d_ltri32);
   dfree(w->d_ltri64);
@@ -188,6 +189,8 @@ kgpu_status refresh_tables(kgpu_world w)
   CK(upload(&w->d_queries, queries.data(), queries.size()));
   w->dev.robots = w->d_robots;
   w->dev.queries = w->d_queries;
+  if (!w->d_dev) CK(cudaMalloc((void**)&w->d_dev, sizeof(KWorldDev)));
+  CK(cudaMemcpy(w->d_dev, &w->dev, sizeof(KWorldDev), cudaMemcpyHostToDevice));
   w->tables_dirty = false;
   return KGPU_OK;
 }
@@ -621,6 +624,7 @@ kgpu_status kgpu_world_set_option(kgpu_world w, const char* name, double v)
     if (!(v > 0 && v < 1)) return fail(KGPU_ERR_INVALID, "eps_band must be in (0,1)");
     w->eps_band = v;
     w->dev.eps_band = (float)v;
+    w->tables_dirty = true;
   } else if (!strcmp(name, "warps_per_block")) {
     int k = (int)v;
     if (k != 4 && k != 8 && k != 16) return fail(KGPU_ERR_INVALID, "warps_per_block must be 4, 8 or 16");
@@ -676,6 +680,8 @@ kgpu_status kgpu_world_get_stats(kgpu_world w, kgpu_stats* out)
   out->tri_pairs = s[2];
   out->band_pairs = s[3];
   out->spills = s[4];
+  out->certified = s[5];
+  out->fp64_hits = s[6];
   return KGPU_OK;
 }
 
@@ -691,7 +697,7 @@ kgpu_status kgpu_fk(kgpu_world w, int32_t robot, const float* q, int32_t B, floa
   kgpu_status st = check_world(w, robot);
   if (st) return st;
   if (B < 0 || (B > 0 && (!q || !T))) return fail(KGPU_ERR_INVALID, "bad buffers");
-  return launch_status(launch_fk(w->dev, robot, q, B, T, (cudaStream_t)s), "kgpu_fk");
+  return launch_status(launch_fk(w->d_dev, robot, q, B, T, (cudaStream_t)s), "kgpu_fk");
 }
 
 kgpu_status kgpu_check_configs(kgpu_world w, int32_t robot, const float* q, int32_t B,
@@ -701,7 +707,7 @@ kgpu_status kgpu_check_configs(kgpu_world w, int32_t robot, const float* q, int3
   if (st) return st;
   if (B < 0 || (B > 0 && !q)) return fail(KGPU_ERR_INVALID, "bad buffers");
   if (!env_hit && !self_hit) return KGPU_OK;
-  return launch_status(launch_check_configs(w->dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
+  return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
                                             env_hit, self_hit, nullptr, grid_blocks(w), w->warps_per_block,
                                             (cudaStream_t)s),
                        "kgpu_check_configs");
@@ -719,7 +725,7 @@ kgpu_status kgpu_check_configs_multi(kgpu_world w, const int32_t* robot_ids, con
   if (B < 0 || (B > 0 && (!q || !robot_ids)) || q_stride < maxl)
     return fail(KGPU_ERR_INVALID, "bad buffers or q_stride %d < max links %d", q_stride, maxl);
   if (!env_hit && !self_hit) return KGPU_OK;
-  return launch_status(launch_check_configs(w->dev, w->scratch, -1, robot_ids, q, q_stride, B, env_hit, self_hit,
+  return launch_status(launch_check_configs(w->d_dev, w->scratch, -1, robot_ids, q, q_stride, B, env_hit, self_hit,
                                             nullptr, grid_blocks(w), w->warps_per_block, (cudaStream_t)s),
                        "kgpu_check_configs_multi");
 }
@@ -730,7 +736,7 @@ kgpu_status kgpu_is_feasible(kgpu_world w, int32_t robot, const float* q, int32_
   kgpu_status st = check_world(w, robot);
   if (st) return st;
   if (B < 0 || (B > 0 && (!q || !feasible))) return fail(KGPU_ERR_INVALID, "bad buffers");
-  return launch_status(launch_check_configs(w->dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
+  return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
                                             nullptr, nullptr, feasible, grid_blocks(w), w->warps_per_block,
                                             (cudaStream_t)s),
                        "kgpu_is_feasible");
@@ -743,7 +749,7 @@ kgpu_status kgpu_check_edges(kgpu_world w, int32_t robot, const float* qa, const
   if (st) return st;
   if (E < 0 || (E > 0 && (!qa || !qb || !nsteps || !first_hit))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if ((st = ensure_edge_scratch(w, E))) return st;
-  return launch_status(launch_check_edges(w->dev, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
+  return launch_status(launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
                                           w->warps_per_block, (cudaStream_t)s),
                        "kgpu_check_edges");
 }
@@ -879,7 +885,7 @@ kgpu_status kgpu_edge_plan_create(kgpu_world w, int32_t robot, const float* qa, 
   p->world = w;
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaError_t le = launch_check_edges(w->dev, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
+    cudaError_t le = launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
                                         w->warps_per_block, cs);
     e = cudaStreamEndCapture(cs, &p->graph);
     if (e == cudaSuccess && le != cudaSuccess) e = le;

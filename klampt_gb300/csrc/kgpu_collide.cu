@@ -22,12 +22,15 @@
 //     32 lanes stay busy across queries.  Lanes pop 32 pairs, test them, and
 //     push children with ballot/popc compaction; leaf/leaf pairs become
 //     triangle-pair jobs that are expanded one triangle pair per lane.
-//   * A triangle pair the FP32 filter cannot separate is re-tested in FP64
-//     by the lane that holds it (band_retest); the first confirmed contact
-//     ends the query set.
+//   * A triangle pair the FP32 filter cannot separate is either certified
+//     as a contact in FP32 (tri_certain_hit32) or re-tested in FP64
+//     (band_retest on FP64 transforms computed once per configuration).
 //   * The shared-memory stack spills its lower half to a per-warp region of
 //     global scratch when full; exhausting that region sets
 //     KGPU_ERR_OVERFLOW instead of dropping work.
+//   * Code size matters more than inlining here: the traversal and the
+//     triangle jobs are out-of-line functions with rolled loops, so the hot
+//     loop stays resident in the instruction cache.
 #include <climits>
 
 #include "kgpu_device.cuh"
@@ -79,7 +82,7 @@ struct EngineArgs {
 };
 
 struct Cnt {
-  unsigned long long items = 0, node_pairs = 0, tri_pairs = 0, band = 0, spills = 0;
+  unsigned long long node_pairs = 0, tri_pairs = 0, band = 0, spills = 0, cert = 0, hit64 = 0;
 };
 
 // Result of one query set.
@@ -95,11 +98,12 @@ __device__ __forceinline__ uint2 make_entry(int nodeA, int la, int tgt, int node
 // (separated beyond the band: done), FP32 intersection certificate (crossing
 // beyond the band: contact), otherwise the FP64 re-test on transforms
 // computed once per configuration (fk64 tracks whether S.T64 is valid).
-__device__ bool run_jobs(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, int njobs, int lane,
-                         int& fk64, Cnt& cnt)
+__device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                      int njobs, int lane, int& fk64, Cnt& cnt)
 {
   // exclusive prefix over job sizes
   uint32_t carry = 0;
+#pragma unroll 1
   for (int b = 0; b < njobs; b += 32) {
     int j = b + lane;
     uint32_t c = 0;
@@ -120,7 +124,10 @@ __device__ bool run_jobs(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, in
   if (lane == 0) S.jobOff[njobs] = carry;
   __syncwarp();
   const uint32_t total = carry;
-  const float eps = W.eps_band;
+  const float eps = W->eps_band;
+  const float4* __restrict__ ltri = W->ltri32;
+  const float4* __restrict__ etri = W->etri32;
+#pragma unroll 1
   for (uint32_t base = 0; base < total; base += 32) {
     uint32_t p = base + lane;
     bool band = false, certain = false;
@@ -132,44 +139,36 @@ __device__ bool run_jobs(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, in
         int mid = (lo + hi + 1) >> 1;
         if (S.jobOff[mid] <= p) lo = mid; else hi = mid - 1;
       }
-      int j = lo;
-      uint32_t r = p - S.jobOff[j];
-      uint32_t jm = S.jobM[j];
-      uint32_t cb = ((jm >> 16) & 3u) + 1;
+      const int j = lo;
+      const uint32_t r = p - S.jobOff[j];
+      const uint32_t jm = S.jobM[j];
+      const uint32_t cb = ((jm >> 16) & 3u) + 1;
       la = jm & 0xff;
       tgt = (jm >> 8) & 0xff;
       tA = (int)(S.jobA[j] & 0x0fffffffu) + (int)(r / cb);
       tB = (int)S.jobB[j] + (int)(r % cb);
       float3 P[3], Q[3];
       const float* TA = S.T[la];
+      const bool self = tgt < 32;
+      const float* TB = S.T[self ? tgt : 0];
+      const float4* qsrc = self ? ltri : etri;
 #pragma unroll
       for (int v = 0; v < 3; ++v) {
-        float4 x = __ldg(W.ltri32 + 3 * (size_t)tA + v);
+        float4 x = __ldg(ltri + 3 * (size_t)tA + v);
         P[v] = xform32(TA, make_float3(x.x, x.y, x.z));
+        float4 y = __ldg(qsrc + 3 * (size_t)tB + v);
+        Q[v] = self ? xform32(TB, make_float3(y.x, y.y, y.z)) : make_float3(y.x, y.y, y.z);
       }
-      float margin = R.link_margin[la];
-      if (tgt < 32) {
-        const float* TB = S.T[tgt];
-#pragma unroll
-        for (int v = 0; v < 3; ++v) {
-          float4 x = __ldg(W.ltri32 + 3 * (size_t)tB + v);
-          Q[v] = xform32(TB, make_float3(x.x, x.y, x.z));
-        }
-        margin += R.link_margin[tgt];
-      } else {
-#pragma unroll
-        for (int v = 0; v < 3; ++v) {
-          float4 x = __ldg(W.etri32 + 3 * (size_t)tB + v);
-          Q[v] = make_float3(x.x, x.y, x.z);
-        }
-        margin += W.group_margin[tgt - 32];
-      }
+      float margin = R.link_margin[la] + (self ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
       band = !tri_separated32(P, Q, eps, margin);
-      if (band && margin == 0.f) certain = tri_certain_hit32(P, Q, eps);
+      if (band && margin == 0.f) certain = tri_certain_hit32(P[0], P[1], P[2], Q[0], Q[1], Q[2], eps);
     }
     cnt.tri_pairs += (p < total) ? 1 : 0;
-    if (__any_sync(0xffffffffu, certain)) return true;
-    bool need64 = band && !certain;
+    if (__any_sync(0xffffffffu, certain)) {
+      cnt.cert++;
+      return true;
+    }
+    const bool need64 = band && !certain;
     if (__any_sync(0xffffffffu, need64)) {
       if (!fk64) {
         warp_fk64(R, S.q64, S.T64, lane);
@@ -180,78 +179,114 @@ __device__ bool run_jobs(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, in
         cnt.band++;
         hit = band_retest(W, R, S.T64, la, tA, tgt, tB);
       }
-      if (__any_sync(0xffffffffu, hit)) return true;
+      if (__any_sync(0xffffffffu, hit)) {
+        cnt.hit64++;
+        return true;
+      }
     }
   }
   return false;
 }
 
+// Node-pair test for one stack entry; returns 0 (culled), 1 (children in c0,
+// c1) or 2 (leaf job in jA, jB, jM).
+__device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __restrict__ W,
+                                          const KRobotDev& R, uint2 e, float eps, uint2& c0, uint2& c1,
+                                          uint32_t& jA, uint32_t& jB, uint32_t& jM)
+{
+  const int nodeA = e.y & 0xfffff;
+  const int la = (e.y >> 20) & 31;
+  const int tgt = (e.y >> 25) & 63;
+  const int nodeB = (int)e.x;
+  const bool self = tgt < 32;
+  const KNode na = W->lnodes[nodeA];
+  const KNode nb = (self ? W->lnodes : W->enodes)[nodeB];
+  const Box32 A = xform_box(S.T[la], na.a, na.b);
+  Box32 Bx;
+  if (self) {
+    Bx = xform_box(S.T[tgt], nb.a, nb.b);
+  } else {
+    Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z);
+    Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z);
+  }
+  const float m = R.link_margin[la] + (self ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
+  if (!boxes_overlap(A, Bx, eps + m)) return 0;
+  const int cntA = f2i(na.b.w), cntB = f2i(nb.b.w);
+  const int ia = f2i(na.a.w), ib = f2i(nb.a.w);
+  if (cntA > 0 && cntB > 0) {
+    jA = (uint32_t)ia | ((uint32_t)(cntA - 1) << 28);
+    jB = (uint32_t)ib;
+    jM = (uint32_t)la | ((uint32_t)tgt << 8) | ((uint32_t)(cntB - 1) << 16);
+    return 2;
+  }
+  const bool splitB = cntA > 0 || (cntB == 0 && (nb.b.x + nb.b.y + nb.b.z) > (na.b.x + na.b.y + na.b.z));
+  if (splitB) {
+    c0 = make_entry(nodeA, la, tgt, ib);
+    c1 = make_entry(nodeA, la, tgt, ib + 1);
+  } else {
+    c0 = make_entry(ia, la, tgt, nodeB);
+    c1 = make_entry(ia + 1, la, tgt, nodeB);
+  }
+  return 1;
+}
+
 // Traverses queries [qbase, qbase+qcount) of robot R for the configuration
 // whose FP32 link transforms are in S.T.  Warp-uniform control flow.
-__device__ int traverse(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, int qbase, int qcount,
-                        int lane, uint2* spill, int spill_cap, int& fk64, Cnt& cnt)
+__device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                     int qbase, int qcount, int lane, uint2* spill, int spill_cap, int& fk64,
+                                     Cnt& cnt)
 {
-  const float eps = W.eps_band;
+  const float eps = W->eps_band;
+  const unsigned lt = lanemask_lt();
   int top = 0, njobs = 0, spill_top = 0;
 
-  auto spill_out = [&]() -> bool {
-    const int H = kStackCap / 2;
-    if (spill_top + H > spill_cap) return false;
-    for (int k = lane; k < H; k += 32) spill[spill_top + k] = S.stack[k];
-    __syncwarp();
-    for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];
-    __syncwarp();
-    spill_top += H;
-    top -= H;
-    cnt.spills++;
-    return true;
-  };
-
   // root pairs of every query, tested in parallel
+#pragma unroll 1
   for (int qb = 0; qb < qcount; qb += 32) {
     if (top > kStackCap - 32) {
-      if (!spill_out()) return TR_OVERFLOW;
+      const int H = kStackCap / 2;
+      if (spill_top + H > spill_cap) return TR_OVERFLOW;
+      for (int k = lane; k < H; k += 32) spill[spill_top + k] = S.stack[k];
+      __syncwarp();
+      for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];
+      __syncwarp();
+      spill_top += H;
+      top -= H;
+      cnt.spills++;
     }
-    int qi = qb + lane;
+    const int qi = qb + lane;
     bool push = false;
     uint2 ent = make_uint2(0, 0);
     if (qi < qcount) {
-      uint32_t qw = __ldg(W.queries + qbase + qi);
-      int a = qw & 0xff, tgt = (qw >> 8) & 0xff;
-      int ra = R.link_root[a];
-      int rb = tgt < 32 ? R.link_root[tgt] : W.group_root[tgt - 32];
+      const uint32_t qw = __ldg(W->queries + qbase + qi);
+      const int a = qw & 0xff, tgt = (qw >> 8) & 0xff;
+      const int ra = R.link_root[a];
+      const int rb = tgt < 32 ? R.link_root[tgt] : W->group_root[tgt - 32];
       if (ra >= 0 && rb >= 0) {
-        KNode na = W.lnodes[ra];
-        Box32 A = xform_box(S.T[a], na.a, na.b);
+        ent = make_entry(ra, a, tgt, rb);
+        // box cull of the root pair; survivors are pushed and expanded below
+        const KNode na = W->lnodes[ra];
+        const KNode nb = (tgt < 32 ? W->lnodes : W->enodes)[rb];
+        const Box32 A = xform_box(S.T[a], na.a, na.b);
         Box32 Bx;
-        float m = R.link_margin[a];
-        if (tgt < 32) {
-          KNode nb = W.lnodes[rb];
-          Bx = xform_box(S.T[tgt], nb.a, nb.b);
-          m += R.link_margin[tgt];
-        } else {
-          KNode nb = W.enodes[rb];
-          Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z);
-          Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z);
-          m += W.group_margin[tgt - 32];
-        }
+        if (tgt < 32) Bx = xform_box(S.T[tgt], nb.a, nb.b);
+        else { Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z); Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z); }
+        const float m = R.link_margin[a] + (tgt < 32 ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
+        push = boxes_overlap(A, Bx, eps + m);
         cnt.node_pairs++;
-        if (boxes_overlap(A, Bx, eps + m)) {
-          push = true;
-          ent = make_entry(ra, a, tgt, rb);
-        }
       }
     }
-    unsigned mp = __ballot_sync(0xffffffffu, push);
-    if (push) S.stack[top + __popc(mp & lanemask_lt())] = ent;
+    const unsigned mp = __ballot_sync(0xffffffffu, push);
+    if (push) S.stack[top + __popc(mp & lt)] = ent;
     top += __popc(mp);
     __syncwarp();
   }
 
+#pragma unroll 1
   for (;;) {
     if (top == 0) {
       if (spill_top > 0) {
-        int n = min(kStackCap / 2, spill_top);
+        const int n = min(kStackCap / 2, spill_top);
         for (int k = lane; k < n; k += 32) S.stack[k] = spill[spill_top - n + k];
         __syncwarp();
         spill_top -= n;
@@ -261,17 +296,25 @@ __device__ int traverse(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, int
       }
     }
     if (njobs > kJobCap - 32 || (top == 0 && njobs > 0)) {
-      bool hit = run_jobs(S, W, R, njobs, lane, fk64, cnt);
+      const bool hit = run_jobs(S, W, R, njobs, lane, fk64, cnt);
       __syncwarp();
       njobs = 0;
       if (hit) return TR_HIT;
       continue;
     }
     if (top > kStackCap - 32) {
-      if (!spill_out()) return TR_OVERFLOW;
+      const int H = kStackCap / 2;
+      if (spill_top + H > spill_cap) return TR_OVERFLOW;
+      for (int k = lane; k < H; k += 32) spill[spill_top + k] = S.stack[k];
+      __syncwarp();
+      for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];
+      __syncwarp();
+      spill_top += H;
+      top -= H;
+      cnt.spills++;
     }
-    int n = min(top, 32);
-    bool have = lane < n;
+    const int n = min(top, 32);
+    const bool have = lane < n;
     uint2 e = make_uint2(0, 0);
     if (have) e = S.stack[top - 1 - lane];
     __syncwarp();
@@ -279,56 +322,16 @@ __device__ int traverse(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, int
     int outcome = 0;  // 1: two children, 2: leaf job
     uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
     uint32_t jA = 0, jB = 0, jM = 0;
-    if (have) {
-      int nodeA = e.y & 0xfffff;
-      int la = (e.y >> 20) & 31;
-      int tgt = (e.y >> 25) & 63;
-      int nodeB = (int)e.x;
-      KNode na = W.lnodes[nodeA];
-      KNode nb = tgt < 32 ? W.lnodes[nodeB] : W.enodes[nodeB];
-      Box32 A = xform_box(S.T[la], na.a, na.b);
-      Box32 Bx;
-      float m = R.link_margin[la];
-      if (tgt < 32) {
-        Bx = xform_box(S.T[tgt], nb.a, nb.b);
-        m += R.link_margin[tgt];
-      } else {
-        Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z);
-        Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z);
-        m += W.group_margin[tgt - 32];
-      }
-      if (boxes_overlap(A, Bx, eps + m)) {
-        int cntA = f2i(na.b.w), cntB = f2i(nb.b.w);
-        int ia = f2i(na.a.w), ib = f2i(nb.a.w);
-        if (cntA > 0 && cntB > 0) {
-          outcome = 2;
-          jA = (uint32_t)ia | ((uint32_t)(cntA - 1) << 28);
-          jB = (uint32_t)ib;
-          jM = (uint32_t)la | ((uint32_t)tgt << 8) | ((uint32_t)(cntB - 1) << 16);
-        } else {
-          outcome = 1;
-          bool splitB = cntA > 0 ||
-                        (cntB == 0 && (nb.b.x + nb.b.y + nb.b.z) > (na.b.x + na.b.y + na.b.z));
-          if (splitB) {
-            c0 = make_entry(nodeA, la, tgt, ib);
-            c1 = make_entry(nodeA, la, tgt, ib + 1);
-          } else {
-            c0 = make_entry(ia, la, tgt, nodeB);
-            c1 = make_entry(ia + 1, la, tgt, nodeB);
-          }
-        }
-      }
-    }
+    if (have) outcome = test_entry(S, W, R, e, eps, c0, c1, jA, jB, jM);
     cnt.node_pairs += have ? 1 : 0;
-    unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
-    unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
-    unsigned lt = lanemask_lt();
+    const unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
+    const unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
     if (outcome == 1) {
-      int r = top + 2 * __popc(m1 & lt);
+      const int r = top + 2 * __popc(m1 & lt);
       S.stack[r] = c1;
       S.stack[r + 1] = c0;
     } else if (outcome == 2) {
-      int r = njobs + __popc(m2 & lt);
+      const int r = njobs + __popc(m2 & lt);
       S.jobA[r] = jA;
       S.jobB[r] = jB;
       S.jobM[r] = jM;
@@ -340,7 +343,8 @@ __device__ int traverse(WarpSmem& S, const KWorldDev& W, const KRobotDev& R, int
 }
 
 template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 16 / WARPS) k_engine(KWorldDev W, EngineArgs A)
+__global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
+    k_engine(const KWorldDev* __restrict__ W, const EngineArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpSmem* all = reinterpret_cast<WarpSmem*>(smem_raw);
@@ -349,14 +353,17 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS) k_engine(KWorldDev W, 
   const int gwarp = blockIdx.x * WARPS + warp;
   uint2* spill = A.spill + (size_t)gwarp * A.spill_per_warp;
   Cnt cnt;
-  int total = A.mode == MODE_EDGES ? A.meta[1] : A.B;
-  int maxn = A.mode == MODE_EDGES ? A.meta[0] : 0;
+  unsigned long long items = 0;
+  const int total = A.mode == MODE_EDGES ? A.meta[1] : A.B;
+  const int maxn = A.mode == MODE_EDGES ? A.meta[0] : 0;
 
+#pragma unroll 1
   for (;;) {
     unsigned int base = 0;
     if (lane == 0) base = atomicAdd(A.head, kGrab);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= (unsigned)total) break;
+#pragma unroll 1
     for (unsigned it = base; it < base + kGrab && it < (unsigned)total; ++it) {
       // ---- decode the item
       int rid = A.robot;
@@ -377,7 +384,7 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS) k_engine(KWorldDev W, 
       } else if (rid < 0) {
         rid = __ldg(A.robot_ids + b);
       }
-      const KRobotDev& R = W.robots[rid];
+      const KRobotDev& R = W->robots[rid];
       const int nl = R.nlinks;
       double q64 = 0.0;
       if (lane < nl) {
@@ -388,12 +395,12 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS) k_engine(KWorldDev W, 
           q64 = (double)__ldg(A.q + (size_t)b * A.q_stride + lane);
         S.q64[lane] = q64;
       }
-      cnt.items++;
-      bool viol = lane < nl && (q64 < R.qmin64[lane] || q64 > R.qmax64[lane]);
-      bool limit_bad = __any_sync(0xffffffffu, viol);
-      bool nonfinite = __any_sync(0xffffffffu, lane < nl && !(fabs(q64) < 1.0e6));
+      items++;
+      const bool viol = lane < nl && (q64 < R.qmin64[lane] || q64 > R.qmax64[lane]);
+      const bool limit_bad = __any_sync(0xffffffffu, viol);
+      const bool nonfinite = __any_sync(0xffffffffu, lane < nl && !(fabs(q64) < 1.0e6));
       if (nonfinite) {
-        if (lane == 0) set_status(W, KGPU_ERR_NOT_FINITE);
+        if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
         continue;
       }
       if (A.mode != MODE_CONFIGS && limit_bad) {
@@ -404,7 +411,7 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS) k_engine(KWorldDev W, 
         continue;
       }
       float P[12];
-      warp_fk32(R, lane, (float)q64, P);
+      warp_fk32(R, lane, q64, P);
       if (lane < nl) {
 #pragma unroll
         for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
@@ -412,16 +419,16 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS) k_engine(KWorldDev W, 
       __syncwarp();
       int env_res = TR_FREE, self_res = TR_FREE;
       int fk64 = 0;
-      bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
-      bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
+      const bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
+      const bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
       if (want_env && R.nqueries_env > 0)
         env_res = traverse(S, W, R, R.query_off, R.nqueries_env, lane, spill, A.spill_per_warp, fk64, cnt);
-      bool stop = A.mode != MODE_CONFIGS && env_res != TR_FREE;
+      const bool stop = A.mode != MODE_CONFIGS && env_res != TR_FREE;
       if (!stop && want_self && R.nqueries_self > 0)
         self_res = traverse(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill,
                             A.spill_per_warp, fk64, cnt);
       if (env_res == TR_OVERFLOW || self_res == TR_OVERFLOW) {
-        if (lane == 0) set_status(W, KGPU_ERR_OVERFLOW);
+        if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
         continue;
       }
       if (lane == 0) {
@@ -437,10 +444,6 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS) k_engine(KWorldDev W, 
       __syncwarp();
     }
   }
-  if (lane == 0 && W.stats) {
-    atomicAdd(W.stats + 0, cnt.items);
-  }
-  // per-lane counters
   unsigned long long np = cnt.node_pairs, tp = cnt.tri_pairs, bd = cnt.band;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -448,11 +451,14 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS) k_engine(KWorldDev W, 
     tp += __shfl_down_sync(0xffffffffu, tp, o);
     bd += __shfl_down_sync(0xffffffffu, bd, o);
   }
-  if (lane == 0 && W.stats) {
-    atomicAdd(W.stats + 1, np);
-    atomicAdd(W.stats + 2, tp);
-    atomicAdd(W.stats + 3, bd);
-    atomicAdd(W.stats + 4, cnt.spills);
+  if (lane == 0 && W->stats) {
+    atomicAdd(W->stats + 0, items);
+    atomicAdd(W->stats + 1, np);
+    atomicAdd(W->stats + 2, tp);
+    atomicAdd(W->stats + 3, bd);
+    atomicAdd(W->stats + 4, cnt.spills);
+    atomicAdd(W->stats + 5, cnt.cert);
+    atomicAdd(W->stats + 6, cnt.hit64);
   }
 }
 
@@ -510,14 +516,14 @@ __global__ void k_edges_finalize(int* first_hit, int E)
   if (e < E && first_hit[e] == INT_MAX) first_hit[e] = -1;
 }
 
-__global__ void k_fk(const KWorldDev W, int robot, const float* q, int B, float* T)
+__global__ void k_fk(const KWorldDev* __restrict__ W, int robot, const float* q, int B, float* T)
 {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= B) return;
-  const KRobotDev& R = W.robots[robot];
+  const KRobotDev& R = W->robots[robot];
   int nl = R.nlinks;
-  float qv = lane < nl ? q[(size_t)warp * nl + lane] : 0.f;
+  double qv = lane < nl ? (double)q[(size_t)warp * nl + lane] : 0.0;
   float P[12];
   warp_fk32(R, lane, qv, P);
   if (lane < nl)
@@ -534,15 +540,14 @@ cudaError_t init_engine()
 // the shared-memory attribute is set once per process by engine_init(), so
 // that launches can be captured into CUDA graphs
 template <int WARPS>
-cudaError_t launch_engine(const KWorldDev& W, const EngineArgs& A, int blocks, cudaStream_t s)
+cudaError_t launch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, cudaStream_t s)
 {
   size_t smem = sizeof(WarpSmem) * WARPS;
   k_engine<WARPS><<<blocks, WARPS * 32, smem, s>>>(W, A);
   return cudaGetLastError();
 }
 
-cudaError_t dispatch_engine(const KWorldDev& W, const EngineArgs& A, int blocks, int warps,
-                            cudaStream_t s)
+cudaError_t dispatch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, int warps, cudaStream_t s)
 {
   switch (warps) {
     case 4: return launch_engine<4>(W, A, blocks, s);
@@ -563,8 +568,7 @@ cudaError_t engine_init()
   return e;
 }
 
-cudaError_t launch_fk(const KWorldDev& W, int robot, const float* q, int B, float* T,
-                      cudaStream_t s)
+cudaError_t launch_fk(const KWorldDev* W, int robot, const float* q, int B, float* T, cudaStream_t s)
 {
   if (B <= 0) return cudaSuccess;
   int threads = 256;
@@ -574,10 +578,9 @@ cudaError_t launch_fk(const KWorldDev& W, int robot, const float* q, int B, floa
   return cudaGetLastError();
 }
 
-cudaError_t launch_check_configs(const KWorldDev& W, const Scratch& S, int robot,
-                                 const int* robot_ids, const float* q, int q_stride, int B,
-                                 uint8_t* env_hit, uint8_t* self_hit, uint8_t* feasible,
-                                 int blocks, int warps_per_block, cudaStream_t s)
+cudaError_t launch_check_configs(const KWorldDev* W, const Scratch& S, int robot, const int* robot_ids,
+                                 const float* q, int q_stride, int B, uint8_t* env_hit, uint8_t* self_hit,
+                                 uint8_t* feasible, int blocks, int warps_per_block, cudaStream_t s)
 {
   if (B <= 0) return cudaSuccess;
   cudaError_t err = cudaMemsetAsync(S.counters, 0, sizeof(unsigned int), s);
@@ -598,9 +601,9 @@ cudaError_t launch_check_configs(const KWorldDev& W, const Scratch& S, int robot
   return dispatch_engine(W, A, blocks, warps_per_block, s);
 }
 
-cudaError_t launch_check_edges(const KWorldDev& W, const Scratch& S, int robot, const float* qa,
-                               const float* qb, const int* nsteps, int E, int* first_hit,
-                               int blocks, int warps_per_block, cudaStream_t s)
+cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S, int robot, const float* qa,
+                               const float* qb, const int* nsteps, int E, int* first_hit, int blocks,
+                               int warps_per_block, cudaStream_t s)
 {
   if (E <= 0) return cudaSuccess;
   cudaError_t err;
@@ -610,7 +613,7 @@ cudaError_t launch_check_edges(const KWorldDev& W, const Scratch& S, int robot, 
   int* fill = S.edge_meta + 4;  // kMaxSteps+2 ints after the meta words
   if ((err = cudaMemsetAsync(fill, 0, sizeof(int) * (kMaxSteps + 2), s)) != cudaSuccess) return err;
   int tb = 256, gb = (E + tb - 1) / tb;
-  k_edges_prep1<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, S.edge_meta, first_hit, W.status);
+  k_edges_prep1<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, S.edge_meta, first_hit, status);
   k_edges_prep2<<<1, 32, 0, s>>>(S.edge_hist, S.edge_round_off, S.edge_meta);
   k_edges_prep3<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, fill, S.edge_perm);
   if ((err = cudaGetLastError()) != cudaSuccess) return err;

@@ -44,14 +44,33 @@ __device__ __forceinline__ float3 xform32(const float* T, float3 v)
                      fmaf(T[6], v.x, fmaf(T[7], v.y, fmaf(T[8], v.z, T[11]))));
 }
 
+// sin and cos of an FP64 angle to FP32 accuracy with little code: the
+// reduction modulo pi/2 runs in FP64 (two FP64 products), the polynomials in
+// FP32 on |r| <= pi/4 (Taylor series to r^9 / r^10, truncation < 3e-9).
+__device__ __forceinline__ void sincos32_of64(double x, float* s, float* c)
+{
+  double k = rint(x * 0.6366197723675814);
+  float r = (float)((x - k * 1.5707963267948966) - k * 6.123233995736766e-17);
+  float r2 = r * r;
+  float ps = fmaf(fmaf(fmaf(fmaf(2.7557319e-06f, r2, -1.98412698e-04f), r2, 8.33333333e-03f), r2,
+                       -1.66666667e-01f), r2 * r, r);
+  float pc = fmaf(fmaf(fmaf(fmaf(fmaf(-2.75573192e-07f, r2, 2.48015873e-05f), r2, -1.38888889e-03f), r2,
+                            4.16666667e-02f), r2, -0.5f), r2, 1.0f);
+  int q = ((int)k) & 3;
+  float sn = (q & 1) ? pc : ps, cs = (q & 1) ? ps : pc;
+  *s = (q & 2) ? -sn : sn;
+  *c = ((q + 1) & 2) ? -cs : cs;
+}
+
 // local transform T0_Parent * J(q) of link i in FP32
-__device__ __forceinline__ void joint_local32(const KRobotDev& R, int i, float q, float* L)
+__device__ __forceinline__ void joint_local32(const KRobotDev& R, int i, double q64, float* L)
 {
   const float* T0 = R.T0P[i];
   int jt = R.jtype[i];
+  float q = (float)q64;
   if (jt == KX_JOINT_REVOLUTE) {
     float s, c;
-    sincosf(q, &s, &c);
+    sincos32_of64(q64, &s, &c);
     float wx = R.axis[i][0], wy = R.axis[i][1], wz = R.axis[i][2];
     float v = 1.f - c;
     float J[12];
@@ -74,7 +93,7 @@ __device__ __forceinline__ void joint_local32(const KRobotDev& R, int i, float q
 // transforms are formed in parallel and chained to the root by pointer
 // jumping (ceil(log2(depth)) rounds of shuffles), which handles serial
 // chains and trees alike.  Result: world transform of link `lane` in P.
-__device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, float q, float* P)
+__device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, double q, float* P)
 {
   int nl = R.nlinks;
   int anc = -1;
@@ -146,22 +165,24 @@ __device__ __forceinline__ bool sep_axis32(float3 a, const float3* p, const floa
   return gap > tol;
 }
 
-// Conservative separation of world-frame triangles P and Q (FP32).
+__device__ __forceinline__ float3 sel3(int i, float3 a, float3 b, float3 c)
+{
+  return i == 0 ? a : (i == 1 ? b : c);
+}
+
+// Conservative separation of world-frame triangles P and Q (FP32): box
+// pre-test, the two face normals, then the 9 edge-edge and 6 in-plane axes in
+// a rolled loop (small code keeps the hot loop in the instruction cache).
 __device__ __forceinline__ bool tri_separated32(const float3* P, const float3* Q, float eps,
                                                 float margin)
 {
-  // box pre-test
-  float3 pmn = make_float3(fminf(P[0].x, fminf(P[1].x, P[2].x)), fminf(P[0].y, fminf(P[1].y, P[2].y)),
-                           fminf(P[0].z, fminf(P[1].z, P[2].z)));
-  float3 pmx = make_float3(fmaxf(P[0].x, fmaxf(P[1].x, P[2].x)), fmaxf(P[0].y, fmaxf(P[1].y, P[2].y)),
-                           fmaxf(P[0].z, fmaxf(P[1].z, P[2].z)));
-  float3 qmn = make_float3(fminf(Q[0].x, fminf(Q[1].x, Q[2].x)), fminf(Q[0].y, fminf(Q[1].y, Q[2].y)),
-                           fminf(Q[0].z, fminf(Q[1].z, Q[2].z)));
-  float3 qmx = make_float3(fmaxf(Q[0].x, fmaxf(Q[1].x, Q[2].x)), fmaxf(Q[0].y, fmaxf(Q[1].y, Q[2].y)),
-                           fmaxf(Q[0].z, fmaxf(Q[1].z, Q[2].z)));
   float bt = eps + margin;
-  if (qmn.x - pmx.x > bt || pmn.x - qmx.x > bt || qmn.y - pmx.y > bt || pmn.y - qmx.y > bt ||
-      qmn.z - pmx.z > bt || pmn.z - qmx.z > bt)
+  if (fminf(Q[0].x, fminf(Q[1].x, Q[2].x)) - fmaxf(P[0].x, fmaxf(P[1].x, P[2].x)) > bt ||
+      fminf(P[0].x, fminf(P[1].x, P[2].x)) - fmaxf(Q[0].x, fmaxf(Q[1].x, Q[2].x)) > bt ||
+      fminf(Q[0].y, fminf(Q[1].y, Q[2].y)) - fmaxf(P[0].y, fmaxf(P[1].y, P[2].y)) > bt ||
+      fminf(P[0].y, fminf(P[1].y, P[2].y)) - fmaxf(Q[0].y, fmaxf(Q[1].y, Q[2].y)) > bt ||
+      fminf(Q[0].z, fminf(Q[1].z, Q[2].z)) - fmaxf(P[0].z, fmaxf(P[1].z, P[2].z)) > bt ||
+      fminf(P[0].z, fminf(P[1].z, P[2].z)) - fmaxf(Q[0].z, fmaxf(Q[1].z, Q[2].z)) > bt)
     return true;
   float3 p[3], q[3];
   p[0] = make_float3(0.f, 0.f, 0.f);
@@ -170,76 +191,77 @@ __device__ __forceinline__ bool tri_separated32(const float3* P, const float3* Q
   q[0] = sub3(Q[0], P[0]);
   q[1] = sub3(Q[1], P[0]);
   q[2] = sub3(Q[2], P[0]);
-  float3 ep[3] = {sub3(p[1], p[0]), sub3(p[2], p[1]), sub3(p[0], p[2])};
-  float3 eq[3] = {sub3(q[1], q[0]), sub3(q[2], q[1]), sub3(q[0], q[2])};
-  float3 np = cross3(ep[0], ep[1]);
-  float3 nq = cross3(eq[0], eq[1]);
+  const float3 ep0 = p[1], ep1 = sub3(p[2], p[1]), ep2 = make_float3(-p[2].x, -p[2].y, -p[2].z);
+  const float3 eq0 = sub3(q[1], q[0]), eq1 = sub3(q[2], q[1]), eq2 = sub3(q[0], q[2]);
+  const float3 np = cross3(ep0, ep1);
+  const float3 nq = cross3(eq0, eq1);
   if (sep_axis32(np, p, q, eps, margin)) return true;
   if (sep_axis32(nq, p, q, eps, margin)) return true;
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      if (sep_axis32(cross3(ep[i], eq[j]), p, q, eps, margin)) return true;
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    if (sep_axis32(cross3(np, ep[i]), p, q, eps, margin)) return true;
-    if (sep_axis32(cross3(nq, eq[i]), p, q, eps, margin)) return true;
+#pragma unroll 1
+  for (int k = 0; k < 15; ++k) {
+    float3 a;
+    if (k < 9) a = cross3(sel3(k / 3, ep0, ep1, ep2), sel3(k % 3, eq0, eq1, eq2));
+    else if (k < 12) a = cross3(np, sel3(k - 9, ep0, ep1, ep2));
+    else a = cross3(nq, sel3(k - 12, eq0, eq1, eq2));
+    if (sep_axis32(a, p, q, eps, margin)) return true;
   }
   return false;
 }
 
-// orient3d(a,b,c,d) = (a-d) . ((b-d) x (c-d))
-__device__ __forceinline__ float orient32(float3 a, float3 b, float3 c, float3 d)
+// Sign of orient3d(a,b,c,d) = det[a-d, b-d, c-d] that holds for every
+// placement of the four points within `delta` (Euclidean) of the given ones,
+// or 0 when the sign is not certain.  With columns u, v, w each moved by at
+// most 2 delta:  |det change| <= 2d(|v||w| + |u||w| + |u||v|)
+// + 4d^2(|u|+|v|+|w|) + 8d^3, plus FP32 rounding <= 12 u |u||v||w|.
+__device__ __forceinline__ int orient_sign32(float3 a, float3 b, float3 c, float3 d, float delta)
 {
-  return dot3(sub3(a, d), cross3(sub3(b, d), sub3(c, d)));
+  float3 u = sub3(a, d), v = sub3(b, d), w = sub3(c, d);
+  float det = dot3(u, cross3(v, w));
+  float nu = sqrtf(dot3(u, u)), nv = sqrtf(dot3(v, v)), nw = sqrtf(dot3(w, w));
+  float B = 2.f * delta * (nv * nw + nu * nw + nu * nv) + 4.f * delta * delta * (nu + nv + nw) +
+            8.f * delta * delta * delta + 12.f * 5.9604645e-08f * nu * nv * nw;
+  B *= 1.01f;
+  return det > B ? 1 : (det < -B ? -1 : 0);
 }
 
-__device__ __forceinline__ int rsign(float x, float B) { return x > B ? 1 : (x < -B ? -1 : 0); }
-
 // Certain intersection of world-frame triangles P and Q despite vertex
-// errors of up to `delta` (Euclidean) per vertex.  An edge of one triangle
-// crossing the other's interior is decided by orientation determinants: its
-// endpoints lie on opposite sides of the other triangle's plane and the three
-// edge-edge orientations agree in sign.  Each determinant's sign is trusted
-// only beyond the bound B = 6 delta L^2 + 12 delta^2 L + 16 u L^3 (vertex
-// perturbation + FP32 rounding, L the diameter of the six vertices), so a
-// "true" here holds for the exact FP64 triangles as well, and the canonical
-// FP64 test then reports the same contact.  Pairs it cannot certify go to the
-// FP64 re-test.
-__device__ __forceinline__ bool tri_certain_hit32(const float3* P, const float3* Q, float delta)
+// errors of up to `delta` per vertex: an edge of one triangle crosses the
+// other's interior — its endpoints lie on opposite sides of the other
+// triangle's plane and the three edge-edge orientations agree in sign — with
+// every sign certain (orient_sign32).  A "true" therefore holds for the exact
+// FP64 triangles too, and the canonical FP64 test reports the same contact.
+// Pairs it cannot certify go to the FP64 re-test.  Called for band pairs
+// only, so it is kept out of line.
+static __device__ __noinline__ bool tri_certain_hit32(float3 P0, float3 P1, float3 P2, float3 Q0, float3 Q1,
+                                                      float3 Q2, float delta)
 {
-  float3 lo = P[0], hi = P[0];
-#pragma unroll
-  for (int k = 1; k < 6; ++k) {
-    float3 v = k < 3 ? P[k] : Q[k - 3];
-    lo = make_float3(fminf(lo.x, v.x), fminf(lo.y, v.y), fminf(lo.z, v.z));
-    hi = make_float3(fmaxf(hi.x, v.x), fmaxf(hi.y, v.y), fmaxf(hi.z, v.z));
-  }
-  float3 dg = sub3(hi, lo);
-  float L = sqrtf(dot3(dg, dg)) * 1.0001f;
-  float B = 6.f * delta * L * L + 12.f * delta * delta * L + 16.f * 5.9604645e-08f * L * L * L;
-  // plane sides
-  int sq[3], sp[3];
-#pragma unroll
+  int sq = 0, sp = 0;  // 2 bits per vertex: 1 = +, 2 = -, 0 = unsure
+#pragma unroll 1
   for (int k = 0; k < 3; ++k) {
-    sq[k] = rsign(orient32(Q[0], Q[1], Q[2], P[k]), B);
-    sp[k] = rsign(orient32(P[0], P[1], P[2], Q[k]), B);
+    int a = orient_sign32(Q0, Q1, Q2, sel3(k, P0, P1, P2), delta);
+    int b = orient_sign32(P0, P1, P2, sel3(k, Q0, Q1, Q2), delta);
+    sq |= (a > 0 ? 1 : (a < 0 ? 2 : 0)) << (2 * k);
+    sp |= (b > 0 ? 1 : (b < 0 ? 2 : 0)) << (2 * k);
   }
-  int E[3][3];
-#pragma unroll
-  for (int i = 0; i < 3; ++i)
-#pragma unroll
-    for (int j = 0; j < 3; ++j)
-      E[i][j] = rsign(orient32(P[i], P[(i + 1) % 3], Q[j], Q[(j + 1) % 3]), B);
-#pragma unroll
+#pragma unroll 1
   for (int i = 0; i < 3; ++i) {
+    int i1 = i == 2 ? 0 : i + 1;
+    int a0 = (sq >> (2 * i)) & 3, a1 = (sq >> (2 * i1)) & 3;
+    int b0 = (sp >> (2 * i)) & 3, b1 = (sp >> (2 * i1)) & 3;
     // edge i of P through the interior of Q
-    if (sq[i] * sq[(i + 1) % 3] == -1 && E[i][0] != 0 && E[i][0] == E[i][1] && E[i][1] == E[i][2])
-      return true;
+    if (a0 && a1 && a0 != a1) {
+      float3 pa = sel3(i, P0, P1, P2), pb = sel3(i1, P0, P1, P2);
+      int e0 = orient_sign32(pa, pb, Q0, Q1, delta);
+      if (e0 != 0 && orient_sign32(pa, pb, Q1, Q2, delta) == e0 && orient_sign32(pa, pb, Q2, Q0, delta) == e0)
+        return true;
+    }
     // edge i of Q through the interior of P
-    if (sp[i] * sp[(i + 1) % 3] == -1 && E[0][i] != 0 && E[0][i] == E[1][i] && E[1][i] == E[2][i])
-      return true;
+    if (b0 && b1 && b0 != b1) {
+      float3 qa = sel3(i, Q0, Q1, Q2), qb = sel3(i1, Q0, Q1, Q2);
+      int e0 = orient_sign32(P0, P1, qa, qb, delta);
+      if (e0 != 0 && orient_sign32(P1, P2, qa, qb, delta) == e0 && orient_sign32(P2, P0, qa, qb, delta) == e0)
+        return true;
+    }
   }
   return false;
 }
@@ -270,8 +292,8 @@ __device__ __forceinline__ void chain64(const KRobotDev& R, const double* q64, i
 // transforms are formed in parallel (lane i, link i), then composed by lane 0
 // in link order exactly as the oracle does (T[i] = T[parent] * L_i), so the
 // result is bit-identical to the sequential chain.
-__device__ __forceinline__ void warp_fk64(const KRobotDev& R, const double* q64, double (*T64)[12],
-                                          int lane)
+static __device__ __noinline__ void warp_fk64(const KRobotDev& R, const double* q64, double (*T64)[12],
+                                              int lane)
 {
   int nl = R.nlinks;
   if (lane < nl) kx_joint_local(R.T0P64[lane], R.axis64[lane], R.jtype[lane], q64[lane], T64[lane]);
@@ -292,30 +314,27 @@ __device__ __forceinline__ void warp_fk64(const KRobotDev& R, const double* q64,
 // triangle tB of link tgt (tgt < 32) or environment triangle tB, with the
 // link transforms T64 of the configuration.  Returns 1 if the canonical
 // predicate reports collision.
-static __device__ __noinline__ int band_retest(const KWorldDev& W, const KRobotDev& R,
+static __device__ __noinline__ int band_retest(const KWorldDev* __restrict__ W, const KRobotDev& R,
                                                const double (*T64)[12], int la, int tA, int tgt, int tB)
 {
   double P[9], Q[9];
-  const double* pa = W.ltri64 + 9 * (size_t)tA;
+  const double* pa = W->ltri64 + 9 * (size_t)tA;
   for (int v = 0; v < 3; ++v) kx_xform_point(T64[la], pa + 3 * v, P + 3 * v);
   double m = R.link_margin64[la];
   if (tgt < 32) {
-    const double* pb = W.ltri64 + 9 * (size_t)tB;
+    const double* pb = W->ltri64 + 9 * (size_t)tB;
     for (int v = 0; v < 3; ++v) kx_xform_point(T64[tgt], pb + 3 * v, Q + 3 * v);
     m = kx_add(m, R.link_margin64[tgt]);
   } else {
-    const double* pb = W.etri64 + 9 * (size_t)tB;
+    const double* pb = W->etri64 + 9 * (size_t)tB;
     for (int i = 0; i < 9; ++i) Q[i] = pb[i];
-    m = kx_add(m, W.obj_margin64[W.etri_obj[tB]]);
+    m = kx_add(m, W->obj_margin64[W->etri_obj[tB]]);
   }
   if (m == 0.0) return kx_tri_tri_overlap(P, Q);
   double cp[3], cq[3];
   return kx_tri_tri_dist2(P, Q, cp, cq) <= kx_mul(m, m);
 }
 
-__device__ __forceinline__ void set_status(const KWorldDev& W, int code)
-{
-  atomicCAS(W.status, 0, code);
-}
+__device__ __forceinline__ void set_status(int* status, int code) { atomicCAS(status, 0, code); }
 
 }  // namespace kgpu

@@ -174,7 +174,8 @@ struct kgpu_world_s {
   int* d_status = nullptr;
   unsigned long long* d_stats = nullptr;
   std::vector<int> robot_node_base, robot_tri_base;
-  kgpu::KWorldDev dev;
+  kgpu::KWorldDev dev;                // host copy of the descriptor
+  kgpu::KWorldDev* d_dev = nullptr;   // device copy read by the engine kernels
   kgpu::Scratch scratch;
   // options
   double eps_band = 1e-4;
@@ -197,16 +198,17 @@ struct kgpu_edge_plan_s {
 };
 
 namespace kgpu {
-// launchers implemented in the .cu files (return a CUDA error code)
-cudaError_t launch_fk(const KWorldDev& W, int robot, const float* q, int B, float* T,
-                      cudaStream_t s);
-cudaError_t launch_check_configs(const KWorldDev& W, const Scratch& S, int robot,
+// launchers implemented in the .cu files (return a CUDA error code).  The
+// engine kernels read the world descriptor from device memory (Wd); the
+// plain and distance kernels take it by value (W).
+cudaError_t launch_fk(const KWorldDev* Wd, int robot, const float* q, int B, float* T, cudaStream_t s);
+cudaError_t launch_check_configs(const KWorldDev* Wd, const Scratch& S, int robot,
                                  const int* robot_ids, const float* q, int q_stride, int B,
                                  uint8_t* env_hit, uint8_t* self_hit, uint8_t* feasible,
                                  int blocks, int warps_per_block, cudaStream_t s);
-cudaError_t launch_check_edges(const KWorldDev& W, const Scratch& S, int robot, const float* qa,
-                               const float* qb, const int* nsteps, int E, int* first_hit,
-                               int blocks, int warps_per_block, cudaStream_t s);
+cudaError_t launch_check_edges(const KWorldDev* Wd, int* status, const Scratch& S, int robot,
+                               const float* qa, const float* qb, const int* nsteps, int E,
+                               int* first_hit, int blocks, int warps_per_block, cudaStream_t s);
 cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q, int B,
                                    uint8_t* env_hit, uint8_t* self_hit, cudaStream_t s);
 cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,

@@ -141,12 +141,12 @@ __global__ void k_plain_configs(KWorldDev W, int robot, const float* q, int B, u
   double qd[kMaxLinks];
   for (int i = 0; i < R.nlinks; ++i) {
     qd[i] = (double)q[(size_t)b * R.nlinks + i];
-    if (!(fabs(qd[i]) < 1.0e6)) { set_status(W, KGPU_ERR_NOT_FINITE); return; }
+    if (!(fabs(qd[i]) < 1.0e6)) { set_status(W.status, KGPU_ERR_NOT_FINITE); return; }
   }
   double T[kMaxLinks][12];
   fk64_all(R, qd, T);
   int r = plain_config(W, R, T, env_hit != nullptr, self_hit != nullptr, false);
-  if (r & 4) { set_status(W, KGPU_ERR_OVERFLOW); return; }
+  if (r & 4) { set_status(W.status, KGPU_ERR_OVERFLOW); return; }
   if (env_hit) env_hit[b] = (r & 1) ? 1 : 0;
   if (self_hit) self_hit[b] = (r & 2) ? 1 : 0;
 }
@@ -159,7 +159,7 @@ __global__ void k_plain_edges(KWorldDev W, int robot, const float* qa, const flo
   const KRobotDev& R = W.robots[robot];
   int nl = R.nlinks;
   int n = nsteps[e];
-  if (n < 1 || n > kMaxSteps) { set_status(W, KGPU_ERR_INVALID); first_hit[e] = -1; return; }
+  if (n < 1 || n > kMaxSteps) { set_status(W.status, KGPU_ERR_INVALID); first_hit[e] = -1; return; }
   int hit = -1;
   double qd[kMaxLinks];
   double T[kMaxLinks][12];
@@ -167,13 +167,13 @@ __global__ void k_plain_edges(KWorldDev W, int robot, const float* qa, const flo
     bool ok = true;
     for (int i = 0; i < nl; ++i) {
       qd[i] = kx_interp((double)qa[(size_t)e * nl + i], (double)qb[(size_t)e * nl + i], k, n);
-      if (!(fabs(qd[i]) < 1.0e6)) { set_status(W, KGPU_ERR_NOT_FINITE); first_hit[e] = -1; return; }
+      if (!(fabs(qd[i]) < 1.0e6)) { set_status(W.status, KGPU_ERR_NOT_FINITE); first_hit[e] = -1; return; }
       if (qd[i] < R.qmin64[i] || qd[i] > R.qmax64[i]) ok = false;
     }
     if (!ok) { hit = k; break; }
     fk64_all(R, qd, T);
     int r = plain_config(W, R, T, true, true, true);
-    if (r & 4) { set_status(W, KGPU_ERR_OVERFLOW); first_hit[e] = -1; return; }
+    if (r & 4) { set_status(W.status, KGPU_ERR_OVERFLOW); first_hit[e] = -1; return; }
     if (r) hit = k;
   }
   first_hit[e] = hit;
