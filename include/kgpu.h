@@ -147,8 +147,10 @@ kgpu_status kgpu_world_set_link_env_mask(kgpu_world world, int32_t robot, int32_
 kgpu_status kgpu_world_enable_self_pair(kgpu_world world, int32_t robot, int32_t i, int32_t j,
                                         int32_t enabled);
 
-/* Named tuning options: "eps_band" (m), "warps_per_block", "blocks_per_sm",
- * "dist_band" (m).  Unknown names are KGPU_ERR_INVALID. */
+/* Named options: "eps_extra" (m, additional inflation of every FP32 test on
+ * top of the computed error bounds, default 0), "blocks_per_sm" (2, 3 or 4
+ * resident engine blocks per SM), read-only "eps_env", "warps_per_block",
+ * "num_sms".  Unknown names are KGPU_ERR_INVALID. */
 kgpu_status kgpu_world_set_option(kgpu_world world, const char* name, double value);
 kgpu_status kgpu_world_get_option(kgpu_world world, const char* name, double* value);
 
@@ -162,9 +164,12 @@ kgpu_status kgpu_world_reset_stats(kgpu_world world);
 
 /* Forward kinematics.  Replaces RobotModel::setConfig -> UpdateFrames
  * (Python/klampt/src/robotsim.cpp:5311-5321).  q: [B*num_links] float,
- * T_out: [B*num_links*12] float world transforms. */
+ * T_out: [B*num_links*12] float world transforms, err_out: [B*num_links]
+ * (may be NULL) a rigorous bound, per link, on the distance between any
+ * vertex of the link placed with T_out and the same vertex placed with the
+ * exact (FP64) transform. */
 kgpu_status kgpu_fk(kgpu_world world, int32_t robot, const float* q, int32_t B, float* T_out,
-                    kgpu_stream stream);
+                    float* err_out, kgpu_stream stream);
 
 /* Environment and self collision verdicts of B configurations, FP32 BVH
  * traversal with the FP64 band re-test.  Replaces, per configuration,

@@ -74,7 +74,7 @@ _SIGS = {
     "kgpu_world_sync": [_c_p, _c_p],
     "kgpu_world_get_stats": [_c_p, _c_p],
     "kgpu_world_reset_stats": [_c_p],
-    "kgpu_fk": [_c_p, _i32, _c_p, _i32, _c_p, _c_p],
+    "kgpu_fk": [_c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
     "kgpu_check_configs": [_c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
     "kgpu_check_configs_multi": [_c_p, _c_p, _c_p, _i32, _i32, _c_p, _c_p, _c_p],
     "kgpu_is_feasible": [_c_p, _i32, _c_p, _i32, _c_p, _c_p],

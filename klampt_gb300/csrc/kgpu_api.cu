@@ -22,6 +22,7 @@ using namespace kgpu;
 namespace kgpu {
 cudaError_t engine_init();
 size_t engine_smem_per_warp();
+int engine_warps_per_block();
 }
 
 namespace {
@@ -152,6 +153,7 @@ kgpu_status refresh_tables(kgpu_world w)
       depth_max = dep > depth_max ? dep : depth_max;
       d.env_mask[i] = w->env_mask[r][i];
       d.link_margin[i] = round_up_f(R->margins[i]);
+      d.link_r[i] = round_up_f(R->link_r[i] * (1.0 + 1e-6));
       d.link_margin64[i] = R->margins[i];
       d.qmin[i] = (float)R->qmin[i];
       d.qmax[i] = (float)R->qmax[i];
@@ -278,6 +280,7 @@ kgpu_status kgpu_robot_create(const kgpu_robot_desc* d, kgpu_robot* out)
   R->bvh.resize(L);
   R->tri64.resize(L);
   R->link_tri_count.assign(L, 0);
+  R->link_r.assign(L, 0.0);
   double reach_link = 0.0;
   for (int l = 0; l < L; ++l) {
     int v0 = d->vert_offset[l], v1 = d->vert_offset[l + 1];
@@ -304,10 +307,13 @@ kgpu_status kgpu_robot_create(const kgpu_robot_desc* d, kgpu_robot* out)
           tri[9 * (size_t)t + 3 * v + i] = x;
         }
       }
+    double rl = 0.0;
     for (size_t k = 0; k < tri.size(); k += 3) {
       double r = std::sqrt(tri[k] * tri[k] + tri[k + 1] * tri[k + 1] + tri[k + 2] * tri[k + 2]);
-      reach_link = std::max(reach_link, r);
+      rl = std::max(rl, r);
     }
+    reach_link = std::max(reach_link, rl);
+    R->link_r[l] = rl;
     std::vector<int> ids(nt);
     for (int t = 0; t < nt; ++t) ids[t] = t;
     build_bvh(tri, ids, nullptr, R->bvh[l]);
@@ -524,7 +530,7 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   if (e == cudaSuccess) e = cudaMemset(w->d_stats, 0, 8 * sizeof(unsigned long long));
   // scratch: per-warp spill stacks, queue heads, edge ordering tables
   Scratch& S = w->scratch;
-  S.max_warps = w->num_sms * 4 * 16;  // up to 4 blocks/SM of 16 warps
+  S.max_warps = w->num_sms * 4 * engine_warps_per_block();  // up to 4 blocks per SM
   S.spill_per_warp = 8192;
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.spill, (size_t)S.max_warps * S.spill_per_warp * sizeof(uint2));
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.counters, 64 * sizeof(unsigned int));
@@ -537,17 +543,11 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
     delete w;
     return cuda_fail(e, "world allocation");
   }
-  // eps_band: bound on |FP32 - FP64| world coordinates (chain depth x
-  // coordinate magnitude x float epsilon, with a large safety factor)
-  double mag = std::max(reach, env ? env->extent : 0.0) + 1.0;
-  int depth = 1;
-  for (int r = 0; r < n; ++r)
-    for (int l = 0; l < robots[r]->nlinks; ++l) {
-      int dep = 0;
-      for (int j = l; j >= 0; j = robots[r]->parents[j]) ++dep;
-      depth = std::max(depth, dep);
-    }
-  w->eps_band = std::max(1e-5, 64.0 * 5.9604644775390625e-08 * (depth + 4) * mag);
+  // environment coordinates are FP64 rounded to FP32 once: a vertex moves by
+  // at most u/2 * |x|_2 <= u * extent (the per-link bounds come from the
+  // kernels' running error analysis)
+  w->eps_env = env ? 5.9604644775390625e-08 * 2.0 * (env->extent + 1e-3) : 0.0;
+  w->eps_extra = 0.0;
   KWorldDev& D = w->dev;
   memset(&D, 0, sizeof D);
   D.lnodes = w->d_lnodes;
@@ -574,7 +574,8 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   } else {
     for (int g = 0; g < kMaxGroups; ++g) D.group_root[g] = -1;
   }
-  D.eps_band = (float)w->eps_band;
+  D.eps_env = round_up_f(w->eps_env);
+  D.eps_extra = 0.f;
   D.status = w->d_status;
   D.stats = w->d_stats;
   w->tables_dirty = true;
@@ -620,23 +621,19 @@ kgpu_status kgpu_world_enable_self_pair(kgpu_world w, int32_t robot, int32_t i, 
 kgpu_status kgpu_world_set_option(kgpu_world w, const char* name, double v)
 {
   if (!w || !name) return fail(KGPU_ERR_INVALID, "null argument");
-  if (!strcmp(name, "eps_band")) {
-    if (!(v > 0 && v < 1)) return fail(KGPU_ERR_INVALID, "eps_band must be in (0,1)");
-    w->eps_band = v;
-    w->dev.eps_band = (float)v;
+  if (!strcmp(name, "eps_extra")) {
+    if (!(v >= 0 && v < 1)) return fail(KGPU_ERR_INVALID, "eps_extra must be in [0,1)");
+    w->eps_extra = v;
+    w->dev.eps_extra = round_up_f(v);
     w->tables_dirty = true;
-  } else if (!strcmp(name, "warps_per_block")) {
-    int k = (int)v;
-    if (k != 4 && k != 8 && k != 16) return fail(KGPU_ERR_INVALID, "warps_per_block must be 4, 8 or 16");
-    w->warps_per_block = k;
   } else if (!strcmp(name, "blocks_per_sm")) {
     int k = (int)v;
-    if (k < 1 || k * w->warps_per_block > 64 || k > 4) return fail(KGPU_ERR_INVALID, "blocks_per_sm out of range");
+    if (k < 2 || k > 4) return fail(KGPU_ERR_INVALID, "blocks_per_sm must be 2, 3 or 4");
     w->blocks_per_sm = k;
   } else {
     return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
   }
-  if (w->num_sms * w->blocks_per_sm * w->warps_per_block > w->scratch.max_warps)
+  if (w->num_sms * w->blocks_per_sm * engine_warps_per_block() > w->scratch.max_warps)
     return fail(KGPU_ERR_INVALID, "launch shape exceeds the scratch sized at creation");
   return KGPU_OK;
 }
@@ -644,8 +641,9 @@ kgpu_status kgpu_world_set_option(kgpu_world w, const char* name, double v)
 kgpu_status kgpu_world_get_option(kgpu_world w, const char* name, double* v)
 {
   if (!w || !name || !v) return fail(KGPU_ERR_INVALID, "null argument");
-  if (!strcmp(name, "eps_band")) *v = w->eps_band;
-  else if (!strcmp(name, "warps_per_block")) *v = w->warps_per_block;
+  if (!strcmp(name, "eps_extra")) *v = w->eps_extra;
+  else if (!strcmp(name, "eps_env")) *v = w->eps_env;
+  else if (!strcmp(name, "warps_per_block")) *v = engine_warps_per_block();
   else if (!strcmp(name, "blocks_per_sm")) *v = w->blocks_per_sm;
   else if (!strcmp(name, "num_sms")) *v = w->num_sms;
   else return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
@@ -692,12 +690,13 @@ kgpu_status kgpu_world_reset_stats(kgpu_world w)
   return KGPU_OK;
 }
 
-kgpu_status kgpu_fk(kgpu_world w, int32_t robot, const float* q, int32_t B, float* T, kgpu_stream s)
+kgpu_status kgpu_fk(kgpu_world w, int32_t robot, const float* q, int32_t B, float* T, float* err,
+                    kgpu_stream s)
 {
   kgpu_status st = check_world(w, robot);
   if (st) return st;
   if (B < 0 || (B > 0 && (!q || !T))) return fail(KGPU_ERR_INVALID, "bad buffers");
-  return launch_status(launch_fk(w->d_dev, robot, q, B, T, (cudaStream_t)s), "kgpu_fk");
+  return launch_status(launch_fk(w->d_dev, robot, q, B, T, err, (cudaStream_t)s), "kgpu_fk");
 }
 
 kgpu_status kgpu_check_configs(kgpu_world w, int32_t robot, const float* q, int32_t B,
@@ -708,7 +707,7 @@ kgpu_status kgpu_check_configs(kgpu_world w, int32_t robot, const float* q, int3
   if (B < 0 || (B > 0 && !q)) return fail(KGPU_ERR_INVALID, "bad buffers");
   if (!env_hit && !self_hit) return KGPU_OK;
   return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
-                                            env_hit, self_hit, nullptr, grid_blocks(w), w->warps_per_block,
+                                            env_hit, self_hit, nullptr, grid_blocks(w), w->blocks_per_sm,
                                             (cudaStream_t)s),
                        "kgpu_check_configs");
 }
@@ -726,7 +725,7 @@ kgpu_status kgpu_check_configs_multi(kgpu_world w, const int32_t* robot_ids, con
     return fail(KGPU_ERR_INVALID, "bad buffers or q_stride %d < max links %d", q_stride, maxl);
   if (!env_hit && !self_hit) return KGPU_OK;
   return launch_status(launch_check_configs(w->d_dev, w->scratch, -1, robot_ids, q, q_stride, B, env_hit, self_hit,
-                                            nullptr, grid_blocks(w), w->warps_per_block, (cudaStream_t)s),
+                                            nullptr, grid_blocks(w), w->blocks_per_sm,(cudaStream_t)s),
                        "kgpu_check_configs_multi");
 }
 
@@ -737,7 +736,7 @@ kgpu_status kgpu_is_feasible(kgpu_world w, int32_t robot, const float* q, int32_
   if (st) return st;
   if (B < 0 || (B > 0 && (!q || !feasible))) return fail(KGPU_ERR_INVALID, "bad buffers");
   return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
-                                            nullptr, nullptr, feasible, grid_blocks(w), w->warps_per_block,
+                                            nullptr, nullptr, feasible, grid_blocks(w), w->blocks_per_sm,
                                             (cudaStream_t)s),
                        "kgpu_is_feasible");
 }
@@ -750,7 +749,7 @@ kgpu_status kgpu_check_edges(kgpu_world w, int32_t robot, const float* qa, const
   if (E < 0 || (E > 0 && (!qa || !qb || !nsteps || !first_hit))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if ((st = ensure_edge_scratch(w, E))) return st;
   return launch_status(launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
-                                          w->warps_per_block, (cudaStream_t)s),
+                                          w->blocks_per_sm,(cudaStream_t)s),
                        "kgpu_check_edges");
 }
 
@@ -782,7 +781,7 @@ kgpu_status kgpu_distance(kgpu_world w, int32_t robot, const float* q, int32_t B
   if (B < 0 || (B > 0 && (!q || !d || !pair || !cp))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if (!(cutoff > 0)) return fail(KGPU_ERR_INVALID, "cutoff must be positive");
   return launch_status(launch_distance(w->dev, w->scratch, robot, q, B, cutoff, d, pair, cp, grad, grid_blocks(w),
-                                       w->warps_per_block, (cudaStream_t)s),
+                                       w->blocks_per_sm,(cudaStream_t)s),
                        "kgpu_distance");
 }
 
@@ -794,7 +793,7 @@ kgpu_status kgpu_softmin_grad(kgpu_world w, int32_t robot, const float* q, int32
   if (T < 0 || Wn < 1 || (T > 0 && (!q || !L))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if (!(tau > 0)) return fail(KGPU_ERR_INVALID, "tau must be positive");
   return launch_status(launch_softmin(w->dev, w->scratch, robot, q, T, Wn, tau, L, dLdq, grid_blocks(w),
-                                      w->warps_per_block, (cudaStream_t)s),
+                                      w->blocks_per_sm,(cudaStream_t)s),
                        "kgpu_softmin_grad");
 }
 
@@ -886,7 +885,7 @@ kgpu_status kgpu_edge_plan_create(kgpu_world w, int32_t robot, const float* qa, 
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
-                                        w->warps_per_block, cs);
+                                        w->blocks_per_sm,cs);
     e = cudaStreamEndCapture(cs, &p->graph);
     if (e == cudaSuccess && le != cudaSuccess) e = le;
   }

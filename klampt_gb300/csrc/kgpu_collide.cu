@@ -39,12 +39,14 @@ namespace kgpu {
 
 namespace {
 
-constexpr int kStackCap = 512;
+constexpr int kStackCap = 384;
 constexpr int kJobCap = 96;
 constexpr int kGrab = 2;  // items taken from the queue per atomic
+constexpr int kWarps = 8; // warps per block
 
 enum Mode { MODE_CONFIGS = 0, MODE_FEASIBLE = 1, MODE_EDGES = 2 };
 
+// per-warp shared memory (~6.4 KB, so that up to 32 warps fit on an SM)
 struct __align__(16) WarpSmem {
   uint2 stack[kStackCap];
   uint32_t jobA[kJobCap];
@@ -52,9 +54,33 @@ struct __align__(16) WarpSmem {
   uint32_t jobM[kJobCap];
   uint32_t jobOff[kJobCap + 1];
   float T[kMaxLinks][12];
-  double q64[kMaxLinks];
-  double T64[kMaxLinks][12];  // FP64 link transforms, computed on first band pair
+  float delta[kMaxLinks];     // per-link bound on |FP32 - exact| world coordinates
+  double q64[kMaxLinks];      // canonical FP64 joint values (filled with T64)
+  const float* item_qa;       // the item's joint values: configuration, or edge
+  const float* item_qb;       //   endpoints qa/qb (item_qb null for configurations)
+  int item_k, item_n;         // edge step k of n
 };
+
+// canonical FP64 joint values of the current item (lane < nl), as the oracle
+// forms them: float input widened, or the FP64 edge interpolation
+__device__ __forceinline__ double item_q64(const WarpSmem& S, int lane)
+{
+  if (S.item_qb == nullptr) return (double)S.item_qa[lane];
+  return kx_interp((double)S.item_qa[lane], (double)S.item_qb[lane], S.item_k, S.item_n);
+}
+
+__device__ __noinline__ void ensure_fk64(WarpSmem& S, const KRobotDev& R, double (*T64)[12], int lane, int& fk64)
+{
+  if (fk64) return;
+  if (lane < R.nlinks) S.q64[lane] = item_q64(S, lane);
+  __syncwarp();
+  warp_fk64(R, S.q64, T64, lane);
+  fk64 = 1;
+}
+
+// per-warp global scratch: FP64 link transforms (filled on the first band
+// pair of a configuration) followed by the stack spill area
+constexpr int kT64Doubles = kMaxLinks * 12;
 
 struct EngineArgs {
   int mode;
@@ -99,7 +125,7 @@ __device__ __forceinline__ uint2 make_entry(int nodeA, int la, int tgt, int node
 // beyond the band: contact), otherwise the FP64 re-test on transforms
 // computed once per configuration (fk64 tracks whether S.T64 is valid).
 __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
-                                      int njobs, int lane, int& fk64, Cnt& cnt)
+                                      int njobs, int lane, double (*T64)[12], int& fk64, Cnt& cnt)
 {
   // exclusive prefix over job sizes
   uint32_t carry = 0;
@@ -124,7 +150,6 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
   if (lane == 0) S.jobOff[njobs] = carry;
   __syncwarp();
   const uint32_t total = carry;
-  const float eps = W->eps_band;
   const float4* __restrict__ ltri = W->ltri32;
   const float4* __restrict__ etri = W->etri32;
 #pragma unroll 1
@@ -159,9 +184,11 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
         float4 y = __ldg(qsrc + 3 * (size_t)tB + v);
         Q[v] = self ? xform32(TB, make_float3(y.x, y.y, y.z)) : make_float3(y.x, y.y, y.z);
       }
-      float margin = R.link_margin[la] + (self ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
-      band = !tri_separated32(P, Q, eps, margin);
-      if (band && margin == 0.f) certain = tri_certain_hit32(P[0], P[1], P[2], Q[0], Q[1], Q[2], eps);
+      const float margin = R.link_margin[la] + (self ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
+      const float dA = S.delta[la] + W->eps_extra;
+      const float dB = (self ? S.delta[tgt] : W->eps_env) + W->eps_extra;
+      band = !tri_separated32(P, Q, dA + dB, margin);
+      if (band && margin == 0.f) certain = tri_certain_hit32(P[0], P[1], P[2], Q[0], Q[1], Q[2], fmaxf(dA, dB));
     }
     cnt.tri_pairs += (p < total) ? 1 : 0;
     if (__any_sync(0xffffffffu, certain)) {
@@ -170,14 +197,11 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
     }
     const bool need64 = band && !certain;
     if (__any_sync(0xffffffffu, need64)) {
-      if (!fk64) {
-        warp_fk64(R, S.q64, S.T64, lane);
-        fk64 = 1;
-      }
+      ensure_fk64(S, R, T64, lane, fk64);
       int hit = 0;
       if (need64) {
         cnt.band++;
-        hit = band_retest(W, R, S.T64, la, tA, tgt, tB);
+        hit = band_retest(W, R, T64, la, tA, tgt, tB);
       }
       if (__any_sync(0xffffffffu, hit)) {
         cnt.hit64++;
@@ -190,8 +214,18 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
 
 // Node-pair test for one stack entry; returns 0 (culled), 1 (children in c0,
 // c1) or 2 (leaf job in jA, jB, jM).
+// box-test tolerance of a (link la, target tgt) pair: error bounds of both
+// sides, the optional extra inflation and the summed margins
+__device__ __forceinline__ float pair_tol(const WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                          int la, int tgt)
+{
+  const bool self = tgt < 32;
+  return S.delta[la] + (self ? S.delta[tgt] : W->eps_env) + 2.f * W->eps_extra + R.link_margin[la] +
+         (self ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
+}
+
 __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __restrict__ W,
-                                          const KRobotDev& R, uint2 e, float eps, uint2& c0, uint2& c1,
+                                          const KRobotDev& R, uint2 e, uint2& c0, uint2& c1,
                                           uint32_t& jA, uint32_t& jB, uint32_t& jM)
 {
   const int nodeA = e.y & 0xfffff;
@@ -209,8 +243,7 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
     Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z);
     Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z);
   }
-  const float m = R.link_margin[la] + (self ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
-  if (!boxes_overlap(A, Bx, eps + m)) return 0;
+  if (!boxes_overlap(A, Bx, pair_tol(S, W, R, la, tgt))) return 0;
   const int cntA = f2i(na.b.w), cntB = f2i(nb.b.w);
   const int ia = f2i(na.a.w), ib = f2i(nb.a.w);
   if (cntA > 0 && cntB > 0) {
@@ -233,10 +266,9 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
 // Traverses queries [qbase, qbase+qcount) of robot R for the configuration
 // whose FP32 link transforms are in S.T.  Warp-uniform control flow.
 __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
-                                     int qbase, int qcount, int lane, uint2* spill, int spill_cap, int& fk64,
-                                     Cnt& cnt)
+                                     int qbase, int qcount, int lane, uint2* spill, int spill_cap,
+                                     double (*T64)[12], int& fk64, Cnt& cnt)
 {
-  const float eps = W->eps_band;
   const unsigned lt = lanemask_lt();
   int top = 0, njobs = 0, spill_top = 0;
 
@@ -271,8 +303,7 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
         Box32 Bx;
         if (tgt < 32) Bx = xform_box(S.T[tgt], nb.a, nb.b);
         else { Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z); Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z); }
-        const float m = R.link_margin[a] + (tgt < 32 ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
-        push = boxes_overlap(A, Bx, eps + m);
+        push = boxes_overlap(A, Bx, pair_tol(S, W, R, a, tgt));
         cnt.node_pairs++;
       }
     }
@@ -296,7 +327,7 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
       }
     }
     if (njobs > kJobCap - 32 || (top == 0 && njobs > 0)) {
-      const bool hit = run_jobs(S, W, R, njobs, lane, fk64, cnt);
+      const bool hit = run_jobs(S, W, R, njobs, lane, T64, fk64, cnt);
       __syncwarp();
       njobs = 0;
       if (hit) return TR_HIT;
@@ -322,7 +353,7 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
     int outcome = 0;  // 1: two children, 2: leaf job
     uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
     uint32_t jA = 0, jB = 0, jM = 0;
-    if (have) outcome = test_entry(S, W, R, e, eps, c0, c1, jA, jB, jM);
+    if (have) outcome = test_entry(S, W, R, e, c0, c1, jA, jB, jM);
     cnt.node_pairs += have ? 1 : 0;
     const unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
     const unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
@@ -342,16 +373,21 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
   }
 }
 
-template <int WARPS>
-__global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
+// MINB: resident blocks of kWarps warps per SM the register allocation is
+// sized for (2 -> 128 registers/thread, 3 -> 80, 4 -> 64).
+template <int MINB>
+__global__ void __launch_bounds__(kWarps * 32, MINB)
     k_engine(const KWorldDev* __restrict__ W, const EngineArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   WarpSmem* all = reinterpret_cast<WarpSmem*>(smem_raw);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   WarpSmem& S = all[warp];
-  const int gwarp = blockIdx.x * WARPS + warp;
-  uint2* spill = A.spill + (size_t)gwarp * A.spill_per_warp;
+  const int gwarp = blockIdx.x * kWarps + warp;
+  uint2* wscratch = A.spill + (size_t)gwarp * A.spill_per_warp;
+  double(*T64)[12] = reinterpret_cast<double(*)[12]>(wscratch);
+  uint2* spill = wscratch + kT64Doubles;
+  const int spill_cap = A.spill_per_warp - kT64Doubles;
   Cnt cnt;
   unsigned long long items = 0;
   const int total = A.mode == MODE_EDGES ? A.meta[1] : A.B;
@@ -386,35 +422,65 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
       }
       const KRobotDev& R = W->robots[rid];
       const int nl = R.nlinks;
-      double q64 = 0.0;
-      if (lane < nl) {
-        if (A.mode == MODE_EDGES)
-          q64 = kx_interp((double)__ldg(A.qa + (size_t)e * nl + lane),
-                          (double)__ldg(A.qb + (size_t)e * nl + lane), k, n);
-        else
-          q64 = (double)__ldg(A.q + (size_t)b * A.q_stride + lane);
-        S.q64[lane] = q64;
+      // joint values in FP32 with an error bound e_q against the canonical
+      // FP64 values (exact for configurations; FMA interpolation for edges)
+      if (lane == 0) {
+        if (A.mode == MODE_EDGES) {
+          S.item_qa = A.qa + (size_t)e * nl;
+          S.item_qb = A.qb + (size_t)e * nl;
+        } else {
+          S.item_qa = A.q + (size_t)b * A.q_stride;
+          S.item_qb = nullptr;
+        }
+        S.item_k = k;
+        S.item_n = n;
       }
+      float q = 0.f, e_q = 0.f;
+      if (lane < nl) {
+        if (A.mode == MODE_EDGES) {
+          const float a = __ldg(A.qa + (size_t)e * nl + lane), bq = __ldg(A.qb + (size_t)e * nl + lane);
+          const float d = bq - a;
+          q = fmaf((float)k / (float)n, d, a);
+          e_q = kU * (fabsf(d) + fabsf(q) + fabsf(a)) * 1.01f + 1e-30f;
+        } else {
+          q = __ldg(A.q + (size_t)b * A.q_stride + lane);
+        }
+      }
+      __syncwarp();
       items++;
-      const bool viol = lane < nl && (q64 < R.qmin64[lane] || q64 > R.qmax64[lane]);
-      const bool limit_bad = __any_sync(0xffffffffu, viol);
-      const bool nonfinite = __any_sync(0xffffffffu, lane < nl && !(fabs(q64) < 1.0e6));
+      const bool nonfinite = __any_sync(0xffffffffu, lane < nl && !(fabsf(q) < 1.0e6f));
       if (nonfinite) {
         if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
         continue;
       }
-      if (A.mode != MODE_CONFIGS && limit_bad) {
-        if (lane == 0) {
-          if (A.mode == MODE_EDGES) atomicMin(A.first_hit + e, k);
-          else A.feasible[b] = 0;
+      if (A.mode != MODE_CONFIGS) {
+        // joint limits: certain in FP32 away from the bounds, canonical FP64
+        // comparison (RobotCSpace.cpp:610-630) within rounding of them
+        bool unsure = false;
+        if (lane < nl) {
+          const float lo = R.qmin[lane], hi = R.qmax[lane];
+          const float tolq = e_q + 4.f * kU * (fabsf(q) + fmaxf(fabsf(lo), fabsf(hi))) + 1e-30f;
+          unsure = !((q - lo) > tolq && (hi - q) > tolq);
         }
-        continue;
+        bool viol = false;
+        if (unsure) {
+          const double q64 = item_q64(S, lane);
+          viol = q64 < R.qmin64[lane] || q64 > R.qmax64[lane];
+        }
+        if (__any_sync(0xffffffffu, viol)) {
+          if (lane == 0) {
+            if (A.mode == MODE_EDGES) atomicMin(A.first_hit + e, k);
+            else A.feasible[b] = 0;
+          }
+          continue;
+        }
       }
-      float P[12];
-      warp_fk32(R, lane, q64, P);
+      float P[12], delta;
+      warp_fk32(R, lane, q, e_q, P, &delta);
       if (lane < nl) {
 #pragma unroll
         for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
+        S.delta[lane] = delta;
       }
       __syncwarp();
       int env_res = TR_FREE, self_res = TR_FREE;
@@ -422,11 +488,11 @@ __global__ void __launch_bounds__(WARPS * 32, 16 / WARPS)
       const bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
       const bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
       if (want_env && R.nqueries_env > 0)
-        env_res = traverse(S, W, R, R.query_off, R.nqueries_env, lane, spill, A.spill_per_warp, fk64, cnt);
+        env_res = traverse(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, cnt);
       const bool stop = A.mode != MODE_CONFIGS && env_res != TR_FREE;
       if (!stop && want_self && R.nqueries_self > 0)
-        self_res = traverse(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill,
-                            A.spill_per_warp, fk64, cnt);
+        self_res = traverse(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill, spill_cap,
+                            T64, fk64, cnt);
       if (env_res == TR_OVERFLOW || self_res == TR_OVERFLOW) {
         if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
         continue;
@@ -516,65 +582,72 @@ __global__ void k_edges_finalize(int* first_hit, int E)
   if (e < E && first_hit[e] == INT_MAX) first_hit[e] = -1;
 }
 
-__global__ void k_fk(const KWorldDev* __restrict__ W, int robot, const float* q, int B, float* T)
+__global__ void k_fk(const KWorldDev* __restrict__ W, int robot, const float* q, int B, float* T, float* err)
 {
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (warp >= B) return;
   const KRobotDev& R = W->robots[robot];
   int nl = R.nlinks;
-  double qv = lane < nl ? (double)q[(size_t)warp * nl + lane] : 0.0;
-  float P[12];
-  warp_fk32(R, lane, qv, P);
-  if (lane < nl)
+  float qv = lane < nl ? q[(size_t)warp * nl + lane] : 0.f;
+  float P[12], delta;
+  warp_fk32(R, lane, qv, 0.f, P, &delta);
+  if (lane < nl) {
     for (int i = 0; i < 12; ++i) T[((size_t)warp * nl + lane) * 12 + i] = P[i];
+    if (err) err[(size_t)warp * nl + lane] = delta;
+  }
 }
 
-template <int WARPS>
+template <int MINB>
 cudaError_t init_engine()
 {
-  return cudaFuncSetAttribute(k_engine<WARPS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)(sizeof(WarpSmem) * WARPS));
+  return cudaFuncSetAttribute(k_engine<MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(sizeof(WarpSmem) * kWarps));
 }
 
 // the shared-memory attribute is set once per process by engine_init(), so
 // that launches can be captured into CUDA graphs
-template <int WARPS>
+template <int MINB>
 cudaError_t launch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, cudaStream_t s)
 {
-  size_t smem = sizeof(WarpSmem) * WARPS;
-  k_engine<WARPS><<<blocks, WARPS * 32, smem, s>>>(W, A);
+  size_t smem = sizeof(WarpSmem) * kWarps;
+  k_engine<MINB><<<blocks, kWarps * 32, smem, s>>>(W, A);
   return cudaGetLastError();
 }
 
-cudaError_t dispatch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, int warps, cudaStream_t s)
+// `blocks` = SMs x blocks per SM; the blocks-per-SM value selects the
+// register budget of the instantiation
+cudaError_t dispatch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, int per_sm, cudaStream_t s)
 {
-  switch (warps) {
+  switch (per_sm) {
+    case 3: return launch_engine<3>(W, A, blocks, s);
     case 4: return launch_engine<4>(W, A, blocks, s);
-    case 16: return launch_engine<16>(W, A, blocks, s);
-    default: return launch_engine<8>(W, A, blocks, s);
+    default: return launch_engine<2>(W, A, blocks, s);
   }
 }
 
 }  // namespace
 
 size_t engine_smem_per_warp() { return sizeof(WarpSmem); }
+int engine_warps_per_block() { return kWarps; }
+int engine_scratch_doubles() { return kT64Doubles; }
 
 cudaError_t engine_init()
 {
-  cudaError_t e = init_engine<4>();
-  if (e == cudaSuccess) e = init_engine<8>();
-  if (e == cudaSuccess) e = init_engine<16>();
+  cudaError_t e = init_engine<2>();
+  if (e == cudaSuccess) e = init_engine<3>();
+  if (e == cudaSuccess) e = init_engine<4>();
   return e;
 }
 
-cudaError_t launch_fk(const KWorldDev* W, int robot, const float* q, int B, float* T, cudaStream_t s)
+cudaError_t launch_fk(const KWorldDev* W, int robot, const float* q, int B, float* T, float* err,
+                      cudaStream_t s)
 {
   if (B <= 0) return cudaSuccess;
   int threads = 256;
   long long warps = B;
   int blocks = (int)((warps * 32 + threads - 1) / threads);
-  k_fk<<<blocks, threads, 0, s>>>(W, robot, q, B, T);
+  k_fk<<<blocks, threads, 0, s>>>(W, robot, q, B, T, err);
   return cudaGetLastError();
 }
 

@@ -4,11 +4,13 @@
 // conservative triangle/triangle separating-axis filter.  "Conservative"
 // means: when the filter reports separation, the canonical FP64 triangles
 // (include/kgpu_exact.h, evaluated on the FP64 forward kinematics) are
-// separated too.  Every FP32 comparison therefore carries an inflation
-// eps (world option "eps_band", default 1e-4 m) that bounds the difference
-// between FP32 and FP64 world coordinates plus the FP32 rounding of the test
-// itself.  Pairs the filter cannot separate form the "band" and are decided
-// by the FP64 re-test, so verdicts equal the FP64 ones bit for bit.
+// separated too.  Every FP32 comparison therefore carries an inflation that
+// bounds the difference between FP32 and FP64 world coordinates — computed
+// per configuration and per link by a running error analysis of the FP32
+// forward kinematics (warp_fk32) — plus the FP32 rounding of the test
+// itself.  Pairs the filter cannot separate form the "band": an FP32
+// intersection certificate or the FP64 re-test decides them, so verdicts
+// equal the FP64 ones bit for bit.
 #pragma once
 
 #include "../../include/kgpu_exact.h"
@@ -44,13 +46,25 @@ __device__ __forceinline__ float3 xform32(const float* T, float3 v)
                      fmaf(T[6], v.x, fmaf(T[7], v.y, fmaf(T[8], v.z, T[11]))));
 }
 
-// sin and cos of an FP64 angle to FP32 accuracy with little code: the
-// reduction modulo pi/2 runs in FP64 (two FP64 products), the polynomials in
-// FP32 on |r| <= pi/4 (Taylor series to r^9 / r^10, truncation < 3e-9).
-__device__ __forceinline__ void sincos32_of64(double x, float* s, float* c)
+constexpr float kU = 5.9604645e-08f;  // unit roundoff of FP32, 2^-24
+
+// sin and cos in FP32 with a known error bound: Cody–Waite reduction modulo
+// pi/2 with a three-part split (pi/2 = C1 + C2 + C3, C1 and C2 of 12
+// significant bits, so k*C1 and k*C2 are exact for |x| < 4096; larger
+// arguments reduce in FP64), then the Taylor series of sin to r^9 and cos to
+// r^10 on |r| <= pi/4 (truncation < 2e-9).  |error| <= kSinCosErr.
+constexpr float kSinCosErr = 4.0f * kU;
+__device__ __forceinline__ void sincos32(float x, float* s, float* c)
 {
-  double k = rint(x * 0.6366197723675814);
-  float r = (float)((x - k * 1.5707963267948966) - k * 6.123233995736766e-17);
+  float k, r;
+  if (fabsf(x) < 4096.f) {
+    k = rintf(x * 0.63661975f);
+    r = fmaf(-k, -8.705516e-10f, fmaf(-k, -4.4535846e-06f, fmaf(-k, 1.57080078125f, x)));
+  } else {
+    double kd = rint((double)x * 0.6366197723675814);
+    r = (float)(((double)x - kd * 1.5707963267948966) - kd * 6.123233995736766e-17);
+    k = (float)fmod(kd, 4.0);
+  }
   float r2 = r * r;
   float ps = fmaf(fmaf(fmaf(fmaf(2.7557319e-06f, r2, -1.98412698e-04f), r2, 8.33333333e-03f), r2,
                        -1.66666667e-01f), r2 * r, r);
@@ -62,15 +76,40 @@ __device__ __forceinline__ void sincos32_of64(double x, float* s, float* c)
   *c = ((q + 1) & 2) ? -cs : cs;
 }
 
-// local transform T0_Parent * J(q) of link i in FP32
-__device__ __forceinline__ void joint_local32(const KRobotDev& R, int i, double q64, float* L)
+__device__ __forceinline__ float tnorm(const float* T)
+{
+  return sqrtf(T[9] * T[9] + T[10] * T[10] + T[11] * T[11]) * 1.0001f;
+}
+
+// Running error bound of an FP32 rigid transform T~ against the exact
+// transform T of the same configuration computed in FP64:
+//   rho >= ||R~ - R||_2   and   tau >= |t~ - t|_2.
+// Composition C = A * B (FP32 with FMA) propagates as
+//   rho_C = rho_A (1 + rho_B) + rho_B + 6u (1 + rho_A)(1 + rho_B)
+//   tau_C = rho_A |t_B| + tau_B + tau_A + 3u (sqrt3 (1 + rho_A)|t_B| + |t_A|)
+// (first-order terms from the operands, the second from FMA rounding of the
+// 3-term dot products, bounded with Cauchy-Schwarz on rows of norm <= 1+rho).
+__device__ __forceinline__ void compose_err(float rA, float tA, float nA, float rB, float tB, float nB,
+                                            float* r, float* t)
+{
+  *r = (rA * (1.f + rB) + rB + 6.f * kU * (1.f + rA) * (1.f + rB)) * 1.0001f;
+  *t = (rA * nB + tB + tA + 3.f * kU * (1.7320509f * (1.f + rA) * nB + nA)) * 1.0001f;
+}
+
+// local transform T0_Parent * J(q) of link i in FP32 and its error bound.
+// e_q bounds |q_fp32 - q_exact|.  For a revolute joint
+//   ||R_J(q~) - R_J(q)|| <= |dq| ;  sin/cos errors: <= 2 kSinCosErr
+//   (R = cI + s[w]x + (1-c)ww^T);  entry rounding and axis rounding <= 12u.
+// T0_Parent rounded to FP32: rho <= u, tau <= u/2 |t0|.
+__device__ __forceinline__ void joint_local32(const KRobotDev& R, int i, float q, float e_q, float* L,
+                                              float* rho, float* tau)
 {
   const float* T0 = R.T0P[i];
   int jt = R.jtype[i];
-  float q = (float)q64;
+  const float r0 = kU, t0 = 0.5f * kU * tnorm(T0);
   if (jt == KX_JOINT_REVOLUTE) {
     float s, c;
-    sincos32_of64(q64, &s, &c);
+    sincos32(q, &s, &c);
     float wx = R.axis[i][0], wy = R.axis[i][1], wz = R.axis[i][2];
     float v = 1.f - c;
     float J[12];
@@ -79,26 +118,39 @@ __device__ __forceinline__ void joint_local32(const KRobotDev& R, int i, double 
     J[6] = wz * wx * v - wy * s; J[7] = wz * wy * v + wx * s; J[8] = c + wz * wz * v;
     J[9] = 0.f; J[10] = 0.f; J[11] = 0.f;
     compose32(T0, J, L);
+    const float rJ = e_q + 2.f * kSinCosErr + 12.f * kU;
+    compose_err(r0, t0, tnorm(T0), rJ, 0.f, 0.f, rho, tau);
   } else if (jt == KX_JOINT_PRISMATIC) {
     float J[12] = {1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0};
     J[9] = R.axis[i][0] * q; J[10] = R.axis[i][1] * q; J[11] = R.axis[i][2] * q;
     compose32(T0, J, L);
+    const float tJ = (e_q + 2.f * kU * fabsf(q)) * 1.0001f;
+    compose_err(r0, t0, tnorm(T0), 0.f, tJ, tnorm(J), rho, tau);
   } else {
 #pragma unroll
     for (int k = 0; k < 12; ++k) L[k] = T0[k];
+    *rho = r0;
+    *tau = t0;
   }
 }
 
 // Warp-cooperative forward kinematics: lane i < nlinks owns link i.  Local
 // transforms are formed in parallel and chained to the root by pointer
 // jumping (ceil(log2(depth)) rounds of shuffles), which handles serial
-// chains and trees alike.  Result: world transform of link `lane` in P.
-__device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, double q, float* P)
+// chains and trees alike.  Result: world transform of link `lane` in P and
+// delta, a bound on |v_world_fp32 - v_world_exact| for every vertex of the
+// link and for every point of its FP32 node boxes:
+//   delta = rho r + tau + u (12 r + 6 |t|),
+// r the largest vertex norm of the link in its own frame (the u-term covers
+// the FP32 rounding of the vertex and box transforms).
+__device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, float q, float e_q, float* P,
+                                          float* delta)
 {
   int nl = R.nlinks;
   int anc = -1;
+  float rho = 0.f, tau = 0.f;
   if (lane < nl) {
-    joint_local32(R, lane, q, P);
+    joint_local32(R, lane, q, e_q, P, &rho, &tau);
     anc = R.parents[lane];
   } else {
 #pragma unroll
@@ -109,15 +161,23 @@ __device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, double q
     float Pa[12];
 #pragma unroll
     for (int k = 0; k < 12; ++k) Pa[k] = __shfl_sync(0xffffffffu, P[k], src);
-    int anc2 = __shfl_sync(0xffffffffu, anc, src);
+    const int anc2 = __shfl_sync(0xffffffffu, anc, src);
+    const float ra = __shfl_sync(0xffffffffu, rho, src);
+    const float ta = __shfl_sync(0xffffffffu, tau, src);
     if (anc >= 0) {
       float o[12];
       compose32(Pa, P, o);
+      float r2, t2;
+      compose_err(ra, ta, tnorm(Pa), rho, tau, tnorm(P), &r2, &t2);
+      rho = r2;
+      tau = t2;
 #pragma unroll
       for (int k = 0; k < 12; ++k) P[k] = o[k];
       anc = anc2;
     }
   }
+  const float rl = lane < nl ? R.link_r[lane] : 0.f;
+  *delta = (rho * rl + tau + kU * (12.f * rl + 6.f * tnorm(P))) * 1.001f + 1e-9f;
 }
 
 // ---- boxes -------------------------------------------------------------
@@ -173,17 +233,27 @@ __device__ __forceinline__ float3 sel3(int i, float3 a, float3 b, float3 c)
 // Conservative separation of world-frame triangles P and Q (FP32): box
 // pre-test, the two face normals, then the 9 edge-edge and 6 in-plane axes in
 // a rolled loop (small code keeps the hot loop in the instruction cache).
+// eps = delta_P + delta_Q (vertex error bounds of the two triangles); the
+// FP32 rounding of the projections adds 8u x span (span bounds every
+// coordinate relative to P's first vertex).
 __device__ __forceinline__ bool tri_separated32(const float3* P, const float3* Q, float eps,
                                                 float margin)
 {
-  float bt = eps + margin;
-  if (fminf(Q[0].x, fminf(Q[1].x, Q[2].x)) - fmaxf(P[0].x, fmaxf(P[1].x, P[2].x)) > bt ||
-      fminf(P[0].x, fminf(P[1].x, P[2].x)) - fmaxf(Q[0].x, fmaxf(Q[1].x, Q[2].x)) > bt ||
-      fminf(Q[0].y, fminf(Q[1].y, Q[2].y)) - fmaxf(P[0].y, fmaxf(P[1].y, P[2].y)) > bt ||
-      fminf(P[0].y, fminf(P[1].y, P[2].y)) - fmaxf(Q[0].y, fmaxf(Q[1].y, Q[2].y)) > bt ||
-      fminf(Q[0].z, fminf(Q[1].z, Q[2].z)) - fmaxf(P[0].z, fmaxf(P[1].z, P[2].z)) > bt ||
-      fminf(P[0].z, fminf(P[1].z, P[2].z)) - fmaxf(Q[0].z, fmaxf(Q[1].z, Q[2].z)) > bt)
+  const float3 pmn = make_float3(fminf(P[0].x, fminf(P[1].x, P[2].x)), fminf(P[0].y, fminf(P[1].y, P[2].y)),
+                                 fminf(P[0].z, fminf(P[1].z, P[2].z)));
+  const float3 pmx = make_float3(fmaxf(P[0].x, fmaxf(P[1].x, P[2].x)), fmaxf(P[0].y, fmaxf(P[1].y, P[2].y)),
+                                 fmaxf(P[0].z, fmaxf(P[1].z, P[2].z)));
+  const float3 qmn = make_float3(fminf(Q[0].x, fminf(Q[1].x, Q[2].x)), fminf(Q[0].y, fminf(Q[1].y, Q[2].y)),
+                                 fminf(Q[0].z, fminf(Q[1].z, Q[2].z)));
+  const float3 qmx = make_float3(fmaxf(Q[0].x, fmaxf(Q[1].x, Q[2].x)), fmaxf(Q[0].y, fmaxf(Q[1].y, Q[2].y)),
+                                 fmaxf(Q[0].z, fmaxf(Q[1].z, Q[2].z)));
+  const float bt = eps + margin;
+  if (qmn.x - pmx.x > bt || pmn.x - qmx.x > bt || qmn.y - pmx.y > bt || pmn.y - qmx.y > bt ||
+      qmn.z - pmx.z > bt || pmn.z - qmx.z > bt)
     return true;
+  const float span = fmaxf(fmaxf(fmaxf(pmx.x, qmx.x) - fminf(pmn.x, qmn.x), fmaxf(pmx.y, qmx.y) - fminf(pmn.y, qmn.y)),
+                           fmaxf(pmx.z, qmx.z) - fminf(pmn.z, qmn.z));
+  eps += 8.f * kU * span;
   float3 p[3], q[3];
   p[0] = make_float3(0.f, 0.f, 0.f);
   p[1] = sub3(P[1], P[0]);

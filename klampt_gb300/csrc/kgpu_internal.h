@@ -64,6 +64,7 @@ struct KRobotDev {
   int link_depth[kMaxLinks];
   uint32_t env_mask[kMaxLinks];
   float link_margin[kMaxLinks];
+  float link_r[kMaxLinks];   // largest vertex norm of the link mesh in its frame (rounded up)
   float qmin[kMaxLinks], qmax[kMaxLinks];
   float T0P[kMaxLinks][12];
   float axis[kMaxLinks][3];
@@ -96,8 +97,11 @@ struct KWorldDev {
   int group_root[kMaxGroups];
   float group_margin[kMaxGroups];
   int num_objects;
-  // options
-  float eps_band;            // FP32 conservative inflation (m)
+  // tolerances (m): the per-link FP32 error bounds come from warp_fk32; the
+  // environment's FP32 coordinates are off by at most eps_env; eps_extra is
+  // an optional additional inflation (world option, default 0)
+  float eps_env;
+  float eps_extra;
   // diagnostics
   int* status;               // device status word
   unsigned long long* stats; // kgpu_stats counters
@@ -125,6 +129,7 @@ struct kgpu_robot_s {
   std::vector<double> T0P, axes, qmin, qmax, margins;
   std::vector<uint8_t> self_mask;   // [L*L] upper triangle
   std::vector<int> link_tri_count;
+  std::vector<double> link_r;              // largest vertex norm per link (link frame)
   // device arrays of this robot's links (local indices per link)
   std::vector<kgpu::HostBvh> bvh;
   std::vector<std::vector<double>> tri64;  // per link, leaf order, 9 per tri
@@ -177,10 +182,10 @@ struct kgpu_world_s {
   kgpu::KWorldDev dev;                // host copy of the descriptor
   kgpu::KWorldDev* d_dev = nullptr;   // device copy read by the engine kernels
   kgpu::Scratch scratch;
-  // options
-  double eps_band = 1e-4;
-  int warps_per_block = 8;
-  int blocks_per_sm = 2;
+  // tolerances
+  double eps_env = 0.0;
+  double eps_extra = 0.0;
+  int blocks_per_sm = 2;   // resident 8-warp engine blocks per SM (2, 3 or 4)
   int num_sms = 0;
   bool tables_dirty = true;
   // pinned staging for the host-buffer entry points
@@ -201,7 +206,8 @@ namespace kgpu {
 // launchers implemented in the .cu files (return a CUDA error code).  The
 // engine kernels read the world descriptor from device memory (Wd); the
 // plain and distance kernels take it by value (W).
-cudaError_t launch_fk(const KWorldDev* Wd, int robot, const float* q, int B, float* T, cudaStream_t s);
+cudaError_t launch_fk(const KWorldDev* Wd, int robot, const float* q, int B, float* T, float* err,
+                      cudaStream_t s);
 cudaError_t launch_check_configs(const KWorldDev* Wd, const Scratch& S, int robot,
                                  const int* robot_ids, const float* q, int q_stride, int B,
                                  uint8_t* env_hit, uint8_t* self_hit, uint8_t* feasible,

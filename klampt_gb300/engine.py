@@ -164,14 +164,18 @@ class World:
         check(lib().kgpu_world_reset_stats(self.handle))
 
     # ---- queries (device) ----------------------------------------------------
-    def fk(self, q, robot: int = 0, sync: bool = True) -> torch.Tensor:
+    def fk(self, q, robot: int = 0, sync: bool = True, with_error: bool = False):
+        """World transforms [B, L, 12] (R row-major, t); with_error also
+        returns [B, L] bounds on the world-position error of any link vertex
+        against FP64 forward kinematics."""
         L = self.robots[robot].num_links
         qd = _dev(q, torch.float32).reshape(-1, L)
         T = torch.empty((qd.shape[0], L, 12), dtype=torch.float32, device="cuda")
-        check(lib().kgpu_fk(self.handle, robot, _dptr(qd), qd.shape[0], _dptr(T), _stream()))
+        err = torch.empty((qd.shape[0], L), dtype=torch.float32, device="cuda") if with_error else None
+        check(lib().kgpu_fk(self.handle, robot, _dptr(qd), qd.shape[0], _dptr(T), _dptr(err), _stream()))
         if sync:
             self.sync()
-        return T
+        return (T, err) if with_error else T
 
     def check_configs(self, q, robot: int = 0, env: bool = True, self_collision: bool = True,
                       sync: bool = True):

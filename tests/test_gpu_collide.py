@@ -44,21 +44,42 @@ def cfg1(built):
     w.close()
 
 
-def test_fk_error_within_band(cfg0):
-    """FP32 forward kinematics stays far inside the inflation band."""
-    robot, env, q, w, o = cfg0
-    T = w.fk(q[:256]).cpu().numpy().astype(np.float64)
-    eps = w.get_option("eps_band")
-    worst = 0.0
-    for b in range(256):
+def _check_fk_bounds(w, o, robot, q):
+    """Every vertex placed with the FP32 transform lies within the reported
+    per-link bound of its FP64 placement."""
+    T, err = w.fk(q, with_error=True)
+    T = T.cpu().numpy().astype(np.float64)
+    err = err.cpu().numpy().astype(np.float64)
+    worst_ratio = 0.0
+    for b in range(len(q)):
         T64 = o.fk(q[b].astype(np.float64))
-        # compare where a point at the link's far end lands (lever 0.3 m)
-        for l in range(robot.num_links):
+        for l, (V, _) in enumerate(robot.meshes):
             R32, t32 = T[b, l, :9].reshape(3, 3), T[b, l, 9:]
             R64, t64 = T64[l, :9].reshape(3, 3), T64[l, 9:]
-            p = np.array([0.05, 0.05, 0.3])
-            worst = max(worst, np.abs(R32 @ p + t32 - (R64 @ p + t64)).max())
-    assert worst < eps / 8, (worst, eps)
+            d = np.linalg.norm(V @ R32.T + t32 - (V @ R64.T + t64), axis=1).max()
+            assert d <= err[b, l], (b, l, d, err[b, l])
+            worst_ratio = max(worst_ratio, d / err[b, l])
+    return worst_ratio, err
+
+
+def test_fk_error_bounds_hold(cfg0):
+    robot, env, q, w, o = cfg0
+    ratio, err = _check_fk_bounds(w, o, robot, q[:256])
+    # bounds are rigorous (ratio <= 1) and tight enough to be useful
+    assert ratio <= 1.0 and err.max() < 5e-5
+
+
+def test_fk_error_bounds_tree_robot(built):
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robot = sc.humanoid()
+    env = sc.env_from_objects("one_box", [sc.box_mesh((2, 2, 2), (0.1, 0.1, 0.1))])
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    q = sc.uniform_configs(robot, 64, np.random.default_rng(11))
+    ratio, err = _check_fk_bounds(w, o, robot, q)
+    assert ratio <= 1.0
+    w.close()
 
 
 def test_cfg0_verdicts_bit_exact(cfg0):
