@@ -1,0 +1,329 @@
+"""Benchmark of the batched planner edge-check path (one JSON line on rank 0).
+
+Workload (the headline configuration): 7-DOF arm, 2,112 triangles per link,
+among 2,000 icospheres (subdivision 2, 640k triangles), 16,384 straight-line
+planner edges of 2..400 steps at 0.01 rad; output the first infeasible step
+of every edge.  A step of this benchmark is one pass over all 16,384 edges.
+
+Reported:
+  value         collision-checked configurations per second (edge steps up
+                to and including each edge's first collision, or all steps of
+                a free edge), device-resident inputs, edge plan replayed as a
+                CUDA graph, L2 flushed (256 MiB write) before every step
+  e2e           the same metric through the C ABI with host buffers
+                (kgpu_check_edges_host: pinned staging, H2D of the edges, D2H
+                of the first-hit indices inside the timed region)
+  plain_fp64    the plain FP64 GPU method on the same edges (configs/s)
+  roofline      algorithmic bytes (FP64 oracle's canonical traversal counts:
+                32 B per BVH node pair, 72 B per triangle pair, plus q and the
+                output) per step / step time, against the measured HBM copy
+                bandwidth
+  cpu_baseline  the FP64 CPU oracle on all host cores over the same edges
+  mismatches    first-hit indices that differ from the oracle's (must be 0)
+
+--impl reference times the reference path's CPU implementation (the FP64
+oracle restatement; the reference's own KrisLibrary code is not part of the
+Klamp't tree and cannot be built here) on all host cores.
+Multi-GPU: edges are independent, so every rank runs the same workload on its
+own GPU (replicas, weak scaling); no collective on the data path.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "collision-checked configs/s and dist+grad evals/s, chosen vs plain GPU, 0 mismatches"
+WORKLOAD = ("7-DOF arm (2,112 tris/link) among 2,000 icospheres (640k tris); 16,384 planner edges, "
+            "2-400 steps at 0.01 rad; first infeasible step per edge")
+NODE_BYTES = 32
+TRI_PAIR_BYTES = 72
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=60)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="engine", choices=["engine", "reference"])
+    p.add_argument("--edges", type=int, default=16384)
+    p.add_argument("--engine-only", action="store_true",
+                   help="only warm-up + timed edge-plan launches (profiling runs); prints the device time")
+    return p.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per checked configuration of the engine kernel, from the
+    committed ncu summary (profiles/k_engine_edges.md), or None."""
+    path = os.path.join(ROOT, "profiles", "k_engine_edges.md")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        for line in f:
+            if line.startswith("dram_bytes_per_item:"):
+                try:
+                    return float(line.split(":", 1)[1].strip())
+                except ValueError:
+                    return None
+    return None
+
+
+def checked_configs(first_hit: np.ndarray, nsteps: np.ndarray) -> int:
+    return int(np.where(first_hit < 0, nsteps + 1, first_hit + 1).sum())
+
+
+def run_reference(args, rank):
+    from klampt_gb300 import scenes as sc
+    from oracle.oracle_py import Oracle
+
+    if rank != 0:
+        return
+    robot, env, (qa, qb, ns) = sc.scene_cfg1(n_edges=args.edges)
+    o = Oracle(robot, env)
+    cores = os.cpu_count() or 1
+    # each step: a bounded sample of the workload (1/4 of the edges)
+    E = max(1, args.edges // 4)
+    idx = np.arange(E)
+    for _ in range(args.warmup):
+        o.check_edges(qa[idx], qb[idx], ns[idx], nthreads=cores)
+    total = 0
+    t0 = time.perf_counter()
+    for s in range(args.steps):
+        sel = (idx + s * E) % args.edges
+        fh, cnt = o.check_edges(qa[sel], qb[sel], ns[sel], nthreads=cores)
+        total += checked_configs(fh, ns[sel])
+    dt = time.perf_counter() - t0
+    v = total / dt
+    line = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "configs/s", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "edges_per_step": int(E)},
+        "cpu_baseline": {"value": v, "unit": "configs/s", "cores": cores, "kind": "port",
+                         "sample": f"{E} of {args.edges} edges per step (rotating), all steps of each edge "
+                                   "up to its first collision"},
+        "e2e": {"value": v, "unit": "configs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    from klampt_gb300 import build as kbuild
+    kbuild.build()
+    from klampt_gb300 import scenes as sc
+    from klampt_gb300.engine import World
+
+    robot, env, (qa, qb, ns) = sc.scene_cfg1(n_edges=args.edges)
+    w = World(env, [robot])
+    a = torch.as_tensor(qa).cuda()
+    b = torch.as_tensor(qb).cuda()
+    n = torch.as_tensor(ns).cuda()
+    out = torch.empty(args.edges, dtype=torch.int32, device="cuda")
+    plan = w.edge_plan(a, b, n, out)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup if args.engine_only else max(3, args.warmup)):
+        plan.launch()
+    w.sync()
+    fh = out.cpu().numpy()
+    per_step = checked_configs(fh, ns)
+    if args.engine_only:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            plan.launch()
+        w.sync()
+        print(json.dumps({"engine_only": True, "edges": args.edges, "configs_checked_per_step": per_step,
+                          "ms_per_step": 1e3 * (time.perf_counter() - t0) / max(1, args.steps)}), flush=True)
+        return
+
+    # ---- timed region: K plan launches, L2 flushed before each -------------
+    clocks = ClockSampler(local)
+    clocks.start()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    evs = []
+    for _ in range(args.steps):
+        flush.zero_()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.launch()
+        e1.record(stream)
+        evs.append((e0, e1))
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    clk = clocks.stop()
+    w.sync()
+    step_ms = [x.elapsed_time(y) for x, y in evs]
+    t_dev = sum(step_ms) / 1e3
+    if world > 1:
+        tt = torch.tensor([t_dev], device="cuda")
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_dev = float(tt.item())
+    value = world * per_step * args.steps / t_dev
+
+    # ---- end to end through the C ABI with host buffers ----------------------
+    for _ in range(2):
+        w.check_edges_host(qa, qb, ns)
+    t0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        fh_h = w.check_edges_host(qa, qb, ns)
+    t_e2e = time.perf_counter() - t0
+    e2e = {"value": world * per_step * e2e_steps / t_e2e, "unit": "configs/s",
+           "h2d_bytes_per_step": int(qa.nbytes + qb.nbytes + ns.nbytes), "d2h_bytes_per_step": int(fh_h.nbytes)}
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+
+    # ---- plain FP64 GPU method on the same edges (one thread per edge) -------
+    sub = args.edges
+    torch.cuda.synchronize()
+    p0 = torch.cuda.Event(enable_timing=True)
+    p1 = torch.cuda.Event(enable_timing=True)
+    p0.record(stream)
+    fh_plain = w.check_edges_plain64(a[:sub], b[:sub], n[:sub], sync=False)
+    p1.record(stream)
+    w.sync()
+    plain_rate = checked_configs(fh_plain.cpu().numpy(), ns[:sub]) / (p0.elapsed_time(p1) / 1e3)
+
+    # ---- FP64 oracle on the host cores: parity, canonical counts, baseline ---
+    from oracle.oracle_py import Oracle
+    o = Oracle(robot, env)
+    cores = os.cpu_count() or 1
+    c0 = time.perf_counter()
+    fh_o, cnt = o.check_edges(qa, qb, ns, nthreads=cores)
+    c_dt = time.perf_counter() - c0
+    mismatches = int((fh_o != fh).sum()) + int((fh_plain.cpu().numpy() != fh_o[:sub]).sum())
+    cpu_rate = checked_configs(fh_o, ns) / c_dt
+    items = int(cnt[2])
+    alg_bytes = int(cnt[0]) * NODE_BYTES + int(cnt[1]) * TRI_PAIR_BYTES + items * (4 * robot.num_links) + 4 * len(ns)
+    achieved = alg_bytes / (t_dev / args.steps) / 1e9
+    peak, peak_kind = peaks()
+    traffic_per_item = profiled_traffic()
+    traffic = traffic_per_item * per_step if traffic_per_item is not None else None
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "configs/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * t_dev / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 traversal + f64 band", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "edges": args.edges, "configs_checked_per_step": per_step,
+                   "env_tris": int(env.num_tris), "l2": "flushed (256 MiB write) before every step",
+                   "launch": "CUDA-graph edge plan"},
+        "e2e": e2e,
+        "gpu_launches": 5 * args.steps,
+        "plain_fp64": {"value": plain_rate, "unit": "configs/s", "edges": sub, "speedup": value / plain_rate},
+        "mismatches": mismatches,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_step": alg_bytes},
+        "cpu_baseline": {"value": cpu_rate, "unit": "configs/s", "cores": cores, "kind": "port",
+                         "sample": f"all {len(ns)} edges, FP64 oracle, std::thread over all cores"},
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    plan.close()
+    w.close()
+    if world > 1:
+        torch.distributed.barrier()
+
+
+if __name__ == "__main__":
+    main()

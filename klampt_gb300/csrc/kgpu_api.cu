@@ -252,13 +252,14 @@ kgpu_status kgpu_robot_create(const kgpu_robot_desc* d, kgpu_robot* out)
   R->margins.assign(L, 0.0);
   if (d->margins) R->margins.assign(d->margins, d->margins + L);
   for (int i = 0; i < L; ++i) {
-    if (R->parents[i] >= i || R->parents[i] < -1) {
+    const int par = R->parents[i], jt = R->jtypes[i];
+    if (par >= i || par < -1) {
       delete R;
-      return fail(KGPU_ERR_INVALID, "link %d: parent %d must be -1 or a smaller index", i, R->parents[i]);
+      return fail(KGPU_ERR_INVALID, "link %d: parent %d must be -1 or a smaller index", i, par);
     }
-    if (R->jtypes[i] < 0 || R->jtypes[i] > 2) {
+    if (jt < 0 || jt > 2) {
       delete R;
-      return fail(KGPU_ERR_INVALID, "link %d: joint type %d unknown", i, R->jtypes[i]);
+      return fail(KGPU_ERR_INVALID, "link %d: joint type %d unknown", i, jt);
     }
     double n2 = R->axes[3 * i] * R->axes[3 * i] + R->axes[3 * i + 1] * R->axes[3 * i + 1] +
                 R->axes[3 * i + 2] * R->axes[3 * i + 2];

@@ -544,27 +544,72 @@ __global__ void k_edges_prep1(const int* nsteps, int E, int* hist, int* meta, in
   atomicMax(meta + 0, n);
 }
 
-// hist[v] -> base position of edges with n == v in the descending order;
-// round_off[k] = number of items in rounds < k; meta[1] = total items.
-__global__ void k_edges_prep2(int* hist, int* round_off, int* meta)
+// inclusive scan of one value per thread over a 1024-thread block
+__device__ __forceinline__ long long block_scan_incl(long long v, long long* sh)
 {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  int maxn = meta[0];
-  long long count = 0;  // edges with n > v
-  for (int v = maxn; v >= 0; --v) {
-    int h = hist[v];
-    hist[v] = (int)count;  // base
-    count += h;
-    round_off[v + 1] = (int)count;  // temporarily: count_ge[v]
+  const int t = threadIdx.x;
+  sh[t] = v;
+  __syncthreads();
+  for (int o = 1; o < 1024; o <<= 1) {
+    long long x = t >= o ? sh[t - o] : 0;
+    __syncthreads();
+    sh[t] += x;
+    __syncthreads();
   }
-  long long acc = 0;
-  round_off[0] = 0;
-  for (int k = 0; k <= maxn; ++k) {
-    long long c = round_off[k + 1];
-    round_off[k + 1] = (int)(acc + c);
-    acc += c;
+  long long r = sh[t];
+  __syncthreads();
+  return r;
+}
+
+// One block of 1024 threads.  count_ge[v] = edges with n >= v (suffix sum of
+// the histogram); hist[v] becomes the base position of the edges with n == v
+// in the descending-n order (= count_ge[v+1]); round_off[k] = number of items
+// in rounds < k (prefix sum of count_ge); meta[1] = total items.
+__global__ void __launch_bounds__(1024) k_edges_prep2(int* hist, int* round_off, int* meta, int* status)
+{
+  __shared__ long long sh[1024];
+  const int t = threadIdx.x;
+  const int maxn = meta[0];
+  const int len = maxn + 1;
+  const int chunk = (len + 1023) / 1024;
+  // suffix sums: thread t owns bins [t*chunk, (t+1)*chunk) counted from the top
+  long long local = 0;
+  for (int i = 0; i < chunk; ++i) {
+    int v = maxn - (t * chunk + i);
+    if (v >= 0) local += hist[v];
   }
-  meta[1] = acc > INT_MAX ? INT_MAX : (int)acc;
+  long long before = block_scan_incl(local, sh) - local;  // edges with larger n
+  long long run = before;
+  for (int i = 0; i < chunk; ++i) {
+    int v = maxn - (t * chunk + i);
+    if (v >= 0) {
+      int h = hist[v];
+      hist[v] = (int)run;  // base = count_ge[v+1]
+      run += h;
+      round_off[v + 1] = (int)run;  // count_ge[v], scanned below
+    }
+  }
+  __syncthreads();
+  // prefix sums of count_ge over k = 0..maxn, thread t owns [t*chunk, ...)
+  local = 0;
+  for (int i = 0; i < chunk; ++i) {
+    int k = t * chunk + i;
+    if (k <= maxn) local += round_off[k + 1];
+  }
+  __syncthreads();
+  long long acc = block_scan_incl(local, sh) - local;
+  for (int i = 0; i < chunk; ++i) {
+    int k = t * chunk + i;
+    if (k <= maxn) {
+      acc += round_off[k + 1];
+      round_off[k + 1] = acc > INT_MAX ? INT_MAX : (int)acc;
+    }
+  }
+  if (t == 0) round_off[0] = 0;
+  if (t == 1023) {
+    if (acc > INT_MAX) atomicCAS(status, 0, KGPU_ERR_INVALID);
+    meta[1] = acc > INT_MAX ? INT_MAX : (int)acc;
+  }
 }
 
 __global__ void k_edges_prep3(const int* nsteps, int E, const int* base, int* fill, int* perm)
@@ -687,7 +732,7 @@ cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S
   if ((err = cudaMemsetAsync(fill, 0, sizeof(int) * (kMaxSteps + 2), s)) != cudaSuccess) return err;
   int tb = 256, gb = (E + tb - 1) / tb;
   k_edges_prep1<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, S.edge_meta, first_hit, status);
-  k_edges_prep2<<<1, 32, 0, s>>>(S.edge_hist, S.edge_round_off, S.edge_meta);
+  k_edges_prep2<<<1, 1024, 0, s>>>(S.edge_hist, S.edge_round_off, S.edge_meta, status);
   k_edges_prep3<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, fill, S.edge_perm);
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   EngineArgs A = {};

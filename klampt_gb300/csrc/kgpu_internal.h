@@ -62,6 +62,7 @@ struct KRobotDev {
   int jtype[kMaxLinks];
   int link_root[kMaxLinks];  // global node index or -1
   int link_depth[kMaxLinks];
+  int link_vert_first[kMaxLinks], link_vert_count[kMaxLinks];  // unique vertices (global)
   uint32_t env_mask[kMaxLinks];
   float link_margin[kMaxLinks];
   float link_r[kMaxLinks];   // largest vertex norm of the link mesh in its frame (rounded up)
@@ -82,6 +83,9 @@ struct KWorldDev {
   const float4* ltri32;      // 3 per tri
   const double* ltri64;      // 9 per tri
   const double* lnode64;     // 6 per node (c, h) FP64 (plain kernel)
+  const int* ltri_orig;      // per link triangle: index in its link's mesh order
+  const float4* lvert32;     // unique link vertices (link frame), mesh order
+  const double* lvert64;     // 3 per unique link vertex
   // environment
   const KNode* enodes;
   const float4* etri32;
@@ -94,6 +98,11 @@ struct KWorldDev {
   const int* obj_group;
   const uint8_t* obj_convex;
   const int* node_obj;       // per env node
+  const int* etri_orig;      // per env triangle (leaf order): global input index
+  const float4* eface32;     // per env triangle: unit outward normal, n . a  (FP32)
+  const double* eface64;     // 4 per env triangle: the same in canonical FP64
+  const int* obj_leaf_first; // per object: its triangles' leaf-order range
+  const int* obj_leaf_count;
   int group_root[kMaxGroups];
   float group_margin[kMaxGroups];
   int num_objects;
@@ -133,6 +142,7 @@ struct kgpu_robot_s {
   // device arrays of this robot's links (local indices per link)
   std::vector<kgpu::HostBvh> bvh;
   std::vector<std::vector<double>> tri64;  // per link, leaf order, 9 per tri
+  std::vector<std::vector<double>> vert64; // per link, unique vertices in mesh order
   double reach = 0.0;                      // bound on |world coordinate| of any link point
 };
 
@@ -159,6 +169,11 @@ struct kgpu_env_s {
   int* d_obj_group = nullptr;
   uint8_t* d_obj_convex = nullptr;
   int* d_node_obj = nullptr;
+  int* d_tri_orig = nullptr;
+  float4* d_face32 = nullptr;
+  double* d_face64 = nullptr;
+  int* d_obj_leaf_first = nullptr;
+  int* d_obj_leaf_count = nullptr;
   int group_root[kgpu::kMaxGroups];
   float group_margin[kgpu::kMaxGroups];
   size_t n_nodes = 0, n_tris = 0;
@@ -176,6 +191,10 @@ struct kgpu_world_s {
   float4* d_ltri32 = nullptr;
   double* d_ltri64 = nullptr;
   double* d_lnode64 = nullptr;
+  int* d_ltri_orig = nullptr;
+  float4* d_lvert32 = nullptr;
+  double* d_lvert64 = nullptr;
+  std::vector<int> robot_vert_base;
   int* d_status = nullptr;
   unsigned long long* d_stats = nullptr;
   std::vector<int> robot_node_base, robot_tri_base;
@@ -185,7 +204,7 @@ struct kgpu_world_s {
   // tolerances
   double eps_env = 0.0;
   double eps_extra = 0.0;
-  int blocks_per_sm = 2;   // resident 8-warp engine blocks per SM (2, 3 or 4)
+  int blocks_per_sm = 3;   // resident 8-warp engine blocks per SM (2, 3 or 4)
   int num_sms = 0;
   bool tables_dirty = true;
   // pinned staging for the host-buffer entry points

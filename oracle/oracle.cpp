@@ -154,6 +154,7 @@ struct Env {
   double group_margin[32];
   std::vector<Bvh> obj_bvh;     // ids are global triangle ids
   std::vector<double> obj_c, obj_h;
+  std::vector<double> face_n, face_top;  // unit outward normal and n . a per triangle
 };
 
 inline void xform_box(const double* T, const Node& n, double* c, double* h)
@@ -320,10 +321,13 @@ bool in_limits(const Robot& R, const double* q)
 //   semantics), ties resolved to the lexicographically smallest
 //   (link triangle, object triangle) pair; search bounded by ub2.
 //   Signed part (convex obstacles only): if the surfaces meet (distance 0),
-//   d = -pen with pen = min over faces f of the obstacle of
-//   (n_f . a_f - min over link vertices v of n_f . v); n_f the unit outward
-//   face normal, a_f the face's first vertex.  The feature pair is then
-//   (v*, f*) and d/dv* = n_f*.
+//   d = -depth, depth = the largest depth of a link vertex inside the
+//   obstacle, depth(v) = min over obstacle faces f of (n_f . a_f - n_f . v)
+//   (n_f the unit outward face normal, a_f the face's first vertex; for a
+//   convex obstacle this is v's distance to the boundary when v is inside),
+//   0 when no vertex is strictly inside.  d is continuous at the onset of
+//   contact.  Feature pair (v*, f*), d/dv* = n_f*; ties resolve to the first
+//   vertex, then the first face, in mesh order.
 // ---------------------------------------------------------------------------
 struct PairResult {
   double d;          // signed distance (or the bound when nothing is closer)
@@ -344,33 +348,38 @@ void face_normal(const double* F, double* n)
   for (int i = 0; i < 3; ++i) n[i] = kx_div(c[i], len);
 }
 
+// deepest link vertex inside convex object o; returns the depth (0 if no
+// vertex is strictly inside), its vertex and face.  Vertices outside the
+// object's bounding box cannot be inside and are skipped.
 double penetration(Ctx& c, int l, int o, int* fbest, int* vbest, double* nbest)
 {
   const Env& E = *c.E;
   const std::vector<double>& V = c.link_verts(l);
   int nv = (int)(V.size() / 3);
-  double best = 1e300;
+  double best = 0.0;
   *fbest = -1;
   *vbest = -1;
-  for (int f = E.obj_first[o]; f < E.obj_first[o] + E.obj_count[o]; ++f) {
-    const double* F = &E.tri[9 * (size_t)f];
-    double n[3];
-    face_normal(F, n);
-    double top = kx_dot3(n, F);
-    double mn = 1e300;
-    int vi = -1;
-    for (int v = 0; v < nv; ++v) {
-      double p = kx_dot3(n, &V[3 * (size_t)v]);
-      if (p < mn) { mn = p; vi = v; }
+  const double* oc = &E.obj_c[3 * o];
+  const double* oh = &E.obj_h[3 * o];
+  for (int v = 0; v < nv; ++v) {
+    const double* x = &V[3 * (size_t)v];
+    if (fabs(x[0] - oc[0]) > oh[0] * (1 + 1e-12) + 1e-12 || fabs(x[1] - oc[1]) > oh[1] * (1 + 1e-12) + 1e-12 ||
+        fabs(x[2] - oc[2]) > oh[2] * (1 + 1e-12) + 1e-12)
+      continue;
+    double dmin = 1e300;
+    int fmin = -1;
+    for (int f = E.obj_first[o]; f < E.obj_first[o] + E.obj_count[o]; ++f) {
+      double dep = kx_sub(E.face_top[f], kx_dot3(&E.face_n[3 * (size_t)f], x));
+      if (dep < dmin) { dmin = dep; fmin = f; }
     }
-    double pen = kx_sub(top, mn);
-    if (pen < best) {
-      best = pen;
-      *fbest = f;
-      *vbest = vi;
-      nbest[0] = n[0]; nbest[1] = n[1]; nbest[2] = n[2];
+    if (dmin > best) {
+      best = dmin;
+      *vbest = v;
+      *fbest = fmin;
     }
   }
+  if (*fbest >= 0)
+    for (int i = 0; i < 3; ++i) nbest[i] = E.face_n[3 * (size_t)*fbest + i];
   return best;
 }
 
@@ -443,6 +452,18 @@ PairResult pair_distance(Ctx& c, int l, int o, double bound)
     int f, v;
     double n[3];
     double pen = penetration(c, l, o, &f, &v, n);
+    if (v < 0) {  // surfaces meet, no vertex inside: d = 0 with no direction
+      if (0.0 < bound) {
+        res.found = 1;
+        res.d = 0.0;
+        std::memcpy(res.cp, bcp, sizeof bcp);
+        std::memcpy(res.cq, bcq, sizeof bcq);
+        res.dir[0] = res.dir[1] = res.dir[2] = 0.0;
+        res.ta = bta;
+        res.tb = btb;
+      }
+      return res;
+    }
     double d = -pen;
     if (d < bound) {
       const std::vector<double>& V = c.link_verts(l);
@@ -644,6 +665,12 @@ void* orc_env_create(int N, const int* vert_off, const double* verts, const int*
           E->tri[9 * (size_t)t + 3 * v + i] = verts[3 * ((size_t)vert_off[o] + tris[3 * (size_t)t + v]) + i];
     }
   }
+  E->face_n.resize(3 * ntot);
+  E->face_top.resize(ntot);
+  for (size_t t = 0; t < ntot; ++t) {
+    face_normal(&E->tri[9 * t], &E->face_n[3 * t]);
+    E->face_top[t] = kx_dot3(&E->face_n[3 * t], &E->tri[9 * t]);
+  }
   for (int g = 0; g < 32; ++g) {
     std::vector<int> ids;
     double gm = 0;
@@ -725,6 +752,53 @@ int orc_check_configs(void* robot, void* env, const unsigned* masks, const float
       counters[1] += x.tri_pairs;
       counters[2] += x.items;
     }
+  }
+  return 0;
+}
+
+/* the same verdicts by testing every triangle pair (no BVH): validates the
+ * oracle's own culling on small meshes */
+int orc_check_configs_brute(void* robot, void* env, const unsigned* masks, const float* q, int B,
+                            unsigned char* env_hit, unsigned char* self_hit)
+{
+  Robot* R = (Robot*)robot;
+  Env* E = (Env*)env;
+  Ctx c;
+  c.init(R, E, masks);
+  double qd[ORC_MAXL];
+  for (int b = 0; b < B; ++b) {
+    for (int i = 0; i < R->L; ++i) qd[i] = (double)q[(size_t)b * R->L + i];
+    c.set_config(qd);
+    bool eh = false, sh = false;
+    for (int l = 0; l < R->L && !eh; ++l) {
+      int nt = (int)(R->tloc[l].size() / 9);
+      for (int o = 0; o < E->N && !eh; ++o) {
+        if (!((masks[l] >> E->groups[o]) & 1u)) continue;
+        double m = R->margins[l] + E->margins[o];
+        for (int ta = 0; ta < nt && !eh; ++ta)
+          for (int tb = E->obj_first[o]; tb < E->obj_first[o] + E->obj_count[o] && !eh; ++tb) {
+            const double* P = c.link_tri(l, ta);
+            const double* Q = &E->tri[9 * (size_t)tb];
+            double cp[3], cq[3];
+            eh = m == 0.0 ? kx_tri_tri_overlap(P, Q) != 0 : kx_tri_tri_dist2(P, Q, cp, cq) <= m * m;
+          }
+      }
+    }
+    for (int i = 0; i < R->L && !sh; ++i)
+      for (int j = i + 1; j < R->L && !sh; ++j) {
+        if (!R->self_mask[i * R->L + j]) continue;
+        int na = (int)(R->tloc[i].size() / 9), nb = (int)(R->tloc[j].size() / 9);
+        double m = R->margins[i] + R->margins[j];
+        for (int ta = 0; ta < na && !sh; ++ta)
+          for (int tb = 0; tb < nb && !sh; ++tb) {
+            const double* P = c.link_tri(i, ta);
+            const double* Q = c.link_tri(j, tb);
+            double cp[3], cq[3];
+            sh = m == 0.0 ? kx_tri_tri_overlap(P, Q) != 0 : kx_tri_tri_dist2(P, Q, cp, cq) <= m * m;
+          }
+      }
+    if (env_hit) env_hit[b] = eh;
+    if (self_hit) self_hit[b] = sh;
   }
   return 0;
 }

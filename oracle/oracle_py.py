@@ -126,6 +126,16 @@ class Oracle:
                                 ctypes.c_int(nthreads), _p(cnt))
         return env_hit, self_hit, cnt
 
+    def check_configs_brute(self, q):
+        """Verdicts by testing every triangle pair (no BVH culling)."""
+        q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, self.nl)
+        B = q.shape[0]
+        eh = np.zeros(B, np.uint8)
+        sh = np.zeros(B, np.uint8)
+        lib().orc_check_configs_brute(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(self.masks),
+                                      _p(q), ctypes.c_int(B), _p(eh), _p(sh))
+        return eh, sh
+
     def is_feasible(self, q, nthreads: int = 1) -> np.ndarray:
         q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, self.nl)
         out = np.zeros(q.shape[0], np.uint8)

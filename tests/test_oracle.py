@@ -1,0 +1,233 @@
+"""Pins the FP64 oracle: known-answer tests (including the rotation
+convention vector of the reference's own tests/test_math_so3.py), independent
+cross-checks of the canonical triangle predicates, and brute force vs BVH
+culling.  CPU only."""
+
+import math
+import os
+
+import numpy as np
+import pytest
+
+from klampt_gb300 import scenes as sc
+from oracle import oracle_py as op
+
+NT = os.cpu_count() or 2
+
+
+def one_link_robot(mesh, axis=(0, 0, 1)):
+    V, F = mesh
+    return sc.RobotSpec(name="one", parents=np.array([-1], np.int32), joint_types=np.zeros(1, np.int32),
+                        T0_parent=np.array([[1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0]], np.float64),
+                        axes=np.array([axis], np.float64), qmin=np.array([-math.pi]), qmax=np.array([math.pi]),
+                        meshes=[(V, F)])
+
+
+def test_sincos_accuracy():
+    x = np.random.default_rng(0).uniform(-100, 100, 200000)
+    s, c = op.sincos(x)
+    ulp = lambda a, b: np.max(np.abs(a - b) / np.spacing(np.maximum(np.abs(b), 1e-300)))
+    assert ulp(s, np.sin(x)) <= 2 and ulp(c, np.cos(x)) <= 2
+    s0, c0 = op.sincos(np.array([0.0, math.pi / 2, -math.pi]))
+    assert s0[0] == 0.0 and c0[0] == 1.0
+    assert abs(s0[1] - 1) < 1e-16 and abs(c0[2] + 1) < 1e-16
+
+
+def test_rotation_convention_matches_reference_so3_vector():
+    """tests/test_math_so3.py:15-19 of the reference: the quaternion
+    (w,x,y,z) = (-4.32978e-17, -0.707107, 4.32978e-17, 0.707107) has
+    roll, pitch, yaw = (0, pi/2, pi), i.e. R = Rz(yaw) Ry(pitch) Rx(roll).
+    A z-y-x chain of revolute joints at those angles must give that matrix."""
+    w, x, y, z = (-4.32978e-17, -0.707107, 4.32978e-17, 0.707107)
+    n = math.sqrt(w * w + x * x + y * y + z * z)
+    w, x, y, z = w / n, x / n, y / n, z / n
+    Rq = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - w * z), 2 * (x * z + w * y)],
+                   [2 * (x * y + w * z), 1 - 2 * (x * x + z * z), 2 * (y * z - w * x)],
+                   [2 * (x * z - w * y), 2 * (y * z + w * x), 1 - 2 * (x * x + y * y)]])
+    I = [1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0]
+    box = sc.box_mesh((0, 0, 0), (0.1, 0.1, 0.1))
+    robot = sc.RobotSpec(name="zyx", parents=np.array([-1, 0, 1], np.int32), joint_types=np.zeros(3, np.int32),
+                         T0_parent=np.array([I, I, I], np.float64),
+                         axes=np.array([[0, 0, 1], [0, 1, 0], [1, 0, 0]], np.float64),
+                         qmin=np.full(3, -4.0), qmax=np.full(3, 4.0), meshes=[box, box, box])
+    o = op.Oracle(robot, None)
+    T = o.fk(np.array([math.pi, math.pi / 2, 0.0]))
+    assert np.allclose(T[2, :9].reshape(3, 3), Rq, atol=2e-6)
+
+
+def test_fk_planar_closed_form():
+    L1, L2 = 0.4, 0.25
+    I = [1, 0, 0, 0, 1, 0, 0, 0, 1]
+    box = sc.box_mesh((0, 0, 0), (0.01, 0.01, 0.01))
+    robot = sc.RobotSpec(name="planar", parents=np.array([-1, 0, 1], np.int32),
+                         joint_types=np.array([0, 0, 2], np.int32),
+                         T0_parent=np.array([I + [0, 0, 0], I + [L1, 0, 0], I + [L2, 0, 0]], np.float64),
+                         axes=np.array([[0, 0, 1], [0, 0, 1], [0, 0, 1]], np.float64),
+                         qmin=np.array([-4, -4, 0.0]), qmax=np.array([4, 4, 0.0]), meshes=[box, box, box])
+    o = op.Oracle(robot, None)
+    for q0, q1 in [(0.3, -1.1), (2.5, 0.7), (-3.0, 3.0)]:
+        T = o.fk(np.array([q0, q1, 0.0]))
+        ex = L1 * math.cos(q0) + L2 * math.cos(q0 + q1)
+        ey = L1 * math.sin(q0) + L2 * math.sin(q0 + q1)
+        assert abs(T[2, 9] - ex) < 1e-15 and abs(T[2, 10] - ey) < 1e-15
+    # prismatic: translation along the axis by q
+    robot.joint_types = np.array([1, 0, 2], np.int32)
+    o = op.Oracle(robot, None)
+    T = o.fk(np.array([0.2, 0.0, 0.0]))
+    assert abs(T[0, 11] - 0.2) < 1e-16
+
+
+@pytest.mark.parametrize("d,expect", [(0.5, 1), (0.999, 1), (1.0, 1), (1.0 + 1e-9, 0), (1.2, 0)])
+def test_box_box_known_answers(d, expect):
+    """Unit cubes (half extent 0.5) at centre distance d collide iff d <= 1;
+    touching faces count as collision."""
+    robot = one_link_robot(sc.box_mesh((0, 0, 0), (0.5, 0.5, 0.5)))
+    env = sc.env_from_objects("b", [sc.box_mesh((d, 0.0, 0.0), (0.5, 0.5, 0.5))])
+    o = op.Oracle(robot, env)
+    eh, _, _ = o.check_configs(np.zeros((1, 1), np.float32))
+    assert eh[0] == expect
+
+
+def test_containment_is_not_collision():
+    """Mesh-mesh collision tests surfaces (PQP semantics): a box strictly
+    inside another does not collide."""
+    robot = one_link_robot(sc.box_mesh((0, 0, 0), (0.1, 0.1, 0.1)))
+    env = sc.env_from_objects("b", [sc.box_mesh((0, 0, 0), (1, 1, 1))])
+    eh, _, _ = op.Oracle(robot, env).check_configs(np.zeros((1, 1), np.float32))
+    assert eh[0] == 0
+
+
+def test_margin_within_distance():
+    robot = one_link_robot(sc.box_mesh((0, 0, 0), (0.5, 0.5, 0.5)))
+    robot.margins = np.array([0.05])
+    env = sc.env_from_objects("b", [sc.box_mesh((1.04, 0, 0), (0.5, 0.5, 0.5))])
+    eh, _, _ = op.Oracle(robot, env).check_configs(np.zeros((1, 1), np.float32))
+    assert eh[0] == 1
+    env = sc.env_from_objects("b", [sc.box_mesh((1.06, 0, 0), (0.5, 0.5, 0.5))])
+    eh, _, _ = op.Oracle(robot, env).check_configs(np.zeros((1, 1), np.float32))
+    assert eh[0] == 0
+
+
+def test_sphere_sphere_distance_and_penetration():
+    """|c1-c2| - r1 - r2 (geometry_ad.py:160-163) within the icospheres'
+    polyhedral tolerance; overlapping spheres give negative distance."""
+    r1, r2 = 0.1, 0.2
+    robot = one_link_robot(sc.icosphere_mesh((0, 0, 0), r1, 3))
+    for D, tol in [(1.0, 2e-3), (0.25, 4e-3)]:
+        env = sc.env_from_objects("s", [sc.icosphere_mesh((D, 0, 0), r2, 3)])
+        o = op.Oracle(robot, env)
+        res = o.pair_distance(np.zeros(1, np.float32), 0, 0)
+        assert res["found"]
+        assert abs(res["d"] - (D - r1 - r2)) < tol, res["d"]
+        if D < r1 + r2:
+            assert res["signed"] and res["d"] < 0
+        else:
+            assert abs(res["cp"][0] - r1) < tol and abs(res["cq"][0] - (D - r2)) < tol
+            assert np.allclose(res["dir"], [-1, 0, 0], atol=0.05)
+
+
+def _np_seg_tri(p0, p1, a, b, c):
+    """Segment / triangle crossing (independent: Moller-Trumbore on the
+    segment's line), returns (crosses, robust)."""
+    e1, e2 = b - a, c - a
+    d = p1 - p0
+    h = np.cross(d, e2)
+    det = e1 @ h
+    if abs(det) < 1e-12:
+        return False, False
+    f = 1.0 / det
+    s = p0 - a
+    u = f * (s @ h)
+    qv = np.cross(s, e1)
+    v = f * (d @ qv)
+    t = f * (e2 @ qv)
+    m = 1e-9
+    inside = u > m and v > m and u + v < 1 - m and t > m and t < 1 - m
+    near = min(abs(u), abs(v), abs(1 - u - v), abs(t), abs(1 - t)) < 1e-7
+    return inside, not near
+
+
+def test_tri_tri_overlap_independent_crosscheck():
+    rng = np.random.default_rng(5)
+    agree = 0
+    for _ in range(3000):
+        P = rng.normal(size=(3, 3))
+        Q = rng.normal(size=(3, 3)) * 0.8 + rng.normal(size=3) * 0.5
+        hit, d2, cp, cq = op.tri_tri(P, Q)
+        cross, robust = False, True
+        for (X, Y) in ((P, Q), (Q, P)):
+            for i in range(3):
+                c, r = _np_seg_tri(X[i], X[(i + 1) % 3], Y[0], Y[1], Y[2])
+                cross |= c
+                robust &= r
+        if not robust:
+            continue
+        assert hit == cross
+        assert (d2 == 0.0) == hit
+        agree += 1
+    assert agree > 2500
+
+
+def test_tri_tri_distance_vs_sampling():
+    rng = np.random.default_rng(6)
+    g = np.linspace(0, 1, 41)
+    uu, vv = np.meshgrid(g, g)
+    m = (uu + vv) <= 1
+    bary = np.stack([1 - uu[m] - vv[m], uu[m], vv[m]], axis=1)
+    for _ in range(60):
+        P = rng.normal(size=(3, 3))
+        Q = rng.normal(size=(3, 3)) + rng.normal(size=3) * 3
+        hit, d2, cp, cq = op.tri_tri(P, Q)
+        if hit:
+            continue
+        SP, SQ = bary @ P, bary @ Q
+        dmin = np.sqrt(((SP[:, None, :] - SQ[None, :, :]) ** 2).sum(-1).min())
+        d = math.sqrt(d2)
+        assert d <= dmin + 1e-12
+        assert dmin - d < 0.15 * max(np.ptp(P, 0).max(), np.ptp(Q, 0).max()) / 40 * 4
+        assert abs(np.linalg.norm(cp - cq) - d) < 1e-12
+
+
+def test_bvh_culling_matches_brute_force():
+    """The oracle's BVH traversal returns exactly the all-pairs verdicts."""
+    robot = sc.arm(6, rings=4, segments=12)
+    env = sc.env_from_objects("boxes", sc.random_boxes(12, np.random.default_rng(3)))
+    o = op.Oracle(robot, env)
+    q = sc.uniform_configs(robot, 96, np.random.default_rng(4))
+    eh, sh, _ = o.check_configs(q, nthreads=NT)
+    eb, sb = o.check_configs_brute(q)
+    assert np.array_equal(eh, eb) and np.array_equal(sh, sb)
+    assert 0 < eh.sum() < len(q) and 0 < sh.sum() < len(q)
+
+
+def test_edge_first_hit_semantics():
+    """first_hit = first infeasible configuration a + (k/n)(b-a), k = 0..n."""
+    robot, env, q = sc.scene_cfg0()
+    o = op.Oracle(robot, env)
+    qa, qb, ns = sc.random_edges(robot, 48, np.random.default_rng(9))
+    fh, _ = o.check_edges(qa, qb, ns, nthreads=NT)
+    for e in range(48):
+        n = int(ns[e])
+        ks = np.arange(n + 1)
+        qs = (qa[e].astype(np.float64)[None, :] + (ks / n)[:, None] * (qb[e].astype(np.float64) - qa[e])[None, :])
+        feas = o.is_feasible(qs.astype(np.float32))
+        # the oracle interpolates in FP64 from the float endpoints; re-deriving
+        # the configurations in float32 can only flip borderline steps
+        bad = np.flatnonzero(feas == 0)
+        expect = int(bad[0]) if bad.size else -1
+        assert fh[e] == expect or abs(fh[e] - expect) <= 1
+
+
+def test_masks_exclude_terrain_for_base_links():
+    """PlannerSettings.cpp:34-41: links with parent -1 are not tested against
+    terrains (group 1)."""
+    robot = sc.arm(2, rings=4, segments=12)
+    terrain = sc.box_mesh((0, 0, 0.05), (1.0, 1.0, 0.02))  # cuts through link 0 only
+    env = sc.env_from_objects("t", [terrain], groups=[1], convex=[1])
+    o = op.Oracle(robot, env)
+    q = np.zeros((1, 2), np.float32)
+    eh, _, _ = o.check_configs(q)
+    assert eh[0] == 0
+    env2 = sc.env_from_objects("o", [terrain], groups=[0], convex=[1])
+    eh, _, _ = op.Oracle(robot, env2).check_configs(q)
+    assert eh[0] == 1
