@@ -113,6 +113,9 @@ void free_world_device(kgpu_world w)
   dfree(w->d_ltri32);
   dfree(w->d_ltri64);
   dfree(w->d_lnode64);
+  dfree(w->d_ltri_orig);
+  dfree(w->d_lvert32);
+  dfree(w->d_lvert64);
   dfree(w->d_status);
   dfree(w->d_stats);
   dfree(w->scratch.spill);
@@ -121,6 +124,7 @@ void free_world_device(kgpu_world w)
   dfree(w->scratch.edge_round_off);
   dfree(w->scratch.edge_perm);
   dfree(w->scratch.edge_meta);
+  dfree(w->scratch.dist_work);
   if (w->pinned) cudaFreeHost(w->pinned);
   w->pinned = nullptr;
   dfree(w->dstage);
@@ -141,8 +145,12 @@ kgpu_status refresh_tables(kgpu_world w)
     memset(&d, 0, sizeof d);
     d.nlinks = R->nlinks;
     int node_base = w->robot_node_base[r];
+    int vert_base = w->robot_vert_base[r];
     int depth_max = 0;
     for (int i = 0; i < R->nlinks; ++i) {
+      d.link_vert_first[i] = vert_base;
+      d.link_vert_count[i] = (int)(R->vert64[i].size() / 3);
+      vert_base += d.link_vert_count[i];
       d.parents[i] = R->parents[i];
       d.jtype[i] = R->jtypes[i];
       d.link_root[i] = R->bvh[i].nodes.empty() ? -1 : node_base;
@@ -280,6 +288,7 @@ kgpu_status kgpu_robot_create(const kgpu_robot_desc* d, kgpu_robot* out)
     }
   R->bvh.resize(L);
   R->tri64.resize(L);
+  R->vert64.resize(L);
   R->link_tri_count.assign(L, 0);
   R->link_r.assign(L, 0.0);
   double reach_link = 0.0;
@@ -322,6 +331,7 @@ kgpu_status kgpu_robot_create(const kgpu_robot_desc* d, kgpu_robot* out)
     for (int k = 0; k < nt; ++k)
       for (int i = 0; i < 9; ++i) R->tri64[l][9 * (size_t)k + i] = tri[9 * (size_t)R->bvh[l].order[k] + i];
     R->link_tri_count[l] = nt;
+    R->vert64[l].assign(d->verts + 3 * (size_t)v0, d->verts + 3 * (size_t)v1);
   }
   double chain = 0.0;
   for (int i = 0; i < L; ++i)
@@ -420,6 +430,27 @@ kgpu_status kgpu_env_create(const kgpu_env_desc* d, kgpu_env* out)
   std::vector<float4> tri32(3 * leaf_tris.size());
   std::vector<double> tri64l(9 * leaf_tris.size());
   std::vector<int> tobj(leaf_tris.size());
+  // canonical FP64 face planes (unit outward normal n = e0 x e1 / |.|, and
+  // n . a with a the first vertex), as the oracle computes them, in leaf order
+  std::vector<double> face64(4 * leaf_tris.size());
+  std::vector<float4> face32(leaf_tris.size());
+  std::vector<int> obj_leaf_first(N, -1), obj_leaf_count(N, 0);
+  for (size_t k = 0; k < leaf_tris.size(); ++k) {
+    const double* F = &E->tri64[9 * (size_t)leaf_tris[k]];
+    double e0[3], e1[3], c[3], n[3];
+    kx_sub3(F + 3, F, e0);
+    kx_sub3(F + 6, F, e1);
+    kx_cross3(e0, e1, c);
+    double len = kx_sqrt(kx_dot3(c, c));
+    for (int i = 0; i < 3; ++i) n[i] = kx_div(c[i], len);
+    double top = kx_dot3(n, F);
+    for (int i = 0; i < 3; ++i) face64[4 * k + i] = n[i];
+    face64[4 * k + 3] = top;
+    face32[k] = make_float4((float)n[0], (float)n[1], (float)n[2], (float)top);
+    int o = E->tri_obj[leaf_tris[k]];
+    if (obj_leaf_first[o] < 0) obj_leaf_first[o] = (int)k;
+    obj_leaf_count[o]++;
+  }
   for (size_t k = 0; k < leaf_tris.size(); ++k) {
     int t = leaf_tris[k];
     for (int v = 0; v < 3; ++v)
@@ -446,6 +477,11 @@ kgpu_status kgpu_env_create(const kgpu_env_desc* d, kgpu_env* out)
   if (e == cudaSuccess) e = upload(&E->d_obj_group, E->groups.data(), E->groups.size());
   if (e == cudaSuccess) e = upload(&E->d_obj_convex, E->convex.data(), E->convex.size());
   if (e == cudaSuccess) e = upload(&E->d_node_obj, node_obj.data(), node_obj.size());
+  if (e == cudaSuccess) e = upload(&E->d_tri_orig, leaf_tris.data(), leaf_tris.size());
+  if (e == cudaSuccess) e = upload(&E->d_face64, face64.data(), face64.size());
+  if (e == cudaSuccess) e = upload(&E->d_face32, face32.data(), face32.size());
+  if (e == cudaSuccess) e = upload(&E->d_obj_leaf_first, obj_leaf_first.data(), obj_leaf_first.size());
+  if (e == cudaSuccess) e = upload(&E->d_obj_leaf_count, obj_leaf_count.data(), obj_leaf_count.size());
   if (e != cudaSuccess) {
     kgpu_env_destroy(E);
     return cuda_fail(e, "environment upload");
@@ -468,6 +504,11 @@ kgpu_status kgpu_env_destroy(kgpu_env E)
   dfree(E->d_obj_group);
   dfree(E->d_obj_convex);
   dfree(E->d_node_obj);
+  dfree(E->d_tri_orig);
+  dfree(E->d_face64);
+  dfree(E->d_face32);
+  dfree(E->d_obj_leaf_first);
+  dfree(E->d_obj_leaf_count);
   delete E;
   return KGPU_OK;
 }
@@ -486,24 +527,33 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&w->num_sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) e = engine_init();
+  if (e == cudaSuccess) e = dist_init();
   if (e != cudaSuccess) {
     delete w;
     return cuda_fail(e, "device query");
   }
   // link BVHs of every robot, concatenated
   std::vector<KNode> nodes;
-  std::vector<double> node64, tri64;
-  std::vector<float4> tri32;
+  std::vector<double> node64, tri64, lvert64;
+  std::vector<float4> tri32, lvert32;
+  std::vector<int> ltri_orig;
   double reach = 0.0;
   for (int r = 0; r < n; ++r) {
     kgpu_robot R = robots[r];
     w->robot_node_base.push_back((int)nodes.size());
     w->robot_tri_base.push_back((int)(tri32.size() / 3));
+    w->robot_vert_base.push_back((int)lvert32.size());
     for (int l = 0; l < R->nlinks; ++l) {
       append_bvh(R->bvh[l], (int)nodes.size(), (int)(tri32.size() / 3), nodes, node64);
       for (size_t k = 0; k < R->tri64[l].size(); k += 3)
         tri32.push_back(make_float4((float)R->tri64[l][k], (float)R->tri64[l][k + 1], (float)R->tri64[l][k + 2], 0.f));
       tri64.insert(tri64.end(), R->tri64[l].begin(), R->tri64[l].end());
+      for (int t : R->bvh[l].order) ltri_orig.push_back(t);
+      for (size_t k = 0; k < R->vert64[l].size(); k += 3) {
+        lvert32.push_back(make_float4((float)R->vert64[l][k], (float)R->vert64[l][k + 1],
+                                      (float)R->vert64[l][k + 2], 0.f));
+        lvert64.insert(lvert64.end(), R->vert64[l].begin() + k, R->vert64[l].begin() + k + 3);
+      }
     }
     reach = std::max(reach, R->reach);
     std::vector<uint32_t> mask(R->nlinks, 0xffffffffu);
@@ -520,11 +570,17 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   if (tri32.empty()) tri32.resize(3);
   if (tri64.empty()) tri64.resize(9);
   if (node64.empty()) node64.resize(6);
+  if (ltri_orig.empty()) ltri_orig.resize(1);
+  if (lvert32.empty()) lvert32.resize(1);
+  if (lvert64.empty()) lvert64.resize(3);
   e = cudaSuccess;
   if (e == cudaSuccess) e = upload(&w->d_lnodes, nodes.data(), nodes.size());
   if (e == cudaSuccess) e = upload(&w->d_lnode64, node64.data(), node64.size());
   if (e == cudaSuccess) e = upload(&w->d_ltri32, tri32.data(), tri32.size());
   if (e == cudaSuccess) e = upload(&w->d_ltri64, tri64.data(), tri64.size());
+  if (e == cudaSuccess) e = upload(&w->d_ltri_orig, ltri_orig.data(), ltri_orig.size());
+  if (e == cudaSuccess) e = upload(&w->d_lvert32, lvert32.data(), lvert32.size());
+  if (e == cudaSuccess) e = upload(&w->d_lvert64, lvert64.data(), lvert64.size());
   if (e == cudaSuccess) e = cudaMalloc((void**)&w->d_status, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(w->d_status, 0, sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc((void**)&w->d_stats, 8 * sizeof(unsigned long long));
@@ -554,6 +610,9 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   D.lnodes = w->d_lnodes;
   D.ltri32 = w->d_ltri32;
   D.ltri64 = w->d_ltri64;
+  D.ltri_orig = w->d_ltri_orig;
+  D.lvert32 = w->d_lvert32;
+  D.lvert64 = w->d_lvert64;
   D.lnode64 = w->d_lnode64;
   if (env) {
     D.enodes = env->d_nodes;
@@ -567,6 +626,11 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
     D.obj_group = env->d_obj_group;
     D.obj_convex = env->d_obj_convex;
     D.node_obj = env->d_node_obj;
+    D.etri_orig = env->d_tri_orig;
+    D.eface32 = env->d_face32;
+    D.eface64 = env->d_face64;
+    D.obj_leaf_first = env->d_obj_leaf_first;
+    D.obj_leaf_count = env->d_obj_leaf_count;
     D.num_objects = env->nobj;
     for (int g = 0; g < kMaxGroups; ++g) {
       D.group_root[g] = env->group_root[g];
@@ -780,9 +844,10 @@ kgpu_status kgpu_distance(kgpu_world w, int32_t robot, const float* q, int32_t B
   kgpu_status st = check_world(w, robot);
   if (st) return st;
   if (B < 0 || (B > 0 && (!q || !d || !pair || !cp))) return fail(KGPU_ERR_INVALID, "bad buffers");
-  if (!(cutoff > 0)) return fail(KGPU_ERR_INVALID, "cutoff must be positive");
-  return launch_status(launch_distance(w->dev, w->scratch, robot, q, B, cutoff, d, pair, cp, grad, grid_blocks(w),
-                                       w->blocks_per_sm,(cudaStream_t)s),
+  if (!(cutoff > 0) || !(cutoff < 1e30)) return fail(KGPU_ERR_INVALID, "cutoff must be positive and finite");
+  if (!w->env) return fail(KGPU_ERR_EMPTY, "distance query without an environment (robotsim.cpp:1786-1787)");
+  return launch_status(launch_distance(w->d_dev, w->scratch, robot, q, B, cutoff, d, pair, cp, grad, w->num_sms,
+                                       (cudaStream_t)s),
                        "kgpu_distance");
 }
 
@@ -793,8 +858,16 @@ kgpu_status kgpu_softmin_grad(kgpu_world w, int32_t robot, const float* q, int32
   if (st) return st;
   if (T < 0 || Wn < 1 || (T > 0 && (!q || !L))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if (!(tau > 0)) return fail(KGPU_ERR_INVALID, "tau must be positive");
-  return launch_status(launch_softmin(w->dev, w->scratch, robot, q, T, Wn, tau, L, dLdq, grid_blocks(w),
-                                      w->blocks_per_sm,(cudaStream_t)s),
+  if (!w->env) return fail(KGPU_ERR_EMPTY, "distance query without an environment (robotsim.cpp:1786-1787)");
+  size_t need = 2 * (size_t)T * Wn + T;
+  if (need > w->scratch.dist_work_cap) {
+    dfree(w->scratch.dist_work);
+    w->scratch.dist_work_cap = 0;
+    CK(cudaMalloc((void**)&w->scratch.dist_work, need * sizeof(double)));
+    w->scratch.dist_work_cap = need;
+  }
+  return launch_status(launch_softmin(w->d_dev, w->scratch, robot, q, T, Wn, tau, L, dLdq, w->robots[robot]->nlinks,
+                                      w->scratch.dist_work, w->num_sms, (cudaStream_t)s),
                        "kgpu_softmin_grad");
 }
 

@@ -1,18 +1,939 @@
-// kgpu_dist.cu — signed distance, soft-min and adjoint kernels.
+// kgpu_dist.cu — signed link-obstacle distance, its minimum per configuration,
+// the soft-min over a trajectory, and the adjoint (gradient) kernels.
+//
+// Replaces the per-pair Geometry3D::distance_ext loop
+// (Python/klampt/src/robotsim.cpp:1782-1819; DistanceQueryResult conventions
+// Python/klampt/src/geometry.h:641-673), WorldPlannerSettings::
+// DistanceLowerBound (Cpp/Planning/PlannerSettings.cpp:372-483) and the
+// autodiff MinDistance / ADModule path (Python/klampt/math/autodiff/
+// geometry_ad.py:613-814, pytorch.py:72-115).
+//
+// Definition (the FP64 oracle's, bit for bit on the value):
+//   d(l, o) = min over triangle pairs of the canonical triangle distance
+//             (kx_tri_tri_dist2), ties to the smallest (link triangle, object
+//             triangle) index;  if that is 0 (surfaces meet) and o is convex,
+//             d = -(largest depth of a link vertex inside o), depth(v) =
+//             min over o's faces of (n_f . a_f - n_f . v), 0 if no vertex is
+//             strictly inside.
+//   min distance  = min over enabled (link, object) pairs, ties to the
+//                   smallest (link, object);
+//   soft-min      = m - tau log sum exp(-(d - m)/tau) over the trajectory's
+//                   pairs with d < m + K tau (K = 12), m the trajectory minimum.
+//
+// GPU method, one warp per configuration (waypoint):
+//   * FP32 FK with per-link error bounds (warp_fk32);
+//   * candidate (link, object) pairs from the object-aware environment tree by
+//     box lower bounds, evaluated nearest first; for the minimum, the bound
+//     starts at 5 cm and grows x4 until a pair is found below it;
+//   * per pair a warp-cooperative BVH-vs-BVH distance traversal in FP32 with
+//     conservative pruning; triangle pairs whose FP32 distance lies within the
+//     error band of the running minimum become candidates and are finalised
+//     in canonical FP64 (one pair per lane, lexicographic warp reduction);
+//     a pair certified intersecting in FP32 ends the search (distance 0);
+//   * depth: link vertices inside the object's box, FP32 min over faces,
+//     FP64 for those within the band of the deepest;
+//   * gradient: dd/dq_j = u . (w_j x (p - o_j)) (revolute), u . w_j
+//     (prismatic), with u = dd/dp at the link feature point p, accumulated as
+//     per-link force/moment sums and pulled back through the chain once per
+//     configuration (the adjoint of FK), on FP32 transforms.
+#include <cfloat>
+#include <climits>
+
 #include "kgpu_device.cuh"
 
 namespace kgpu {
 
-cudaError_t launch_distance(const KWorldDev&, const Scratch&, int, const float*, int, double, double*, int*,
-                            double*, float*, int, int, cudaStream_t)
+namespace {
+
+constexpr int kDW = 8;         // warps per block
+constexpr int kDStack = 512;   // node-pair stack entries per warp
+constexpr int kDGStack = 512;  // environment-tree stack for gathering objects
+constexpr int kDJobs = 64;     // leaf-pair jobs
+constexpr int kDCand = 64;     // FP64 triangle-pair candidates
+constexpr int kDPairs = 128;   // (link, object) candidates per link and round
+constexpr double kSoftK = 12.0;
+
+struct __align__(16) DistSmem {
+  uint2 stack[kDStack];
+  uint32_t gstack[kDGStack];
+  uint32_t jobA[kDJobs], jobB[kDJobs], jobOff[kDJobs + 1];
+  uint32_t candA[kDCand], candB[kDCand];
+  float candD[kDCand];
+  int pobj[kDPairs];
+  float plb[kDPairs];
+  float T[kMaxLinks][12];
+  float delta[kMaxLinks];
+  float F[kMaxLinks][3], M[kMaxLinks][3];
+  double q64[kMaxLinks];
+  const float* item_qa;
+  const float* item_qb;
+  int item_k, item_n;
+  // running exact best of the current pair (FP64 finalisation)
+  double b2;
+  int bA, bB;
+  double bcp[3], bcq[3];
+};
+
+struct DistArgs {
+  int mode;            // 0 min distance, 1 soft-min pass 1 (minimum), 2 soft-min pass 2
+  int robot;
+  const float* q;      // [B, L]
+  int B;
+  double cutoff;
+  double* d;           // [B]
+  int* pair;           // [B*2]
+  double* cp;          // [B*6]
+  float* grad;         // [B*L] (mode 0: dd/dq, mode 2: unnormalised soft-min gradient)
+  const double* m_traj;  // mode 2: [T] trajectory minima
+  double* wsum;        // mode 2: [B] per-waypoint sums
+  int W;               // waypoints per trajectory
+  double tau;
+  unsigned int* head;
+  uint2* scratch;
+  int scratch_per_warp;
+};
+
+struct DCnt {
+  unsigned long long pairs = 0, tri = 0, band = 0;
+};
+
+__device__ __forceinline__ float box_dist32(const Box32& A, float3 c, float3 h)
 {
-  return cudaErrorNotSupported;
+  float gx = fmaxf(0.f, fabsf(A.c.x - c.x) - A.h.x - h.x);
+  float gy = fmaxf(0.f, fabsf(A.c.y - c.y) - A.h.y - h.y);
+  float gz = fmaxf(0.f, fabsf(A.c.z - c.z) - A.h.z - h.z);
+  return sqrtf(gx * gx + gy * gy + gz * gz);
 }
 
-cudaError_t launch_softmin(const KWorldDev&, const Scratch&, int, const float*, int, int, double, double*,
-                           float*, int, int, cudaStream_t)
+__device__ __forceinline__ float warp_min(float v)
 {
-  return cudaErrorNotSupported;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// ---- FP32 triangle distance (value only; features come from FP64) --------
+__device__ __forceinline__ float clamp01f(float x) { return fminf(1.f, fmaxf(0.f, x)); }
+
+__device__ float seg_seg2_32(float3 p1, float3 d1, float3 p2, float3 d2)
+{
+  const float3 r = sub3(p1, p2);
+  const float a = dot3(d1, d1), e = dot3(d2, d2), f = dot3(d2, r);
+  float s, t;
+  if (a <= 1e-30f && e <= 1e-30f) {
+    s = 0.f; t = 0.f;
+  } else if (a <= 1e-30f) {
+    s = 0.f; t = clamp01f(f / e);
+  } else {
+    const float c = dot3(d1, r);
+    if (e <= 1e-30f) {
+      t = 0.f; s = clamp01f(-c / a);
+    } else {
+      const float b = dot3(d1, d2);
+      const float den = a * e - b * b;
+      s = den > 0.f ? clamp01f((b * f - c * e) / den) : 0.f;
+      t = (b * s + f) / e;
+      if (t < 0.f) { t = 0.f; s = clamp01f(-c / a); }
+      else if (t > 1.f) { t = 1.f; s = clamp01f((b - c) / a); }
+    }
+  }
+  const float3 w = make_float3(r.x + d1.x * s - d2.x * t, r.y + d1.y * s - d2.y * t, r.z + d1.z * s - d2.z * t);
+  return dot3(w, w);
+}
+
+__device__ float pt_tri2_32(float3 p, float3 a, float3 b, float3 c)
+{
+  const float3 ab = sub3(b, a), ac = sub3(c, a), ap = sub3(p, a);
+  const float d1 = dot3(ab, ap), d2 = dot3(ac, ap);
+  float3 q;
+  if (d1 <= 0.f && d2 <= 0.f) { q = a; goto done; }
+  {
+    const float3 bp = sub3(p, b);
+    const float d3 = dot3(ab, bp), d4 = dot3(ac, bp);
+    if (d3 >= 0.f && d4 <= d3) { q = b; goto done; }
+    const float vc = d1 * d4 - d3 * d2;
+    if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
+      const float v = d1 / (d1 - d3);
+      q = make_float3(a.x + ab.x * v, a.y + ab.y * v, a.z + ab.z * v);
+      goto done;
+    }
+    const float3 cp = sub3(p, c);
+    const float d5 = dot3(ab, cp), d6 = dot3(ac, cp);
+    if (d6 >= 0.f && d5 <= d6) { q = c; goto done; }
+    const float vb = d5 * d2 - d1 * d6;
+    if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
+      const float w = d2 / (d2 - d6);
+      q = make_float3(a.x + ac.x * w, a.y + ac.y * w, a.z + ac.z * w);
+      goto done;
+    }
+    const float va = d3 * d6 - d5 * d4;
+    if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
+      const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+      q = make_float3(b.x + (c.x - b.x) * w, b.y + (c.y - b.y) * w, b.z + (c.z - b.z) * w);
+      goto done;
+    }
+    const float den = 1.f / (va + vb + vc);
+    const float v = vb * den, w = vc * den;
+    q = make_float3(a.x + ab.x * v + ac.x * w, a.y + ab.y * v + ac.y * w, a.z + ab.z * v + ac.z * w);
+  }
+done:
+  const float3 dd = sub3(p, q);
+  return dot3(dd, dd);
+}
+
+// squared distance of two separated triangles: 9 edge-edge + 6 vertex-face
+__device__ float tri_dist2_32(const float3* P, const float3* Q)
+{
+  float best = FLT_MAX;
+#pragma unroll 1
+  for (int k = 0; k < 9; ++k) {
+    const int i = k / 3, j = k % 3;
+    const float3 pa = sel3(i, P[0], P[1], P[2]), pb = sel3(i == 2 ? 0 : i + 1, P[0], P[1], P[2]);
+    const float3 qa = sel3(j, Q[0], Q[1], Q[2]), qb = sel3(j == 2 ? 0 : j + 1, Q[0], Q[1], Q[2]);
+    best = fminf(best, seg_seg2_32(pa, sub3(pb, pa), qa, sub3(qb, qa)));
+  }
+#pragma unroll 1
+  for (int k = 0; k < 3; ++k) {
+    best = fminf(best, pt_tri2_32(sel3(k, P[0], P[1], P[2]), Q[0], Q[1], Q[2]));
+    best = fminf(best, pt_tri2_32(sel3(k, Q[0], Q[1], Q[2]), P[0], P[1], P[2]));
+  }
+  return best;
+}
+
+// lexicographic (d2, a, b) minimum across the warp; result in every lane
+__device__ __forceinline__ void warp_lexmin(double& d2, int& a, int& b, int& src, int lane)
+{
+  src = lane;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double od = __shfl_xor_sync(0xffffffffu, d2, o);
+    const int oa = __shfl_xor_sync(0xffffffffu, a, o);
+    const int ob = __shfl_xor_sync(0xffffffffu, b, o);
+    const int os = __shfl_xor_sync(0xffffffffu, src, o);
+    const bool take = od < d2 || (od == d2 && (oa < a || (oa == a && (ob < b || (ob == b && os < src)))));
+    if (take) { d2 = od; a = oa; b = ob; src = os; }
+  }
+}
+
+__device__ __forceinline__ double item_q64(const DistSmem& S, int lane)
+{
+  if (S.item_qb == nullptr) return (double)S.item_qa[lane];
+  return kx_interp((double)S.item_qa[lane], (double)S.item_qb[lane], S.item_k, S.item_n);
+}
+
+__device__ __noinline__ void dist_fk64(DistSmem& S, const KRobotDev& R, double (*T64)[12], int lane, int& fk64)
+{
+  if (fk64) return;
+  if (lane < R.nlinks) S.q64[lane] = item_q64(S, lane);
+  __syncwarp();
+  warp_fk64(R, S.q64, T64, lane);
+  fk64 = 1;
+}
+
+// FP64 finalisation of the pending candidates of pair (l, o): exact squared
+// distances, merged into the running lexicographic best (S.b2, S.bA, S.bB).
+__device__ __noinline__ void flush_cands(DistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                         double (*T64)[12], int& fk64, int lane, int l, int ncand, DCnt& cnt)
+{
+  dist_fk64(S, R, T64, lane, fk64);
+  for (int base = 0; base < ncand; base += 32) {
+    const int k = base + lane;
+    double d2 = DBL_MAX;
+    int oa = INT_MAX, ob = INT_MAX;
+    double cp[3] = {0, 0, 0}, cq[3] = {0, 0, 0};
+    if (k < ncand) {
+      const int tA = (int)S.candA[k], tB = (int)S.candB[k];
+      double P[9], Q[9];
+      const double* pa = W->ltri64 + 9 * (size_t)tA;
+      for (int v = 0; v < 3; ++v) kx_xform_point(T64[l], pa + 3 * v, P + 3 * v);
+      const double* pb = W->etri64 + 9 * (size_t)tB;
+      for (int i = 0; i < 9; ++i) Q[i] = pb[i];
+      d2 = kx_tri_tri_dist2(P, Q, cp, cq);
+      oa = W->ltri_orig[tA];
+      ob = W->etri_orig[tB];
+      cnt.band++;
+    }
+    int src;
+    double m2 = d2;
+    int ma = oa, mb = ob;
+    warp_lexmin(m2, ma, mb, src, lane);
+    const bool better = m2 < S.b2 || (m2 == S.b2 && (ma < S.bA || (ma == S.bA && mb < S.bB)));
+    __syncwarp();
+    if (better && lane == src) {
+      S.b2 = d2;
+      S.bA = oa;
+      S.bB = ob;
+      for (int i = 0; i < 3; ++i) { S.bcp[i] = cp[i]; S.bcq[i] = cq[i]; }
+    }
+    __syncwarp();
+  }
+}
+
+struct PairOut {
+  int found;
+  double d;
+  double cp[3], cq[3];
+  float dir[3];
+};
+
+// Signed distance of (link l, object o) below `bound` (found = d < bound).
+__device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                       double (*T64)[12], int& fk64, int lane, int l, int o, double bound,
+                                       PairOut& out, DCnt& cnt)
+{
+  cnt.pairs++;
+  const unsigned lt = lanemask_lt();
+  const float dl = S.delta[l] + W->eps_extra;
+  const float de = W->eps_env + W->eps_extra;
+  const float fb = bound > 0.0 ? (bound < 1e30 ? (float)bound * 1.000001f + 1e-7f : FLT_MAX) : 0.f;
+  float m32 = FLT_MAX;  // running FP32 minimum (warp-uniform)
+  bool overlap = false;
+  int top = 0, njobs = 0, ncand = 0;
+  int certA = -1, certB = -1;
+  if (lane == 0) {
+    S.b2 = DBL_MAX;
+    S.bA = INT_MAX;
+    S.bB = INT_MAX;
+    S.stack[0] = make_uint2((uint32_t)W->obj_root[o], (uint32_t)R.link_root[l]);
+  }
+  __syncwarp();
+  top = 1;
+  const float* TA = S.T[l];
+#pragma unroll 1
+  while (top > 0 || njobs > 0) {
+    if (njobs > kDJobs - 32 || (top == 0 && njobs > 0)) {
+      // ---- triangle pairs, one per lane
+      uint32_t carry = 0;
+      for (int b = 0; b < njobs; b += 32) {
+        const int j = b + lane;
+        uint32_t c = 0;
+        if (j < njobs) c = ((S.jobA[j] >> 28) + 1) * ((S.jobB[j] >> 28) + 1);
+        uint32_t incl = c;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+          const uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
+          if (lane >= off) incl += v;
+        }
+        if (j < njobs) S.jobOff[j] = carry + incl - c;
+        carry += __shfl_sync(0xffffffffu, incl, 31);
+      }
+      __syncwarp();
+      const uint32_t total = carry;
+#pragma unroll 1
+      for (uint32_t base = 0; base < total && !overlap; base += 32) {
+        const uint32_t p = base + lane;
+        float d32 = FLT_MAX, e = 0.f;
+        bool certain = false;
+        int tA = 0, tB = 0;
+        if (p < total) {
+          int lo = 0, hi = njobs - 1;
+          while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (S.jobOff[mid] <= p) lo = mid; else hi = mid - 1;
+          }
+          const uint32_t r = p - S.jobOff[lo];
+          const uint32_t cb = (S.jobB[lo] >> 28) + 1;
+          tA = (int)(S.jobA[lo] & 0x0fffffffu) + (int)(r / cb);
+          tB = (int)(S.jobB[lo] & 0x0fffffffu) + (int)(r % cb);
+          float3 P[3], Q[3];
+#pragma unroll
+          for (int v = 0; v < 3; ++v) {
+            const float4 x = __ldg(W->ltri32 + 3 * (size_t)tA + v);
+            P[v] = xform32(TA, make_float3(x.x, x.y, x.z));
+            const float4 y = __ldg(W->etri32 + 3 * (size_t)tB + v);
+            Q[v] = make_float3(y.x, y.y, y.z);
+          }
+          float3 lo3 = P[0], hi3 = P[0];
+#pragma unroll
+          for (int k = 1; k < 6; ++k) {
+            const float3 v = k < 3 ? P[k] : Q[k - 3];
+            lo3 = make_float3(fminf(lo3.x, v.x), fminf(lo3.y, v.y), fminf(lo3.z, v.z));
+            hi3 = make_float3(fmaxf(hi3.x, v.x), fmaxf(hi3.y, v.y), fmaxf(hi3.z, v.z));
+          }
+          const float span = fmaxf(fmaxf(hi3.x - lo3.x, hi3.y - lo3.y), hi3.z - lo3.z);
+          e = dl + de + 128.f * kU * span + 1e-8f;
+          if (!tri_separated32(P, Q, dl + de, 0.f)) {
+            d32 = 0.f;
+            certain = tri_certain_hit32(P[0], P[1], P[2], Q[0], Q[1], Q[2], fmaxf(dl, de));
+          } else {
+            d32 = sqrtf(tri_dist2_32(P, Q));
+          }
+          cnt.tri++;
+        }
+        const unsigned mc = __ballot_sync(0xffffffffu, certain);
+        if (mc) {
+          overlap = true;
+          const int src = __ffs(mc) - 1;
+          certA = __shfl_sync(0xffffffffu, tA, src);
+          certB = __shfl_sync(0xffffffffu, tB, src);
+          break;
+        }
+        m32 = fminf(m32, warp_min(d32));
+        const float emax = warp_min(-e) * -1.f;  // largest band in this batch
+        const float lim = fminf(m32 * (1.f + 2e-5f) + 2.f * emax, fb + emax);
+        const bool cand = p < total && d32 - e <= lim;
+        const unsigned mcand = __ballot_sync(0xffffffffu, cand);
+        if (ncand + __popc(mcand) > kDCand) {
+          flush_cands(S, W, R, T64, fk64, lane, l, ncand, cnt);
+          ncand = 0;
+          if (S.b2 < DBL_MAX) m32 = fminf(m32, (float)sqrt(S.b2) * (1.f + 1e-6f));
+        }
+        if (cand) {
+          const int r = ncand + __popc(mcand & lt);
+          S.candA[r] = (uint32_t)tA;
+          S.candB[r] = (uint32_t)tB;
+          S.candD[r] = d32 - e;
+        }
+        ncand += __popc(mcand);
+        __syncwarp();
+      }
+      njobs = 0;
+      if (overlap) break;
+      continue;
+    }
+    // ---- node pairs
+    const int n = min(top, 32);
+    const bool have = lane < n;
+    uint2 en = make_uint2(0, 0);
+    if (have) en = S.stack[top - 1 - lane];
+    __syncwarp();
+    top -= n;
+    int outcome = 0;
+    uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
+    uint32_t jA = 0, jB = 0;
+    if (have) {
+      const int nodeB = (int)en.x, nodeA = (int)en.y;
+      const KNode na = W->lnodes[nodeA];
+      const KNode nb = W->enodes[nodeB];
+      const Box32 A = xform_box(TA, na.a, na.b);
+      const float lb = box_dist32(A, make_float3(nb.a.x, nb.a.y, nb.a.z), make_float3(nb.b.x, nb.b.y, nb.b.z)) -
+                       (dl + de) * 1.7321f - 4.f * kU * (fabsf(A.c.x) + fabsf(A.c.y) + fabsf(A.c.z) + 1.f);
+      const float lim = fminf(m32 * (1.f + 2e-5f) + 3.f * (dl + de) + 1e-5f, fb + 2.f * (dl + de) + 1e-5f);
+      if (lb <= lim) {
+        const int cntA = f2i(na.b.w), cntB = f2i(nb.b.w);
+        const int ia = f2i(na.a.w), ib = f2i(nb.a.w);
+        if (cntA > 0 && cntB > 0) {
+          outcome = 2;
+          jA = (uint32_t)ia | ((uint32_t)(cntA - 1) << 28);
+          jB = (uint32_t)ib | ((uint32_t)(cntB - 1) << 28);
+        } else {
+          outcome = 1;
+          const bool splitB = cntA > 0 || (cntB == 0 && (nb.b.x + nb.b.y + nb.b.z) > (na.b.x + na.b.y + na.b.z));
+          if (splitB) { c0 = make_uint2((uint32_t)ib, (uint32_t)nodeA); c1 = make_uint2((uint32_t)ib + 1, (uint32_t)nodeA); }
+          else { c0 = make_uint2((uint32_t)nodeB, (uint32_t)ia); c1 = make_uint2((uint32_t)nodeB, (uint32_t)ia + 1); }
+        }
+      }
+    }
+    const unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
+    const unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
+    if (top + 2 * __popc(m1) > kDStack) {
+      // stack would overflow: the pair is evaluated conservatively by giving up
+      // pruning precision is not an option, so flag and stop
+      if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
+      out.found = 0;
+      return;
+    }
+    if (outcome == 1) {
+      const int r = top + 2 * __popc(m1 & lt);
+      S.stack[r] = c1;
+      S.stack[r + 1] = c0;
+    } else if (outcome == 2) {
+      const int r = njobs + __popc(m2 & lt);
+      S.jobA[r] = jA;
+      S.jobB[r] = jB;
+    }
+    top += 2 * __popc(m1);
+    njobs += __popc(m2);
+    __syncwarp();
+  }
+
+  // ---- unsigned distance: exact zero (certified contact) or FP64 finalisation
+  bool zero = overlap;
+  if (!overlap) {
+    // drop stale candidates, then finalise
+    const float lim = fminf(m32 * (1.f + 2e-5f), fb);
+    int keep = 0;
+    for (int base = 0; base < ncand; base += 32) {
+      const int k = base + lane;
+      bool ok = false;
+      uint32_t a = 0, b = 0;
+      float dd = 0.f;
+      if (k < ncand) {
+        a = S.candA[k]; b = S.candB[k]; dd = S.candD[k];
+        ok = dd <= lim + 1e-6f;
+      }
+      __syncwarp();
+      const unsigned mk = __ballot_sync(0xffffffffu, ok);
+      if (ok) {
+        const int r = keep + __popc(mk & lt);
+        S.candA[r] = a; S.candB[r] = b; S.candD[r] = dd;
+      }
+      keep += __popc(mk);
+      __syncwarp();
+    }
+    if (keep > 0) flush_cands(S, W, R, T64, fk64, lane, l, keep, cnt);
+    if (S.b2 == DBL_MAX) { out.found = 0; return; }
+    zero = S.b2 == 0.0;
+  }
+  if (!zero) {
+    const double d = kx_sqrt(S.b2);
+    out.found = d < bound;
+    out.d = d;
+    for (int i = 0; i < 3; ++i) {
+      out.cp[i] = S.bcp[i];
+      out.cq[i] = S.bcq[i];
+      out.dir[i] = (float)((S.bcp[i] - S.bcq[i]) / d);
+    }
+    return;
+  }
+  // ---- surfaces meet
+  int vbest = -1, fbest = -1;
+  double depth = 0.0;
+  if (W->obj_convex[o]) {
+    // deepest link vertex inside the convex object
+    const int vf = R.link_vert_first[l], vc = R.link_vert_count[l];
+    const KNode ob = W->enodes[W->obj_root[o]];
+    const float tolb = dl + de + 8.f * kU * (fabsf(ob.a.x) + fabsf(ob.a.y) + fabsf(ob.a.z) + 1.f);
+    const int ff = W->obj_leaf_first[o], fc = W->obj_leaf_count[o];
+    const float ed = dl + de + 32.f * kU * (fabsf(ob.a.x) + fabsf(ob.a.y) + fabsf(ob.a.z) + fabsf(ob.b.x) +
+                                           fabsf(ob.b.y) + fabsf(ob.b.z) + 1.f);
+    float lmax = -FLT_MAX;
+    // pass 1: FP32 depths, lane-local maximum
+    for (int v = lane; v < vc; v += 32) {
+      const float4 x = __ldg(W->lvert32 + vf + v);
+      const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
+      if (fabsf(w.x - ob.a.x) > ob.b.x + tolb || fabsf(w.y - ob.a.y) > ob.b.y + tolb ||
+          fabsf(w.z - ob.a.z) > ob.b.z + tolb)
+        continue;
+      float dmin = FLT_MAX;
+      for (int f = ff; f < ff + fc; ++f) {
+        const float4 pl = __ldg(W->eface32 + f);
+        dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
+      }
+      lmax = fmaxf(lmax, dmin);
+    }
+    const float gmax = -warp_min(-lmax);
+    if (gmax > -ed) {
+      dist_fk64(S, R, T64, lane, fk64);
+      // pass 2: FP64 depth of every vertex within the band of the deepest
+      double bd = 0.0;
+      int bv = INT_MAX, bf = -1;
+      for (int v = lane; v < vc; v += 32) {
+        const float4 x = __ldg(W->lvert32 + vf + v);
+        const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
+        if (fabsf(w.x - ob.a.x) > ob.b.x + tolb || fabsf(w.y - ob.a.y) > ob.b.y + tolb ||
+            fabsf(w.z - ob.a.z) > ob.b.z + tolb)
+          continue;
+        float dmin = FLT_MAX;
+        for (int f = ff; f < ff + fc; ++f) {
+          const float4 pl = __ldg(W->eface32 + f);
+          dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
+        }
+        if (dmin < gmax - 2.f * ed || dmin <= -ed) continue;
+        double w64[3];
+        kx_xform_point(T64[l], W->lvert64 + 3 * (size_t)(vf + v), w64);
+        double dm = DBL_MAX;
+        int fm = -1, fo = INT_MAX;
+        for (int f = ff; f < ff + fc; ++f) {
+          const double* pl = W->eface64 + 4 * (size_t)f;
+          const double dep = kx_sub(pl[3], kx_dot3(pl, w64));
+          const int orig = W->etri_orig[f];
+          if (dep < dm || (dep == dm && orig < fo)) { dm = dep; fm = f; fo = orig; }
+        }
+        if (dm > bd || (dm == bd && dm > 0.0 && v < bv)) { bd = dm; bv = v; bf = fm; }
+      }
+      // warp maximum of (depth, -vertex)
+      double wd = bd;
+      int wv = bd > 0.0 ? bv : INT_MAX, wf = bf, src = lane;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const double od = __shfl_xor_sync(0xffffffffu, wd, off);
+        const int ov = __shfl_xor_sync(0xffffffffu, wv, off);
+        const int ofc = __shfl_xor_sync(0xffffffffu, wf, off);
+        const int os = __shfl_xor_sync(0xffffffffu, src, off);
+        if (od > wd || (od == wd && (ov < wv || (ov == wv && os < src)))) { wd = od; wv = ov; wf = ofc; src = os; }
+      }
+      if (wd > 0.0) {
+        depth = wd;
+        vbest = wv;
+        fbest = wf;
+      }
+    }
+  }
+  if (vbest >= 0) {
+    double w64[3];
+    kx_xform_point(T64[l], W->lvert64 + 3 * (size_t)(R.link_vert_first[l] + vbest), w64);
+    const double* pl = W->eface64 + 4 * (size_t)fbest;
+    out.d = -depth;
+    out.found = -depth < bound;
+    for (int i = 0; i < 3; ++i) {
+      out.cp[i] = w64[i];
+      out.cq[i] = kx_add(w64[i], kx_mul(depth, pl[i]));
+      out.dir[i] = (float)pl[i];
+    }
+    return;
+  }
+  // contact without a vertex inside (or a non-convex object): d = 0, no direction
+  out.d = 0.0;
+  out.found = 0.0 < bound;
+  float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (certA >= 0) x = __ldg(W->ltri32 + 3 * (size_t)certA);
+  const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
+  out.cp[0] = out.cq[0] = w.x;
+  out.cp[1] = out.cq[1] = w.y;
+  out.cp[2] = out.cq[2] = w.z;
+  out.dir[0] = out.dir[1] = out.dir[2] = 0.f;
+}
+
+// Gathers objects of group g whose root box is within `bound` of link l's
+// world box (lower bound lb in plb) and lb > lower (already handled), into
+// S.pobj/plb starting at `count`; stops early when the list is full (the
+// caller then evaluates and calls again with `resume` state in the stack).
+// Returns the new count; `top` carries the traversal stack between calls.
+__device__ int gather_objects(DistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R, int lane, int l,
+                              float bound, float lower, int count, int& top)
+{
+  const unsigned lt = lanemask_lt();
+  const KNode la = W->lnodes[R.link_root[l]];
+  const Box32 A = xform_box(S.T[l], la.a, la.b);
+  const float slack = (S.delta[l] + W->eps_env + 2.f * W->eps_extra) * 1.7321f +
+                      4.f * kU * (fabsf(A.c.x) + fabsf(A.c.y) + fabsf(A.c.z) + 1.f) + 1e-7f;
+  while (top > 0 && count <= kDPairs - 32) {
+    if (top > kDGStack - 64) {
+      if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
+      top = 0;
+      break;
+    }
+    const int n = min(top, 32);
+    const bool have = lane < n;
+    int node = 0;
+    if (have) node = (int)S.gstack[top - 1 - lane];
+    __syncwarp();
+    top -= n;
+    int outcome = 0;
+    float lbv = 0.f;
+    int child = 0;
+    if (have) {
+      const KNode nb = W->enodes[node];
+      lbv = box_dist32(A, make_float3(nb.a.x, nb.a.y, nb.a.z), make_float3(nb.b.x, nb.b.y, nb.b.z)) - slack;
+      if (lbv <= bound) {
+        const int o = W->node_obj[node];
+        if (o >= 0) {
+          outcome = lbv > lower ? 2 : 0;
+          child = o;
+        } else {
+          outcome = 1;
+          child = f2i(nb.a.w);
+        }
+      }
+    }
+    const unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
+    const unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
+    if (outcome == 1) {
+      const int r = top + 2 * __popc(m1 & lt);
+      S.gstack[r] = (uint32_t)child + 1;
+      S.gstack[r + 1] = (uint32_t)child;
+    } else if (outcome == 2) {
+      const int r = count + __popc(m2 & lt);
+      S.pobj[r] = child;
+      S.plb[r] = lbv;
+    }
+    top += 2 * __popc(m1);
+    count += __popc(m2);
+    __syncwarp();
+  }
+  return count;
+}
+
+// Adds a pair's contribution (weight wgt, feature point p, direction u) to
+// the per-link force / moment accumulators.
+__device__ __forceinline__ void add_wrench(DistSmem& S, int lane, int l, float wgt, const PairOut& po)
+{
+  if (lane == 0) {
+    const float ux = wgt * po.dir[0], uy = wgt * po.dir[1], uz = wgt * po.dir[2];
+    const float px = (float)po.cp[0], py = (float)po.cp[1], pz = (float)po.cp[2];
+    S.F[l][0] += ux; S.F[l][1] += uy; S.F[l][2] += uz;
+    S.M[l][0] += py * uz - pz * uy;
+    S.M[l][1] += pz * ux - px * uz;
+    S.M[l][2] += px * uy - py * ux;
+  }
+  __syncwarp();
+}
+
+// Adjoint of FK: gradient g_j = w_j . (M_sub(j) - o_j x F_sub(j)) for a
+// revolute joint, w_j . F_sub(j) for a prismatic one, with F_sub/M_sub the
+// sums over link j's subtree (children have larger indices than parents).
+__device__ void pullback(DistSmem& S, const KRobotDev& R, int lane, float* g_out)
+{
+  const int nl = R.nlinks;
+  if (lane == 0) {
+    for (int i = nl - 1; i > 0; --i) {
+      const int p = R.parents[i];
+      if (p < 0) continue;
+      for (int k = 0; k < 3; ++k) {
+        S.F[p][k] += S.F[i][k];
+        S.M[p][k] += S.M[i][k];
+      }
+    }
+  }
+  __syncwarp();
+  if (lane < nl && g_out) {
+    const float* T = S.T[lane];
+    const float wx = T[0] * R.axis[lane][0] + T[1] * R.axis[lane][1] + T[2] * R.axis[lane][2];
+    const float wy = T[3] * R.axis[lane][0] + T[4] * R.axis[lane][1] + T[5] * R.axis[lane][2];
+    const float wz = T[6] * R.axis[lane][0] + T[7] * R.axis[lane][1] + T[8] * R.axis[lane][2];
+    float g = 0.f;
+    if (R.jtype[lane] == KX_JOINT_REVOLUTE) {
+      const float ox = T[9], oy = T[10], oz = T[11];
+      const float* F = S.F[lane];
+      const float* M = S.M[lane];
+      const float tx = M[0] - (oy * F[2] - oz * F[1]);
+      const float ty = M[1] - (oz * F[0] - ox * F[2]);
+      const float tz = M[2] - (ox * F[1] - oy * F[0]);
+      g = wx * tx + wy * ty + wz * tz;
+    } else if (R.jtype[lane] == KX_JOINT_PRISMATIC) {
+      g = wx * S.F[lane][0] + wy * S.F[lane][1] + wz * S.F[lane][2];
+    }
+    g_out[lane] = g;
+  }
+  __syncwarp();
+}
+
+__global__ void __launch_bounds__(kDW * 32, 2) k_dist(const KWorldDev* __restrict__ W, const DistArgs A)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  DistSmem* all = reinterpret_cast<DistSmem*>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  DistSmem& S = all[warp];
+  const int gwarp = blockIdx.x * kDW + warp;
+  double(*T64)[12] = reinterpret_cast<double(*)[12]>(A.scratch + (size_t)gwarp * A.scratch_per_warp);
+  const KRobotDev& R = W->robots[A.robot];
+  const int nl = R.nlinks;
+  DCnt cnt;
+
+  for (;;) {
+    unsigned int it = 0;
+    if (lane == 0) it = atomicAdd(A.head, 1u);
+    it = __shfl_sync(0xffffffffu, it, 0);
+    if (it >= (unsigned)A.B) break;
+    const int b = (int)it;
+    if (lane == 0) {
+      S.item_qa = A.q + (size_t)b * nl;
+      S.item_qb = nullptr;
+      S.item_k = 0;
+      S.item_n = 0;
+    }
+    float q = lane < nl ? __ldg(A.q + (size_t)b * nl + lane) : 0.f;
+    __syncwarp();
+    if (__any_sync(0xffffffffu, lane < nl && !(fabsf(q) < 1.0e6f))) {
+      if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
+      continue;
+    }
+    float P[12], delta;
+    warp_fk32(R, lane, q, 0.f, P, &delta);
+    if (lane < nl) {
+      for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
+      S.delta[lane] = delta;
+      S.F[lane][0] = S.F[lane][1] = S.F[lane][2] = 0.f;
+      S.M[lane][0] = S.M[lane][1] = S.M[lane][2] = 0.f;
+    }
+    __syncwarp();
+    int fk64 = 0;
+
+    if (A.mode == 0 || A.mode == 1) {
+      // ---- minimum over pairs, iterative deepening of the search bound
+      double best = A.cutoff;
+      int bl = -1, bo = -1;
+      PairOut bp;
+      bp.found = 0;
+      // rounds: objects whose box lower bound lies in (lower, bound]; done
+      // once the best distance is <= bound (every unvisited object is
+      // farther) or the bound reached the cutoff
+      float lower = -1.f;
+      double round_bound = fmin(A.cutoff, 0.05);
+      for (;;) {
+        const float bound = round_bound >= A.cutoff ? FLT_MAX : (float)round_bound * 1.000001f;
+        for (int l = 0; l < nl; ++l) {
+          if (R.link_root[l] < 0) continue;
+          for (int g = 0; g < kMaxGroups; ++g) {
+            if (!((R.env_mask[l] >> g) & 1u) || W->group_root[g] < 0) continue;
+            int top = 1;
+            if (lane == 0) S.gstack[0] = (uint32_t)W->group_root[g];
+            __syncwarp();
+            while (top > 0) {
+              // box bounds limit the unsigned distance: a pair can be
+              // negative only when its boxes meet, hence max(best, 0)
+              const float reach = (float)fmax(best, 0.0) * 1.00001f + 1e-6f;
+              const int np = gather_objects(S, W, R, lane, l, fminf(bound, reach), lower,
+                                            0, top);
+              // evaluate nearest first
+              for (int done = 0; done < np; ++done) {
+                float v = FLT_MAX;
+                int idx = -1;
+                for (int k = lane; k < np; k += 32)
+                  if (S.plb[k] < v) { v = S.plb[k]; idx = k; }
+                const float vm = warp_min(v);
+                const unsigned mm = __ballot_sync(0xffffffffu, v == vm && idx >= 0);
+                const int owner = __ffs(mm) - 1;
+                const int k = __shfl_sync(0xffffffffu, idx, owner);
+                if (lane == 0) S.plb[k] = FLT_MAX;
+                __syncwarp();
+                if (vm > (float)fmax(best, 0.0) * 1.00001f + 1e-6f) break;
+                const int o = S.pobj[k];
+                PairOut po;
+                eval_pair(S, W, R, T64, fk64, lane, l, o, nextafter(best, 1e300), po, cnt);
+                if (po.found && (po.d < best || (po.d == best && (l < bl || (l == bl && o < bo))))) {
+                  best = po.d;
+                  bl = l;
+                  bo = o;
+                  bp = po;
+                }
+              }
+            }
+          }
+        }
+        if (best <= round_bound || round_bound >= A.cutoff) break;
+        lower = bound;
+        round_bound = fmin(A.cutoff, round_bound * 4.0);
+      }
+      if (lane == 0) {
+        A.d[b] = bl >= 0 ? best : A.cutoff;
+        if (A.mode == 0) {
+          A.pair[2 * b] = bl;
+          A.pair[2 * b + 1] = bo;
+          for (int i = 0; i < 3; ++i) {
+            A.cp[6 * b + i] = bl >= 0 ? bp.cp[i] : 0.0;
+            A.cp[6 * b + 3 + i] = bl >= 0 ? bp.cq[i] : 0.0;
+          }
+        }
+      }
+      if (A.mode == 0 && A.grad) {
+        if (bl >= 0) add_wrench(S, lane, bl, 1.f, bp);
+        pullback(S, R, lane, A.grad + (size_t)b * nl);
+      }
+    } else {
+      // ---- soft-min pass 2: every pair below m + K tau
+      const int t = b / A.W;
+      const double m = A.m_traj[t];
+      const double bnd = m + kSoftK * A.tau;
+      double sum = 0.0;
+      const float fbnd = (float)fmax(bnd, 0.0) * 1.000001f + 1e-6f;
+      for (int l = 0; l < nl; ++l) {
+        if (R.link_root[l] < 0) continue;
+        for (int g = 0; g < kMaxGroups; ++g) {
+          if (!((R.env_mask[l] >> g) & 1u) || W->group_root[g] < 0) continue;
+          int top = 1;
+          if (lane == 0) S.gstack[0] = (uint32_t)W->group_root[g];
+          __syncwarp();
+          while (top > 0) {
+            const int np = gather_objects(S, W, R, lane, l, fbnd, -1.f, 0, top);
+            for (int k = 0; k < np; ++k) {
+              PairOut po;
+              eval_pair(S, W, R, T64, fk64, lane, l, S.pobj[k], bnd, po, cnt);
+              if (!po.found) continue;
+              const double e = exp(-(po.d - m) / A.tau);
+              sum += e;
+              add_wrench(S, lane, l, (float)e, po);
+            }
+          }
+        }
+      }
+      if (lane == 0) A.wsum[b] = sum;
+      pullback(S, R, lane, A.grad ? A.grad + (size_t)b * nl : nullptr);
+    }
+  }
+  (void)cnt;
+}
+
+// per-trajectory minimum of the waypoint minima
+__global__ void k_traj_min(const double* dwp, int T, int Wn, double* m)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  double v = dwp[(size_t)t * Wn];
+  for (int w = 1; w < Wn; ++w) v = fmin(v, dwp[(size_t)t * Wn + w]);
+  m[t] = v;
+}
+
+// L = m - tau log(sum), gradient normalised by the sum (waypoints in order)
+__global__ void k_softmin_final(const double* wsum, const double* m, int T, int Wn, int L, double tau,
+                                double* out, float* grad)
+{
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= T) return;
+  double s = 0.0;
+  for (int w = 0; w < Wn; ++w) s += wsum[(size_t)t * Wn + w];
+  out[t] = m[t] - tau * log(s);
+  if (grad) {
+    const float inv = (float)(1.0 / s);
+    for (int k = 0; k < Wn * L; ++k) grad[(size_t)t * Wn * L + k] *= inv;
+  }
+}
+
+}  // namespace
+
+cudaError_t dist_init()
+{
+  return cudaFuncSetAttribute(k_dist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(DistSmem) * kDW));
+}
+
+cudaError_t launch_distance(const KWorldDev* Wd, const Scratch& S, int robot, const float* q, int B, double cutoff,
+                            double* d, int* pair, double* cp, float* grad, int num_sms, cudaStream_t s)
+{
+  if (B <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(S.counters + 1, 0, sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  DistArgs A = {};
+  A.mode = 0;
+  A.robot = robot;
+  A.q = q;
+  A.B = B;
+  A.cutoff = cutoff;
+  A.d = d;
+  A.pair = pair;
+  A.cp = cp;
+  A.grad = grad;
+  A.head = S.counters + 1;
+  A.scratch = S.spill;
+  A.scratch_per_warp = (int)S.spill_per_warp;
+  k_dist<<<num_sms * 2, kDW * 32, sizeof(DistSmem) * kDW, s>>>(Wd, A);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_softmin(const KWorldDev* Wd, const Scratch& S, int robot, const float* q, int T, int Wn,
+                           double tau, double* L, float* dLdq, int nl, double* work, int num_sms, cudaStream_t s)
+{
+  if (T <= 0) return cudaSuccess;
+  const int B = T * Wn;
+  double* dwp = work;            // [B]
+  double* mt = work + B;         // [T]
+  double* wsum = work + B + T;   // [B]
+  cudaError_t e = cudaMemsetAsync(S.counters + 1, 0, 2 * sizeof(unsigned int), s);
+  if (e != cudaSuccess) return e;
+  DistArgs A = {};
+  A.robot = robot;
+  A.q = q;
+  A.B = B;
+  A.scratch = S.spill;
+  A.scratch_per_warp = (int)S.spill_per_warp;
+  // pass 1: waypoint minima (no cutoff)
+  A.mode = 1;
+  A.cutoff = 1e3;
+  A.d = dwp;
+  A.head = S.counters + 1;
+  k_dist<<<num_sms * 2, kDW * 32, sizeof(DistSmem) * kDW, s>>>(Wd, A);
+  k_traj_min<<<(T + 127) / 128, 128, 0, s>>>(dwp, T, Wn, mt);
+  // pass 2: every pair below m + K tau, unnormalised gradients
+  A.mode = 2;
+  A.m_traj = mt;
+  A.wsum = wsum;
+  A.W = Wn;
+  A.tau = tau;
+  A.grad = dLdq;
+  A.head = S.counters + 2;
+  k_dist<<<num_sms * 2, kDW * 32, sizeof(DistSmem) * kDW, s>>>(Wd, A);
+  k_softmin_final<<<(T + 127) / 128, 128, 0, s>>>(wsum, mt, T, Wn, nl, tau, L, dLdq);
+  return cudaGetLastError();
 }
 
 }  // namespace kgpu

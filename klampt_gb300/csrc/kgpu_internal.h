@@ -127,6 +127,8 @@ struct Scratch {
   int* edge_perm = nullptr;
   int* edge_meta = nullptr;          // [0] max n, [1] total items
   size_t edge_cap = 0;
+  double* dist_work = nullptr;       // soft-min per-waypoint minima, sums, trajectory minima
+  size_t dist_work_cap = 0;
 };
 
 }  // namespace kgpu
@@ -239,10 +241,12 @@ cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q
 cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,
                                  const float* qb, const int* nsteps, int E, int* first_hit,
                                  cudaStream_t s);
-cudaError_t launch_distance(const KWorldDev& W, const Scratch& S, int robot, const float* q,
-                            int B, double cutoff, double* d, int* pair, double* cp, float* grad,
-                            int blocks, int warps_per_block, cudaStream_t s);
-cudaError_t launch_softmin(const KWorldDev& W, const Scratch& S, int robot, const float* q, int T,
-                           int Wn, double tau, double* L, float* dLdq, int blocks,
-                           int warps_per_block, cudaStream_t s);
+cudaError_t dist_init();
+cudaError_t launch_distance(const KWorldDev* Wd, const Scratch& S, int robot, const float* q, int B,
+                            double cutoff, double* d, int* pair, double* cp, float* grad, int num_sms,
+                            cudaStream_t s);
+// work: 2*T*Wn + T doubles of device scratch
+cudaError_t launch_softmin(const KWorldDev* Wd, const Scratch& S, int robot, const float* q, int T,
+                           int Wn, double tau, double* L, float* dLdq, int nl, double* work,
+                           int num_sms, cudaStream_t s);
 }  // namespace kgpu

@@ -395,9 +395,10 @@ PairResult pair_distance(Ctx& c, int l, int o, double bound)
   const Bvh& A = R.bvh[l];
   const Bvh& B = E.obj_bvh[o];
   if (A.empty() || B.empty()) return res;
-  // unsigned search bounded by max(bound, 0): intersecting pairs always found
+  // unsigned search bounded by max(bound, 0); with a non-positive bound only
+  // contact (squared distance exactly 0) matters
   double ub = bound > 0 ? bound : 0.0;
-  double best2 = ub * ub;
+  double best2 = ub * ub > 1e-300 ? ub * ub : 1e-300;  // (a tiny bound must not underflow to 0)
   int bta = -1, btb = -1;
   double bcp[3] = {0, 0, 0}, bcq[3] = {0, 0, 0};
   bool have = false;
@@ -558,7 +559,9 @@ MinResult min_distance(Ctx& c, double bound)
     if (c.R->bvh[l].empty()) continue;
     for (int o = 0; o < c.E->N; ++o) {
       if (!pair_enabled(c, l, o)) continue;
-      if (link_obj_lb(c, l, o) > m.d + 1e-9) continue;
+      // the box bound limits the unsigned distance; a pair can be negative
+      // only when its boxes meet (bound 0)
+      if (link_obj_lb(c, l, o) > std::max(m.d, 0.0) + 1e-9) continue;
       // ties must reach the comparison: search with a bound slightly above m.d
       PairResult pr = pair_distance(c, l, o, std::nextafter(m.d, 1e300));
       if (pr.found && pr.d < m.d) {
@@ -930,33 +933,33 @@ int orc_min_distance(void* robot, void* env, const unsigned* masks, const float*
 
 /* soft-min of the signed distance over all (waypoint, link, object) pairs of
  * each trajectory: L = m - tau*log(sum exp(-(d-m)/tau)), m the trajectory's
- * minimum, summing pairs with d < m + 30 tau; dL/dq by the chain rule through
- * each pair's feature point.  q [T*W*L]; Lout [T]; grad [T*W*L] or NULL. */
+ * minimum, summing pairs with d < m + 12 tau (a pair beyond contributes less
+ * than e^-12 of the leading term and is left out by definition); dL/dq by the
+ * chain rule through each pair's feature point.  q [T*W*L]; Lout [T]; grad
+ * [T*W*L] or NULL. */
 int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, int T, int W,
                 double tau, double* Lout, double* grad, int nthreads)
 {
   Robot* R = (Robot*)robot;
   Env* E = (Env*)env;
-  const double K = 30.0;
+  const double K = 12.0;
   parallel_for(T, nthreads, [&](int, int t0, int t1) {
     Ctx c;
     c.init(R, E, masks);
     double qd[ORC_MAXL];
     for (int t = t0; t < t1; ++t) {
-      // pass 1: the trajectory minimum
+      // pass 1: the trajectory minimum (distances searched up to 1000 m)
       double m = 1e300;
       for (int w = 0; w < W; ++w) {
         const float* qw = q + ((size_t)t * W + w) * R->L;
         for (int i = 0; i < R->L; ++i) qd[i] = (double)qw[i];
         c.set_config(qd);
-        MinResult r = min_distance(c, 1e300);
+        MinResult r = min_distance(c, 1e3);
         m = std::min(m, r.d);
       }
       double bound = m + K * tau;
       double sum = 0.0;
       std::vector<double> g(W * R->L, 0.0);
-      struct Term { int w, l; double wgt; double p[3], u[3]; };
-      std::vector<Term> terms;
       for (int w = 0; w < W; ++w) {
         const float* qw = q + ((size_t)t * W + w) * R->L;
         for (int i = 0; i < R->L; ++i) qd[i] = (double)qw[i];
@@ -965,20 +968,12 @@ int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, i
           if (R->bvh[l].empty()) continue;
           for (int o = 0; o < E->N; ++o) {
             if (!pair_enabled(c, l, o)) continue;
-            if (link_obj_lb(c, l, o) > bound + 1e-9) continue;
+            if (link_obj_lb(c, l, o) > std::max(bound, 0.0) + 1e-9) continue;
             PairResult pr = pair_distance(c, l, o, bound);
             if (!pr.found) continue;
             double e = exp(-(pr.d - m) / tau);
             sum += e;
-            if (grad) {
-              Term tm;
-              tm.w = w; tm.l = l; tm.wgt = e;
-              std::memcpy(tm.p, pr.cp, sizeof tm.p);
-              std::memcpy(tm.u, pr.dir, sizeof tm.u);
-              terms.push_back(tm);
-              double* gw = &g[(size_t)w * R->L];
-              feature_gradient(c, l, pr.cp, pr.dir, e, gw);
-            }
+            if (grad) feature_gradient(c, l, pr.cp, pr.dir, e, &g[(size_t)w * R->L]);
           }
         }
       }

@@ -1,0 +1,119 @@
+"""GPU parity of signed distance, its gradient and the trajectory soft-min
+against the FP64 oracle, plus central finite differences (h = 1e-5)."""
+
+import os
+
+import numpy as np
+import pytest
+
+from klampt_gb300 import scenes as sc
+
+pytestmark = pytest.mark.gpu
+
+NT = os.cpu_count() or 4
+GRAD_RTOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def built():
+    from klampt_gb300 import build
+    build.build()
+    from oracle import oracle_py
+    oracle_py.build()
+    return True
+
+
+@pytest.fixture(scope="module")
+def cfg2(built):
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robot, env, q = sc.scene_cfg2(T=16, W=8)
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    yield robot, env, q, w, o
+    w.close()
+
+
+def _grad_close(g, g_ref, rtol=GRAD_RTOL):
+    g = np.asarray(g, np.float64)
+    g_ref = np.asarray(g_ref, np.float64)
+    scale = max(np.abs(g_ref).max(), 1e-6)
+    return np.abs(g - g_ref).max() <= rtol * scale + 1e-7
+
+
+def test_min_distance_matches_oracle(cfg2):
+    robot, env, q, w, o = cfg2
+    qq = q.reshape(-1, robot.num_links)[:96]
+    d_o, p_o, cp_o, g_o = o.min_distance(qq, 1e3, nthreads=NT)
+    d, p, cp, g = w.distance(qq, 1e3)
+    d, p, cp, g = d.cpu().numpy(), p.cpu().numpy(), cp.cpu().numpy(), g.cpu().numpy()
+    assert np.array_equal(p, p_o), np.flatnonzero((p != p_o).any(1))[:5]
+    rel = np.abs(d - d_o) / np.maximum(np.abs(d_o), 1e-12)
+    assert rel.max() <= 1e-6, (rel.max(), np.argmax(rel))
+    nz = d_o != 0
+    assert np.allclose(cp[nz], cp_o[nz], rtol=0, atol=1e-9)
+    for b in range(len(qq)):
+        assert _grad_close(g[b], g_o[b]), (b, g[b], g_o[b])
+    assert (d_o < 0).any() and (d_o > 0).any()
+
+
+def test_min_distance_cutoff_terrain(built):
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robot, env, q = sc.scene_cfg4(n_configs=64, nx=128, ny=256, spacing=0.016)
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    d_o, p_o, cp_o, g_o = o.min_distance(q, 0.2, nthreads=NT)
+    d, p, cp, g = w.distance(q, 0.2)
+    d, p, g = d.cpu().numpy(), p.cpu().numpy(), g.cpu().numpy()
+    assert np.array_equal(p, p_o)
+    assert np.allclose(d, d_o, rtol=1e-6, atol=1e-12)
+    for b in range(len(q)):
+        assert _grad_close(g[b], g_o[b])
+    w.close()
+
+
+def test_softmin_matches_oracle(cfg2):
+    robot, env, q, w, o = cfg2
+    qt = q[:4]
+    L_o, G_o = o.softmin(qt, 0.01, nthreads=NT)
+    L, G = w.softmin(qt, 0.01)
+    L, G = L.cpu().numpy(), G.cpu().numpy()
+    assert np.allclose(L, L_o, rtol=1e-6, atol=1e-12), (L, L_o)
+    for t in range(len(qt)):
+        assert _grad_close(G[t], G_o[t]), (t, np.abs(G[t] - G_o[t]).max(), np.abs(G_o[t]).max())
+
+
+def test_softmin_finite_differences(cfg2):
+    """Central differences of the GPU soft-min (FP64 distances), h = 1e-5,
+    against the adjoint gradient."""
+    robot, env, q, w, o = cfg2
+    qt = q[4:6].copy()
+    T, Wn, L = qt.shape
+    _, G = w.softmin(qt, 0.01)
+    G = G.cpu().numpy().astype(np.float64)
+    h = 1e-5
+    plus, minus, steps = [], [], []
+    for t in range(T):
+        for wp in range(Wn):
+            for j in range(L):
+                a = qt[t].copy()
+                b = qt[t].copy()
+                a[wp, j] = np.float32(qt[t, wp, j] + h)
+                b[wp, j] = np.float32(qt[t, wp, j] - h)
+                plus.append(a)
+                minus.append(b)
+                steps.append(float(a[wp, j]) - float(b[wp, j]))
+    Lp, _ = w.softmin(np.stack(plus), 0.01, want_grad=False)
+    Lm, _ = w.softmin(np.stack(minus), 0.01, want_grad=False)
+    fd = (Lp.cpu().numpy() - Lm.cpu().numpy()) / np.asarray(steps)
+    fd = fd.reshape(T, Wn, L)
+    ok = 0
+    total = 0
+    for t in range(T):
+        scale = max(np.abs(G[t]).max(), 1e-6)
+        err = np.abs(fd[t] - G[t]) / scale
+        ok += int((err <= GRAD_RTOL).sum())
+        total += err.size
+    # kinks (a closest feature switching inside +-h) may spoil a few entries
+    assert ok >= 0.95 * total, (ok, total)
