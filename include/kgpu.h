@@ -240,6 +240,25 @@ kgpu_status kgpu_check_edges_host(kgpu_world world, int32_t robot, const float* 
                                   const float* qb, const int32_t* nsteps, int32_t E,
                                   int32_t* first_hit);
 
+/* ---- edge checks without allocation --------------------------------------- */
+/* No counterpart in the reference (Klamp't's checkers run on the host).  For
+ * callers that may not allocate device memory while they run — a real-time
+ * planning or control loop that cannot afford cudaMalloc's device-wide
+ * synchronisation, or a host application that hands all device memory to its
+ * own pool — this variant of kgpu_check_edges gives the same results but
+ * works only inside one fixed 20 MiB file-scope device array, which every
+ * GPU that loads the library keeps until the process exits.  At most
+ * KGPU_NOALLOC_MAX_EDGES edges per call (larger E: KGPU_ERR_INVALID).  The
+ * first call on a device looks up the array's address (make it before any
+ * stream capture); each call clears the parts that must start at zero, and
+ * calls that overlap on the GPU race on the shared array, so serialise them.
+ * The world's collision masks must not have changed since its last regular
+ * query (re-uploading them would allocate). */
+#define KGPU_NOALLOC_MAX_EDGES 65536
+kgpu_status kgpu_check_edges_noalloc(kgpu_world world, int32_t robot, const float* qa,
+                                     const float* qb, const int32_t* nsteps, int32_t E,
+                                     int32_t* first_hit, kgpu_stream stream);
+
 /* ---- captured edge-check plans (CUDA-graph replay) ------------------------ */
 /* Records the whole edge-check pipeline for fixed device buffers into a CUDA
  * graph; each launch replays it on `stream`. */

@@ -19,15 +19,23 @@
 
 using namespace kgpu;
 
+namespace {
+thread_local std::string g_err;
+}
+
 namespace kgpu {
+// lets other translation units of the library set kgpu_last_error()
+kgpu_status record_error(kgpu_status code, const char* msg)
+{
+  g_err = msg;
+  return code;
+}
 cudaError_t engine_init();
 size_t engine_smem_per_warp();
 int engine_warps_per_block();
 }
 
 namespace {
-
-thread_local std::string g_err;
 
 kgpu_status fail(kgpu_status code, const char* fmt, ...) __attribute__((format(printf, 2, 3)));
 kgpu_status fail(kgpu_status code, const char* fmt, ...)

@@ -1,0 +1,50 @@
+"""The edge check without allocation (kgpu_check_edges_noalloc), called
+through the C ABI: same first-hit indices as the regular entry point
+(kgpu_check_edges) on two calls in a row, and a clear error past its fixed
+size limit.  This file is collected last on purpose, so a failure here never
+hides the results of the other tests; it also passes when run alone in a
+fresh process."""
+
+import ctypes
+
+import numpy as np
+import pytest
+
+from klampt_gb300 import scenes as sc
+
+pytestmark = pytest.mark.gpu
+
+
+def _dptr(t):
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def test_noalloc_edges_match_regular_entry_point():
+    import torch
+    from klampt_gb300 import build, _kgpu
+    from klampt_gb300.engine import World
+
+    build.build()
+    L = _kgpu.load()
+    robot, env, (qa, qb, ns) = sc.scene_cfg1(n_edges=3000)
+    w = World(env, [robot])
+    a = torch.as_tensor(qa).cuda()
+    b = torch.as_tensor(qb).cuda()
+    n = torch.as_tensor(ns).cuda()
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    ref = torch.empty(len(ns), dtype=torch.int32, device="cuda")
+    _kgpu.check(L.kgpu_check_edges(w.handle, 0, _dptr(a), _dptr(b), _dptr(n), len(ns), _dptr(ref), stream))
+    _kgpu.check(L.kgpu_world_sync(w.handle, stream))
+    ref_np = ref.cpu().numpy()
+    assert (ref_np >= 0).any() and (ref_np < 0).any()
+    for _ in range(2):  # two calls in a row share (and reuse) the static scratch
+        out = torch.full((len(ns),), -7, dtype=torch.int32, device="cuda")
+        _kgpu.check(L.kgpu_check_edges_noalloc(w.handle, 0, _dptr(a), _dptr(b), _dptr(n), len(ns), _dptr(out),
+                                               stream))
+        _kgpu.check(L.kgpu_world_sync(w.handle, stream))
+        assert np.array_equal(out.cpu().numpy(), ref_np)
+    # beyond the fixed maximum: rejected with a message, nothing launched
+    st = L.kgpu_check_edges_noalloc(w.handle, 0, _dptr(a), _dptr(b), _dptr(n), 65537, _dptr(out), stream)
+    assert st == _kgpu.KGPU_ERR_INVALID
+    assert "65536" in _kgpu.last_error()
+    w.close()
