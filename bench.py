@@ -152,6 +152,61 @@ def checked_configs(first_hit: np.ndarray, nsteps: np.ndarray) -> int:
     return int(np.where(first_hit < 0, nsteps + 1, first_hit + 1).sum())
 
 
+def _event_ms(fn, reps: int) -> float:
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    total = 0.0
+    for _ in range(reps):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        fn()
+        e.record()
+        torch.cuda.synchronize()
+        total += s.elapsed_time(e)
+    return total / reps
+
+
+def secondary_metrics(reps: int = 2) -> dict:
+    """dist+grad evaluations/s (trajectory soft-min with its adjoint
+    gradient; clamped minimum distance with gradient) and the heterogeneous
+    multi-robot batch, each on a stated sample of its workload."""
+    import torch
+    from klampt_gb300 import scenes as sc
+    from klampt_gb300.engine import World
+
+    out = {}
+    T, Wn = 1024, 32
+    robot, env, q = sc.scene_cfg2(T=T, W=Wn)
+    w = World(env, [robot])
+    qd = torch.as_tensor(q).cuda()
+    ms = _event_ms(lambda: w.softmin(qd, 0.01, sync=False), reps)
+    w.sync()
+    out["softmin_grad"] = {"value": T * Wn / (ms / 1e3), "unit": "waypoint dist+grad evals/s",
+                           "sample": f"{T} of 8,192 trajectories x {Wn} waypoints, tau 0.01 m, 2,000 icospheres"}
+    w.close()
+    n4 = 65536
+    robot4, env4, q4 = sc.scene_cfg4(n_configs=n4)
+    w4 = World(env4, [robot4])
+    q4d = torch.as_tensor(q4).cuda()
+    ms = _event_ms(lambda: w4.distance(q4d, 0.2, sync=False), reps)
+    w4.sync()
+    out["min_distance_grad"] = {"value": n4 / (ms / 1e3), "unit": "config dist+grad evals/s",
+                                "sample": f"{n4} of 1,048,576 configurations, cutoff 0.2 m, terrain 1.05M tris + 500 boxes"}
+    w4.close()
+    robots, env3, (ids, q3) = sc.scene_cfg3()
+    w3 = World(env3, robots)
+    ids_d = torch.as_tensor(ids).cuda()
+    q3d = torch.as_tensor(q3).cuda()
+    ms = _event_ms(lambda: w3.check_configs_multi(ids_d, q3d, sync=False), reps)
+    w3.sync()
+    out["hetero_configs"] = {"value": len(ids) / (ms / 1e3), "unit": "configs/s",
+                             "sample": "65,536 configs of 6/7/12/30-DOF robots (40/30/20/10%), 1.0M-tri environment, one launch"}
+    w3.close()
+    return out
+
+
 def run_reference(args, rank):
     from klampt_gb300 import scenes as sc
     from oracle.oracle_py import Oracle
@@ -210,6 +265,11 @@ def main():
     a = torch.as_tensor(qa).cuda()
     b = torch.as_tensor(qb).cuda()
     n = torch.as_tensor(ns).cuda()
+    tuned = None
+    if not args.engine_only:
+        from klampt_gb300 import autotune
+        sample = min(args.edges, 4096)
+        tuned, _ = autotune.tune_edges(w, qa[:sample], qb[:sample], ns[:sample])
     out = torch.empty(args.edges, dtype=torch.int32, device="cuda")
     plan = w.edge_plan(a, b, n, out)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
@@ -299,6 +359,9 @@ def main():
     peak, peak_kind = peaks()
     traffic_per_item = profiled_traffic()
     traffic = traffic_per_item * per_step if traffic_per_item is not None else None
+    plan.close()
+    w.close()
+    secondary = secondary_metrics()
 
     line = {
         "metric": METRIC, "value": value, "unit": "configs/s", "n_gpus": world, "steps": args.steps,
@@ -306,7 +369,8 @@ def main():
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 traversal + f64 band", "data": "synthetic (seeded)",
         "config": {"workload": WORKLOAD, "edges": args.edges, "configs_checked_per_step": per_step,
                    "env_tris": int(env.num_tris), "l2": "flushed (256 MiB write) before every step",
-                   "launch": "CUDA-graph edge plan"},
+                   "launch": "CUDA-graph edge plan", "autotuned": tuned},
+        "secondary": secondary,
         "e2e": e2e,
         "gpu_launches": 5 * args.steps,
         "plain_fp64": {"value": plain_rate, "unit": "configs/s", "edges": sub, "speedup": value / plain_rate},
@@ -319,8 +383,6 @@ def main():
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
-    plan.close()
-    w.close()
     if world > 1:
         torch.distributed.barrier()
 

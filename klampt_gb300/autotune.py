@@ -1,0 +1,66 @@
+"""Autotuner for the engine's launch shape and work split.
+
+Tries, on a sample of the caller's own workload, every combination of
+  blocks_per_sm  2, 3, 4   (8-warp blocks per SM; selects the register budget
+                            of the engine instantiation: 128 / 80 / 64)
+  grab           1, 2, 4   (work items a warp takes per queue atomic)
+  job_flush      32, 64    (triangle-pair jobs collected before testing)
+times each with CUDA events (best of `reps` after one warm-up) and leaves the
+fastest setting in the world.  Results are identical for every setting; only
+the time changes.
+"""
+
+from __future__ import annotations
+
+import itertools
+from typing import Callable, Dict, List, Tuple
+
+import torch
+
+from .engine import World
+
+GRID = {"blocks_per_sm": (2, 3, 4), "grab": (1, 2, 4), "job_flush": (32, 64)}
+
+
+def _time(fn: Callable[[], None], reps: int) -> float:
+    fn()
+    torch.cuda.synchronize()
+    best = float("inf")
+    for _ in range(reps):
+        s = torch.cuda.Event(enable_timing=True)
+        e = torch.cuda.Event(enable_timing=True)
+        s.record()
+        fn()
+        e.record()
+        torch.cuda.synchronize()
+        best = min(best, s.elapsed_time(e))
+    return best
+
+
+def tune(world: World, run: Callable[[], None], reps: int = 3) -> Tuple[Dict[str, int], List[Tuple[Dict[str, int], float]]]:
+    """Times `run` (a closure launching the workload on `world`) under every
+    setting; applies and returns the best plus the full table (ms)."""
+    table = []
+    keys = list(GRID)
+    for values in itertools.product(*(GRID[k] for k in keys)):
+        cfg = dict(zip(keys, values))
+        for k, v in cfg.items():
+            world.set_option(k, v)
+        table.append((cfg, _time(run, reps)))
+    best = min(table, key=lambda x: x[1])[0]
+    for k, v in best.items():
+        world.set_option(k, v)
+    world.sync()
+    return best, table
+
+
+def tune_edges(world: World, qa, qb, nsteps, robot: int = 0, reps: int = 3):
+    a = torch.as_tensor(qa).cuda()
+    b = torch.as_tensor(qb).cuda()
+    n = torch.as_tensor(nsteps).cuda()
+    return tune(world, lambda: world.check_edges(a, b, n, robot=robot, sync=False), reps)
+
+
+def tune_configs(world: World, q, robot: int = 0, reps: int = 3):
+    qd = torch.as_tensor(q).cuda()
+    return tune(world, lambda: world.check_configs(qd, robot=robot, sync=False), reps)

@@ -703,6 +703,14 @@ kgpu_status kgpu_world_set_option(kgpu_world w, const char* name, double v)
     int k = (int)v;
     if (k < 2 || k > 4) return fail(KGPU_ERR_INVALID, "blocks_per_sm must be 2, 3 or 4");
     w->blocks_per_sm = k;
+  } else if (!strcmp(name, "grab")) {
+    int k = (int)v;
+    if (k < 1 || k > 16) return fail(KGPU_ERR_INVALID, "grab must be in [1,16]");
+    w->grab = k;
+  } else if (!strcmp(name, "job_flush")) {
+    int k = (int)v;
+    if (k < 8 || k > 64) return fail(KGPU_ERR_INVALID, "job_flush must be in [8,64]");
+    w->job_flush = k;
   } else {
     return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
   }
@@ -718,6 +726,8 @@ kgpu_status kgpu_world_get_option(kgpu_world w, const char* name, double* v)
   else if (!strcmp(name, "eps_env")) *v = w->eps_env;
   else if (!strcmp(name, "warps_per_block")) *v = engine_warps_per_block();
   else if (!strcmp(name, "blocks_per_sm")) *v = w->blocks_per_sm;
+  else if (!strcmp(name, "grab")) *v = w->grab;
+  else if (!strcmp(name, "job_flush")) *v = w->job_flush;
   else if (!strcmp(name, "num_sms")) *v = w->num_sms;
   else return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
   return KGPU_OK;
@@ -781,7 +791,7 @@ kgpu_status kgpu_check_configs(kgpu_world w, int32_t robot, const float* q, int3
   if (!env_hit && !self_hit) return KGPU_OK;
   return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
                                             env_hit, self_hit, nullptr, grid_blocks(w), w->blocks_per_sm,
-                                            (cudaStream_t)s),
+                                            (cudaStream_t)s, w->grab, w->job_flush),
                        "kgpu_check_configs");
 }
 
@@ -798,7 +808,8 @@ kgpu_status kgpu_check_configs_multi(kgpu_world w, const int32_t* robot_ids, con
     return fail(KGPU_ERR_INVALID, "bad buffers or q_stride %d < max links %d", q_stride, maxl);
   if (!env_hit && !self_hit) return KGPU_OK;
   return launch_status(launch_check_configs(w->d_dev, w->scratch, -1, robot_ids, q, q_stride, B, env_hit, self_hit,
-                                            nullptr, grid_blocks(w), w->blocks_per_sm,(cudaStream_t)s),
+                                            nullptr, grid_blocks(w), w->blocks_per_sm, (cudaStream_t)s, w->grab,
+                                            w->job_flush),
                        "kgpu_check_configs_multi");
 }
 
@@ -810,7 +821,7 @@ kgpu_status kgpu_is_feasible(kgpu_world w, int32_t robot, const float* q, int32_
   if (B < 0 || (B > 0 && (!q || !feasible))) return fail(KGPU_ERR_INVALID, "bad buffers");
   return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
                                             nullptr, nullptr, feasible, grid_blocks(w), w->blocks_per_sm,
-                                            (cudaStream_t)s),
+                                            (cudaStream_t)s, w->grab, w->job_flush),
                        "kgpu_is_feasible");
 }
 
@@ -822,7 +833,7 @@ kgpu_status kgpu_check_edges(kgpu_world w, int32_t robot, const float* qa, const
   if (E < 0 || (E > 0 && (!qa || !qb || !nsteps || !first_hit))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if ((st = ensure_edge_scratch(w, E))) return st;
   return launch_status(launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
-                                          w->blocks_per_sm,(cudaStream_t)s),
+                                          w->blocks_per_sm, (cudaStream_t)s, w->grab, w->job_flush),
                        "kgpu_check_edges");
 }
 
@@ -967,7 +978,7 @@ kgpu_status kgpu_edge_plan_create(kgpu_world w, int32_t robot, const float* qa, 
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
-                                        w->blocks_per_sm,cs);
+                                        w->blocks_per_sm, cs, w->grab, w->job_flush);
     e = cudaStreamEndCapture(cs, &p->graph);
     if (e == cudaSuccess && le != cudaSuccess) e = le;
   }

@@ -105,6 +105,9 @@ struct EngineArgs {
   unsigned int* head;
   uint2* spill;
   int spill_per_warp;
+  // work split (autotuned): items per queue grab, triangle-job flush size
+  int grab;
+  int job_flush;
 };
 
 struct Cnt {
@@ -267,7 +270,7 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
 // whose FP32 link transforms are in S.T.  Warp-uniform control flow.
 __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
                                      int qbase, int qcount, int lane, uint2* spill, int spill_cap,
-                                     double (*T64)[12], int& fk64, Cnt& cnt)
+                                     double (*T64)[12], int& fk64, int job_flush, Cnt& cnt)
 {
   const unsigned lt = lanemask_lt();
   int top = 0, njobs = 0, spill_top = 0;
@@ -326,7 +329,7 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
         return TR_FREE;
       }
     }
-    if (njobs > kJobCap - 32 || (top == 0 && njobs > 0)) {
+    if (njobs >= job_flush || (top == 0 && njobs > 0)) {
       const bool hit = run_jobs(S, W, R, njobs, lane, T64, fk64, cnt);
       __syncwarp();
       njobs = 0;
@@ -392,15 +395,17 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
   unsigned long long items = 0;
   const int total = A.mode == MODE_EDGES ? A.meta[1] : A.B;
   const int maxn = A.mode == MODE_EDGES ? A.meta[0] : 0;
+  const int grab = A.grab >= 1 && A.grab <= 16 ? A.grab : kGrab;
+  const int job_flush = A.job_flush >= 8 && A.job_flush <= kJobCap - 32 ? A.job_flush : kJobCap - 32;
 
 #pragma unroll 1
   for (;;) {
     unsigned int base = 0;
-    if (lane == 0) base = atomicAdd(A.head, kGrab);
+    if (lane == 0) base = atomicAdd(A.head, (unsigned)grab);
     base = __shfl_sync(0xffffffffu, base, 0);
     if (base >= (unsigned)total) break;
 #pragma unroll 1
-    for (unsigned it = base; it < base + kGrab && it < (unsigned)total; ++it) {
+    for (unsigned it = base; it < base + grab && it < (unsigned)total; ++it) {
       // ---- decode the item
       int rid = A.robot;
       int b = (int)it, e = 0, k = 0, n = 0;
@@ -488,11 +493,12 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
       const bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
       const bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
       if (want_env && R.nqueries_env > 0)
-        env_res = traverse(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, cnt);
+        env_res = traverse(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, job_flush,
+                           cnt);
       const bool stop = A.mode != MODE_CONFIGS && env_res != TR_FREE;
       if (!stop && want_self && R.nqueries_self > 0)
         self_res = traverse(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill, spill_cap,
-                            T64, fk64, cnt);
+                            T64, fk64, job_flush, cnt);
       if (env_res == TR_OVERFLOW || self_res == TR_OVERFLOW) {
         if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
         continue;
@@ -698,12 +704,15 @@ cudaError_t launch_fk(const KWorldDev* W, int robot, const float* q, int B, floa
 
 cudaError_t launch_check_configs(const KWorldDev* W, const Scratch& S, int robot, const int* robot_ids,
                                  const float* q, int q_stride, int B, uint8_t* env_hit, uint8_t* self_hit,
-                                 uint8_t* feasible, int blocks, int warps_per_block, cudaStream_t s)
+                                 uint8_t* feasible, int blocks, int per_sm, cudaStream_t s, int grab,
+                                 int job_flush)
 {
   if (B <= 0) return cudaSuccess;
   cudaError_t err = cudaMemsetAsync(S.counters, 0, sizeof(unsigned int), s);
   if (err != cudaSuccess) return err;
   EngineArgs A = {};
+  A.grab = grab;
+  A.job_flush = job_flush;
   A.mode = feasible ? MODE_FEASIBLE : MODE_CONFIGS;
   A.robot = robot;
   A.robot_ids = robot_ids;
@@ -716,12 +725,12 @@ cudaError_t launch_check_configs(const KWorldDev* W, const Scratch& S, int robot
   A.head = S.counters;
   A.spill = S.spill;
   A.spill_per_warp = (int)S.spill_per_warp;
-  return dispatch_engine(W, A, blocks, warps_per_block, s);
+  return dispatch_engine(W, A, blocks, per_sm, s);
 }
 
 cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S, int robot, const float* qa,
                                const float* qb, const int* nsteps, int E, int* first_hit, int blocks,
-                               int warps_per_block, cudaStream_t s)
+                               int per_sm, cudaStream_t s, int grab, int job_flush)
 {
   if (E <= 0) return cudaSuccess;
   cudaError_t err;
@@ -736,6 +745,8 @@ cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S
   k_edges_prep3<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, fill, S.edge_perm);
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   EngineArgs A = {};
+  A.grab = grab;
+  A.job_flush = job_flush;
   A.mode = MODE_EDGES;
   A.robot = robot;
   A.qa = qa;
@@ -749,7 +760,7 @@ cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S
   A.head = S.counters;
   A.spill = S.spill;
   A.spill_per_warp = (int)S.spill_per_warp;
-  if ((err = dispatch_engine(W, A, blocks, warps_per_block, s)) != cudaSuccess) return err;
+  if ((err = dispatch_engine(W, A, blocks, per_sm, s)) != cudaSuccess) return err;
   k_edges_finalize<<<gb, tb, 0, s>>>(first_hit, E);
   return cudaGetLastError();
 }

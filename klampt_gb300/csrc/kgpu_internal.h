@@ -207,6 +207,8 @@ struct kgpu_world_s {
   double eps_env = 0.0;
   double eps_extra = 0.0;
   int blocks_per_sm = 3;   // resident 8-warp engine blocks per SM (2, 3 or 4)
+  int grab = 2;            // work items per queue atomic (1..16)
+  int job_flush = 64;      // triangle-pair jobs collected before testing them (8..64)
   int num_sms = 0;
   bool tables_dirty = true;
   // pinned staging for the host-buffer entry points
@@ -229,13 +231,17 @@ namespace kgpu {
 // plain and distance kernels take it by value (W).
 cudaError_t launch_fk(const KWorldDev* Wd, int robot, const float* q, int B, float* T, float* err,
                       cudaStream_t s);
+// per_sm selects the register budget of the engine instantiation; grab = items
+// per work-queue atomic, job_flush = triangle-pair job batch size (0 = default)
 cudaError_t launch_check_configs(const KWorldDev* Wd, const Scratch& S, int robot,
                                  const int* robot_ids, const float* q, int q_stride, int B,
                                  uint8_t* env_hit, uint8_t* self_hit, uint8_t* feasible,
-                                 int blocks, int warps_per_block, cudaStream_t s);
+                                 int blocks, int per_sm, cudaStream_t s, int grab = 0,
+                                 int job_flush = 0);
 cudaError_t launch_check_edges(const KWorldDev* Wd, int* status, const Scratch& S, int robot,
                                const float* qa, const float* qb, const int* nsteps, int E,
-                               int* first_hit, int blocks, int warps_per_block, cudaStream_t s);
+                               int* first_hit, int blocks, int per_sm, cudaStream_t s,
+                               int grab = 0, int job_flush = 0);
 cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q, int B,
                                    uint8_t* env_hit, uint8_t* self_hit, cudaStream_t s);
 cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,

@@ -28,9 +28,6 @@
 
 namespace kgpu {
 kgpu_status record_error(kgpu_status code, const char* msg);
-cudaError_t launch_check_edges(const KWorldDev* Wd, int* status, const Scratch& S, int robot, const float* qa,
-                               const float* qb, const int* nsteps, int E, int* first_hit, int blocks,
-                               int per_sm, cudaStream_t s);
 int engine_warps_per_block();
 int engine_scratch_doubles();
 }  // namespace kgpu

@@ -1,0 +1,126 @@
+"""The Klamp't-facing layer (RobotModel / WorldCollider / RobotCSpace), the
+autograd wrappers and the heterogeneous multi-robot batch, against the FP64
+oracle, through the C ABI."""
+
+import math
+import os
+
+import numpy as np
+import pytest
+
+from klampt_gb300 import scenes as sc
+
+pytestmark = pytest.mark.gpu
+NT = os.cpu_count() or 4
+
+
+@pytest.fixture(scope="module")
+def world0():
+    from klampt_gb300 import build
+    build.build()
+    from klampt_gb300.klampt import WorldModel
+    from oracle.oracle_py import Oracle
+    robot, env, q = sc.scene_cfg0()
+    W = WorldModel([robot], env)
+    yield W, robot, env, q, Oracle(robot, env)
+    W.close()
+
+
+def test_robotmodel_set_config_and_transforms(world0):
+    W, robot, env, q, o = world0
+    r = W.robot(0)
+    with pytest.raises(RuntimeError):
+        r.setConfig([0.0, 1.0])
+    r.setConfig(q[3].astype(np.float64))
+    T64 = o.fk(q[3].astype(np.float64))
+    for i in range(r.numLinks()):
+        R, t = r.link(i).getTransform()
+        Rr = np.asarray(R).reshape(3, 3).T  # column-major -> row-major
+        assert np.allclose(Rr, T64[i, :9].reshape(3, 3), atol=1e-5)
+        assert np.allclose(t, T64[i, 9:], atol=1e-5)
+    eh, sh, _ = o.check_configs(q[3:4])
+    assert r.selfCollides() == bool(sh[0])
+
+
+def test_collider_and_cspace(world0):
+    from klampt_gb300.klampt import RobotCSpace, WorldCollider
+    W, robot, env, q, o = world0
+    col = WorldCollider(W)
+    eh, sh = col.check_configs(q[:512])
+    eo, so, _ = o.check_configs(q[:512], nthreads=NT)
+    assert np.array_equal(eh, eo.astype(bool)) and np.array_equal(sh, so.astype(bool))
+    space = RobotCSpace(W.robot(0), col)
+    f = space.isFeasibleBatch(q[:512])
+    assert np.array_equal(f, o.is_feasible(q[:512], nthreads=NT).astype(bool))
+    assert space.feasible(q[0]) == bool(f[0])
+    space.setVisibilityEpsilon(1e-2)
+    qa, qb, _ = sc.random_edges(robot, 64, np.random.default_rng(12))
+    vis, fh = space.isVisibleBatch(qa, qb)
+    n = space.steps(qa, qb)
+    fh_o, _ = o.check_edges(qa, qb, n, nthreads=NT)
+    assert np.array_equal(fh, fh_o) and np.array_equal(vis, fh_o < 0)
+    assert space.isVisible(qa[0], qb[0]) == bool(vis[0])
+
+
+def test_collider_distance_result(world0):
+    from klampt_gb300.klampt import DistanceQuerySettings, WorldCollider
+    W, robot, env, q, o = world0
+    col = WorldCollider(W)
+    W.robot(0).setConfig(q[5].astype(np.float64))
+    res = col.distance(settings=DistanceQuerySettings(upperBound=2.0))
+    d_o, p_o, cp_o, _ = o.min_distance(q[5:6], 2.0)
+    assert abs(res.d - d_o[0]) <= 1e-9 * max(1.0, abs(d_o[0]))
+    assert (res.elem1, res.elem2) == tuple(p_o[0])
+    if res.hasGradients:
+        assert abs(np.linalg.norm(res.grad1) - 1.0) < 1e-6
+
+
+def test_autograd_wrappers():
+    import torch
+    from klampt_gb300.autodiff import MinDistance, SoftMinDistance
+    from klampt_gb300.engine import World
+    robot, env, q = sc.scene_cfg2(T=8, W=4)
+    w = World(env, [robot])
+    qt = torch.as_tensor(q).cuda().requires_grad_(True)
+    L = SoftMinDistance.apply(qt, w, 0.01)
+    (2.0 * L).sum().backward()
+    L2, G = w.softmin(q, 0.01)
+    assert torch.allclose(L.detach(), L2)
+    assert torch.allclose(qt.grad, 2.0 * G)
+    qc = torch.as_tensor(q.reshape(-1, 7)[:16]).cuda().requires_grad_(True)
+    d = MinDistance.apply(qc, w, 1.0)
+    d.sum().backward()
+    _, _, _, g = w.distance(q.reshape(-1, 7)[:16], 1.0)
+    assert torch.allclose(qc.grad, g)
+    w.close()
+
+
+def test_autotuner_keeps_results(world0):
+    from klampt_gb300 import autotune
+    W, robot, env, q, o = world0
+    w = W.engine
+    before = w.check_configs(q[:512])
+    best, table = autotune.tune_configs(w, q[:512], reps=1)
+    assert len(table) == 18 and set(best) == {"blocks_per_sm", "grab", "job_flush"}
+    assert all(w.get_option(k) == v for k, v in best.items())
+    after = w.check_configs(q[:512])
+    assert all(np.array_equal(x.cpu().numpy(), y.cpu().numpy()) for x, y in zip(before, after))
+
+
+def test_heterogeneous_batch_matches_oracle():
+    """Four robots (6-DOF, 7-DOF, 12-DOF dual arm, 30-DOF humanoid) in one
+    launch, every configuration checked against its own robot's oracle."""
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robots, env, (ids, q) = sc.scene_cfg3(total=1024, n_spheres=70, n_boxes=870)
+    w = World(env, robots)
+    eh, sh = w.check_configs_multi(ids, q)
+    eh, sh = eh.cpu().numpy(), sh.cpu().numpy()
+    for r, spec in enumerate(robots):
+        sel = np.flatnonzero(ids == r)
+        o = Oracle(spec, env)
+        eo, so, _ = o.check_configs(q[sel, :spec.num_links], nthreads=NT)
+        assert np.array_equal(eh[sel], eo), r
+        assert np.array_equal(sh[sel], so), r
+    assert 0 < eh.mean() < 1 and 0 < sh.mean() < 1
+    w.close()
