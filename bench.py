@@ -59,7 +59,27 @@ def parse():
     p.add_argument("--edges", type=int, default=16384)
     p.add_argument("--engine-only", action="store_true",
                    help="only warm-up + timed edge-plan launches (profiling runs); prints the device time")
+    p.add_argument("--dist-only", type=int, default=0, metavar="N",
+                   help="only N minimum-distance+gradient evaluations on the soft-min scene (profiling runs)")
     return p.parse_args()
+
+
+def run_dist_only(args):
+    import torch
+    from klampt_gb300 import build as kbuild
+    kbuild.build()
+    from klampt_gb300 import scenes as sc
+    from klampt_gb300.engine import World
+    robot, env, q = sc.scene_cfg2(T=(args.dist_only + 31) // 32, W=32)
+    w = World(env, [robot])
+    qd = torch.as_tensor(q.reshape(-1, robot.num_links)[:args.dist_only]).cuda()
+    for _ in range(max(1, args.warmup)):
+        w.distance(qd, 1e3)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        w.distance(qd, 1e3, sync=False)
+    w.sync()
+    print(json.dumps({"dist_only": args.dist_only, "ms_per_step": 1e3 * (time.perf_counter() - t0) / max(1, args.steps)}))
 
 
 def dist_env():
@@ -245,6 +265,9 @@ def run_reference(args, rank):
 def main():
     args = parse()
     rank, world, local = dist_env()
+    if args.dist_only:
+        run_dist_only(args)
+        return
     if args.impl == "reference":
         run_reference(args, rank)
         return

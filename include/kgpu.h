@@ -111,6 +111,10 @@ typedef struct {
   uint64_t spills;         /* traversal stack spills to global memory           */
   uint64_t certified;      /* contacts certified in FP32 (no FP64 needed)       */
   uint64_t fp64_hits;      /* contacts confirmed by the FP64 re-test            */
+  uint64_t dist_pairs;     /* (link, object) pairs evaluated by distance queries */
+  uint64_t dist_node_pairs;/* BVH node pairs tested by distance queries          */
+  uint64_t dist_tri_pairs; /* triangle pairs evaluated in FP32 by distance queries */
+  uint64_t dist_fp64;      /* triangle pairs finalised in FP64                     */
 } kgpu_stats;
 
 /* ---- model construction --------------------------------------------------- */

@@ -48,7 +48,9 @@ class EnvDesc(ctypes.Structure):
 class Stats(ctypes.Structure):
     _fields_ = [("items", ctypes.c_uint64), ("node_pairs", ctypes.c_uint64), ("tri_pairs", ctypes.c_uint64),
                 ("band_pairs", ctypes.c_uint64), ("spills", ctypes.c_uint64), ("certified", ctypes.c_uint64),
-                ("fp64_hits", ctypes.c_uint64)]
+                ("fp64_hits", ctypes.c_uint64), ("dist_pairs", ctypes.c_uint64),
+                ("dist_node_pairs", ctypes.c_uint64), ("dist_tri_pairs", ctypes.c_uint64),
+                ("dist_fp64", ctypes.c_uint64)]
 
 
 class KgpuError(RuntimeError):

@@ -62,6 +62,15 @@ struct Builder {
       out.node_c64[3 * (size_t)node + i] = c[i];
       out.node_h64[3 * (size_t)node + i] = h[i];
     }
+    double r2 = 0.0;
+    for (int k = 0; k < n; ++k) {
+      const double* T = &tri[9 * (size_t)ids[k]];
+      for (int v = 0; v < 3; ++v) {
+        double dx = T[3 * v] - c[0], dy = T[3 * v + 1] - c[1], dz = T[3 * v + 2] - c[2];
+        r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
+      }
+    }
+    out.node_r[node] = std::sqrt(r2) * (1.0 + 1e-9) + 1e-12;
     float cf[3], hf[3];
     for (int i = 0; i < 3; ++i) {
       cf[i] = (float)c[i];
@@ -78,6 +87,7 @@ struct Builder {
     out.nodes.resize(l + 2);
     out.node_c64.resize(3 * (size_t)(l + 2));
     out.node_h64.resize(3 * (size_t)(l + 2));
+    out.node_r.resize(l + 2, 0.0);
     out.node_obj.resize(l + 2, -1);
     return l;
   }
@@ -131,6 +141,7 @@ void build_bvh(const std::vector<double>& tri, const std::vector<int>& ids,
   out.nodes.clear();
   out.node_c64.clear();
   out.node_h64.clear();
+  out.node_r.clear();
   out.node_obj.clear();
   out.order.clear();
   if (ids.empty()) return;
@@ -144,6 +155,7 @@ void build_bvh(const std::vector<double>& tri, const std::vector<int>& ids,
   out.nodes.resize(1);
   out.node_c64.resize(3);
   out.node_h64.resize(3);
+  out.node_r.assign(1, 0.0);
   out.node_obj.assign(1, -1);
   if (!tri_obj) {
     out.order = ids;

@@ -100,7 +100,7 @@ inline int as_int(float f)
 
 // appends `b` to the concatenated arrays with node/triangle index shifts
 void append_bvh(const HostBvh& b, int node_base, int tri_base, std::vector<KNode>& nodes,
-                std::vector<double>& node64)
+                std::vector<double>& node64, std::vector<float>* node_r = nullptr)
 {
   for (size_t k = 0; k < b.nodes.size(); ++k) {
     KNode n = b.nodes[k];
@@ -109,6 +109,19 @@ void append_bvh(const HostBvh& b, int node_base, int tri_base, std::vector<KNode
     nodes.push_back(n);
     for (int i = 0; i < 3; ++i) node64.push_back(b.node_c64[3 * k + i]);
     for (int i = 0; i < 3; ++i) node64.push_back(b.node_h64[3 * k + i]);
+    if (node_r) {
+      // sphere about the FP32 centre: the FP64 radius plus the centre's rounding
+      const double cf[3] = {b.nodes[k].a.x, b.nodes[k].a.y, b.nodes[k].a.z};
+      double off2 = 0.0;
+      for (int i = 0; i < 3; ++i) {
+        const double d = b.node_c64[3 * k + i] - cf[i];
+        off2 += d * d;
+      }
+      double r = b.node_r[k] + std::sqrt(off2);
+      float f = (float)r;
+      if ((double)f < r) f = std::nextafter(f, 3.0e38f);
+      node_r->push_back(f);
+    }
   }
 }
 
@@ -121,6 +134,7 @@ void free_world_device(kgpu_world w)
   dfree(w->d_ltri32);
   dfree(w->d_ltri64);
   dfree(w->d_lnode64);
+  dfree(w->d_lnode_r);
   dfree(w->d_ltri_orig);
   dfree(w->d_lvert32);
   dfree(w->d_lvert64);
@@ -545,6 +559,7 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   std::vector<double> node64, tri64, lvert64;
   std::vector<float4> tri32, lvert32;
   std::vector<int> ltri_orig;
+  std::vector<float> lnode_r;
   double reach = 0.0;
   for (int r = 0; r < n; ++r) {
     kgpu_robot R = robots[r];
@@ -552,7 +567,7 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
     w->robot_tri_base.push_back((int)(tri32.size() / 3));
     w->robot_vert_base.push_back((int)lvert32.size());
     for (int l = 0; l < R->nlinks; ++l) {
-      append_bvh(R->bvh[l], (int)nodes.size(), (int)(tri32.size() / 3), nodes, node64);
+      append_bvh(R->bvh[l], (int)nodes.size(), (int)(tri32.size() / 3), nodes, node64, &lnode_r);
       for (size_t k = 0; k < R->tri64[l].size(); k += 3)
         tri32.push_back(make_float4((float)R->tri64[l][k], (float)R->tri64[l][k + 1], (float)R->tri64[l][k + 2], 0.f));
       tri64.insert(tri64.end(), R->tri64[l].begin(), R->tri64[l].end());
@@ -578,12 +593,14 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   if (tri32.empty()) tri32.resize(3);
   if (tri64.empty()) tri64.resize(9);
   if (node64.empty()) node64.resize(6);
+  if (lnode_r.empty()) lnode_r.resize(1);
   if (ltri_orig.empty()) ltri_orig.resize(1);
   if (lvert32.empty()) lvert32.resize(1);
   if (lvert64.empty()) lvert64.resize(3);
   e = cudaSuccess;
   if (e == cudaSuccess) e = upload(&w->d_lnodes, nodes.data(), nodes.size());
   if (e == cudaSuccess) e = upload(&w->d_lnode64, node64.data(), node64.size());
+  if (e == cudaSuccess) e = upload(&w->d_lnode_r, lnode_r.data(), lnode_r.size());
   if (e == cudaSuccess) e = upload(&w->d_ltri32, tri32.data(), tri32.size());
   if (e == cudaSuccess) e = upload(&w->d_ltri64, tri64.data(), tri64.size());
   if (e == cudaSuccess) e = upload(&w->d_ltri_orig, ltri_orig.data(), ltri_orig.size());
@@ -591,8 +608,8 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   if (e == cudaSuccess) e = upload(&w->d_lvert64, lvert64.data(), lvert64.size());
   if (e == cudaSuccess) e = cudaMalloc((void**)&w->d_status, sizeof(int));
   if (e == cudaSuccess) e = cudaMemset(w->d_status, 0, sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&w->d_stats, 8 * sizeof(unsigned long long));
-  if (e == cudaSuccess) e = cudaMemset(w->d_stats, 0, 8 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&w->d_stats, 16 * sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemset(w->d_stats, 0, 16 * sizeof(unsigned long long));
   // scratch: per-warp spill stacks, queue heads, edge ordering tables
   Scratch& S = w->scratch;
   S.max_warps = w->num_sms * 4 * engine_warps_per_block();  // up to 4 blocks per SM
@@ -622,6 +639,7 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   D.lvert32 = w->d_lvert32;
   D.lvert64 = w->d_lvert64;
   D.lnode64 = w->d_lnode64;
+  D.lnode_r = w->d_lnode_r;
   if (env) {
     D.enodes = env->d_nodes;
     D.etri32 = env->d_tri32;
@@ -754,7 +772,7 @@ kgpu_status kgpu_world_sync(kgpu_world w, kgpu_stream stream)
 kgpu_status kgpu_world_get_stats(kgpu_world w, kgpu_stats* out)
 {
   if (!w || !out) return fail(KGPU_ERR_INVALID, "null argument");
-  unsigned long long s[8];
+  unsigned long long s[16];
   CK(cudaMemcpy(s, w->d_stats, sizeof s, cudaMemcpyDeviceToHost));
   out->items = s[0];
   out->node_pairs = s[1];
@@ -763,13 +781,17 @@ kgpu_status kgpu_world_get_stats(kgpu_world w, kgpu_stats* out)
   out->spills = s[4];
   out->certified = s[5];
   out->fp64_hits = s[6];
+  out->dist_pairs = s[8];
+  out->dist_node_pairs = s[9];
+  out->dist_tri_pairs = s[10];
+  out->dist_fp64 = s[11];
   return KGPU_OK;
 }
 
 kgpu_status kgpu_world_reset_stats(kgpu_world w)
 {
   if (!w) return fail(KGPU_ERR_INVALID, "null world");
-  CK(cudaMemset(w->d_stats, 0, 8 * sizeof(unsigned long long)));
+  CK(cudaMemset(w->d_stats, 0, 16 * sizeof(unsigned long long)));
   return KGPU_OK;
 }
 

@@ -50,7 +50,7 @@ constexpr int kDStack = 512;   // node-pair stack entries per warp
 constexpr int kDGStack = 512;  // environment-tree stack for gathering objects
 constexpr int kDJobs = 64;     // leaf-pair jobs
 constexpr int kDCand = 64;     // FP64 triangle-pair candidates
-constexpr int kDPairs = 128;   // (link, object) candidates per link and round
+constexpr int kDPairs = 128;   // gathered (link, object) candidates
 constexpr double kSoftK = 12.0;
 
 struct __align__(16) DistSmem {
@@ -60,6 +60,7 @@ struct __align__(16) DistSmem {
   uint32_t candA[kDCand], candB[kDCand];
   float candD[kDCand];
   int pobj[kDPairs];
+  int plink[kDPairs];
   float plb[kDPairs];
   float T[kMaxLinks][12];
   float delta[kMaxLinks];
@@ -94,7 +95,7 @@ struct DistArgs {
 };
 
 struct DCnt {
-  unsigned long long pairs = 0, tri = 0, band = 0;
+  unsigned long long pairs = 0, tri = 0, band = 0, nodes = 0;
 };
 
 __device__ __forceinline__ float box_dist32(const Box32& A, float3 c, float3 h)
@@ -301,7 +302,9 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
   const float* TA = S.T[l];
 #pragma unroll 1
   while (top > 0 || njobs > 0) {
-    if (njobs > kDJobs - 32 || (top == 0 && njobs > 0)) {
+    // triangle jobs are tested early (16 at a time): the running minimum they
+    // produce is what prunes the rest of the traversal
+    if (njobs >= 16 || (top == 0 && njobs > 0)) {
       // ---- triangle pairs, one per lane
       uint32_t carry = 0;
       for (int b = 0; b < njobs; b += 32) {
@@ -352,7 +355,23 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
           }
           const float span = fmaxf(fmaxf(hi3.x - lo3.x, hi3.y - lo3.y), hi3.z - lo3.z);
           e = dl + de + 128.f * kU * span + 1e-8f;
-          if (!tri_separated32(P, Q, dl + de, 0.f)) {
+          // triangle-box lower bound: skip the full distance when it cannot
+          // be a candidate
+          float3 pl = P[0], ph = P[0], ql = Q[0], qh = Q[0];
+#pragma unroll
+          for (int k = 1; k < 3; ++k) {
+            pl = make_float3(fminf(pl.x, P[k].x), fminf(pl.y, P[k].y), fminf(pl.z, P[k].z));
+            ph = make_float3(fmaxf(ph.x, P[k].x), fmaxf(ph.y, P[k].y), fmaxf(ph.z, P[k].z));
+            ql = make_float3(fminf(ql.x, Q[k].x), fminf(ql.y, Q[k].y), fminf(ql.z, Q[k].z));
+            qh = make_float3(fmaxf(qh.x, Q[k].x), fmaxf(qh.y, Q[k].y), fmaxf(qh.z, Q[k].z));
+          }
+          const float gx = fmaxf(0.f, fmaxf(ql.x - ph.x, pl.x - qh.x));
+          const float gy = fmaxf(0.f, fmaxf(ql.y - ph.y, pl.y - qh.y));
+          const float gz = fmaxf(0.f, fmaxf(ql.z - ph.z, pl.z - qh.z));
+          const float blb = sqrtf(gx * gx + gy * gy + gz * gz) * (1.f - 4.f * kU);
+          if (blb - e > fminf(m32 * (1.f + 2e-5f) + 2.f * e, fb + e)) {
+            d32 = FLT_MAX;  // not a candidate (and no better than the running minimum)
+          } else if (!tri_separated32(P, Q, dl + de, 0.f)) {
             d32 = 0.f;
             certain = tri_certain_hit32(P[0], P[1], P[2], Q[0], Q[1], Q[2], fmaxf(dl, de));
           } else {
@@ -401,13 +420,23 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
     int outcome = 0;
     uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
     uint32_t jA = 0, jB = 0;
+    cnt.nodes += have ? 1 : 0;
     if (have) {
       const int nodeB = (int)en.x, nodeA = (int)en.y;
       const KNode na = W->lnodes[nodeA];
       const KNode nb = W->enodes[nodeB];
       const Box32 A = xform_box(TA, na.a, na.b);
-      const float lb = box_dist32(A, make_float3(nb.a.x, nb.a.y, nb.a.z), make_float3(nb.b.x, nb.b.y, nb.b.z)) -
-                       (dl + de) * 1.7321f - 4.f * kU * (fabsf(A.c.x) + fabsf(A.c.y) + fabsf(A.c.z) + 1.f);
+      const float slack = 4.f * kU * (fabsf(A.c.x) + fabsf(A.c.y) + fabsf(A.c.z) + 1.f);
+      const float lb_box = box_dist32(A, make_float3(nb.a.x, nb.a.y, nb.a.z), make_float3(nb.b.x, nb.b.y, nb.b.z)) -
+                           (dl + de) * 1.7321f - slack;
+      // the rotation-invariant sphere about the node centre is tighter than the
+      // world box of a rotated node in most directions
+      const float gx = fmaxf(0.f, fabsf(A.c.x - nb.a.x) - nb.b.x);
+      const float gy = fmaxf(0.f, fabsf(A.c.y - nb.a.y) - nb.b.y);
+      const float gz = fmaxf(0.f, fabsf(A.c.z - nb.a.z) - nb.b.z);
+      const float lb_sph = sqrtf(gx * gx + gy * gy + gz * gz) * (1.f - 4.f * kU) - __ldg(W->lnode_r + nodeA) -
+                           (dl + de) * 1.7321f - slack;
+      const float lb = fmaxf(lb_box, lb_sph);
       const float lim = fminf(m32 * (1.f + 2e-5f) + 3.f * (dl + de) + 1e-5f, fb + 2.f * (dl + de) + 1e-5f);
       if (lb <= lim) {
         const int cntA = f2i(na.b.w), cntB = f2i(nb.b.w);
@@ -505,8 +534,11 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
       if (fabsf(w.x - ob.a.x) > ob.b.x + tolb || fabsf(w.y - ob.a.y) > ob.b.y + tolb ||
           fabsf(w.z - ob.a.z) > ob.b.z + tolb)
         continue;
+      // a vertex stops counting once it is no deeper than the deepest so far
+      // (or outside the band): its final minimum can only be lower
+      const float stop = fmaxf(lmax, -ed);
       float dmin = FLT_MAX;
-      for (int f = ff; f < ff + fc; ++f) {
+      for (int f = ff; f < ff + fc && dmin > stop; ++f) {
         const float4 pl = __ldg(W->eface32 + f);
         dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
       }
@@ -524,8 +556,9 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
         if (fabsf(w.x - ob.a.x) > ob.b.x + tolb || fabsf(w.y - ob.a.y) > ob.b.y + tolb ||
             fabsf(w.z - ob.a.z) > ob.b.z + tolb)
           continue;
+        const float stop = fmaxf(gmax - 2.f * ed, -ed);
         float dmin = FLT_MAX;
-        for (int f = ff; f < ff + fc; ++f) {
+        for (int f = ff; f < ff + fc && dmin >= stop; ++f) {
           const float4 pl = __ldg(W->eface32 + f);
           dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
         }
@@ -598,6 +631,7 @@ __device__ int gather_objects(DistSmem& S, const KWorldDev* __restrict__ W, cons
   const Box32 A = xform_box(S.T[l], la.a, la.b);
   const float slack = (S.delta[l] + W->eps_env + 2.f * W->eps_extra) * 1.7321f +
                       4.f * kU * (fabsf(A.c.x) + fabsf(A.c.y) + fabsf(A.c.z) + 1.f) + 1e-7f;
+  const float rad = __ldg(W->lnode_r + R.link_root[l]);
   while (top > 0 && count <= kDPairs - 32) {
     if (top > kDGStack - 64) {
       if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
@@ -615,7 +649,12 @@ __device__ int gather_objects(DistSmem& S, const KWorldDev* __restrict__ W, cons
     int child = 0;
     if (have) {
       const KNode nb = W->enodes[node];
-      lbv = box_dist32(A, make_float3(nb.a.x, nb.a.y, nb.a.z), make_float3(nb.b.x, nb.b.y, nb.b.z)) - slack;
+      const float gx = fmaxf(0.f, fabsf(A.c.x - nb.a.x) - nb.b.x);
+      const float gy = fmaxf(0.f, fabsf(A.c.y - nb.a.y) - nb.b.y);
+      const float gz = fmaxf(0.f, fabsf(A.c.z - nb.a.z) - nb.b.z);
+      lbv = fmaxf(box_dist32(A, make_float3(nb.a.x, nb.a.y, nb.a.z), make_float3(nb.b.x, nb.b.y, nb.b.z)),
+                  sqrtf(gx * gx + gy * gy + gz * gz) * (1.f - 4.f * kU) - rad) -
+            slack;
       if (lbv <= bound) {
         const int o = W->node_obj[node];
         if (o >= 0) {
@@ -636,6 +675,7 @@ __device__ int gather_objects(DistSmem& S, const KWorldDev* __restrict__ W, cons
     } else if (outcome == 2) {
       const int r = count + __popc(m2 & lt);
       S.pobj[r] = child;
+      S.plink[r] = l;
       S.plb[r] = lbv;
     }
     top += 2 * __popc(m1);
@@ -751,8 +791,37 @@ __global__ void __launch_bounds__(kDW * 32, 2) k_dist(const KWorldDev* __restric
       // farther) or the bound reached the cutoff
       float lower = -1.f;
       double round_bound = fmin(A.cutoff, 0.05);
+      // evaluates the gathered (link, object) pairs nearest first, over all
+      // links at once, so that the closest pair of any link sets the bound
+      // that prunes the rest
+      auto eval_list = [&](int np) {
+        for (int done = 0; done < np; ++done) {
+          float v = FLT_MAX;
+          int idx = -1;
+          for (int k = lane; k < np; k += 32)
+            if (S.plb[k] < v) { v = S.plb[k]; idx = k; }
+          const float vm = warp_min(v);
+          const unsigned mm = __ballot_sync(0xffffffffu, v == vm && idx >= 0);
+          if (mm == 0u) break;
+          const int owner = __ffs(mm) - 1;
+          const int k = __shfl_sync(0xffffffffu, idx, owner);
+          if (lane == 0) S.plb[k] = FLT_MAX;
+          __syncwarp();
+          if (vm > (float)fmax(best, 0.0) * 1.00001f + 1e-6f) break;
+          const int o = S.pobj[k], l = S.plink[k];
+          PairOut po;
+          eval_pair(S, W, R, T64, fk64, lane, l, o, nextafter(best, 1e300), po, cnt);
+          if (po.found && (po.d < best || (po.d == best && (l < bl || (l == bl && o < bo))))) {
+            best = po.d;
+            bl = l;
+            bo = o;
+            bp = po;
+          }
+        }
+      };
       for (;;) {
         const float bound = round_bound >= A.cutoff ? FLT_MAX : (float)round_bound * 1.000001f;
+        int np = 0;
         for (int l = 0; l < nl; ++l) {
           if (R.link_root[l] < 0) continue;
           for (int g = 0; g < kMaxGroups; ++g) {
@@ -764,34 +833,16 @@ __global__ void __launch_bounds__(kDW * 32, 2) k_dist(const KWorldDev* __restric
               // box bounds limit the unsigned distance: a pair can be
               // negative only when its boxes meet, hence max(best, 0)
               const float reach = (float)fmax(best, 0.0) * 1.00001f + 1e-6f;
-              const int np = gather_objects(S, W, R, lane, l, fminf(bound, reach), lower,
-                                            0, top);
-              // evaluate nearest first
-              for (int done = 0; done < np; ++done) {
-                float v = FLT_MAX;
-                int idx = -1;
-                for (int k = lane; k < np; k += 32)
-                  if (S.plb[k] < v) { v = S.plb[k]; idx = k; }
-                const float vm = warp_min(v);
-                const unsigned mm = __ballot_sync(0xffffffffu, v == vm && idx >= 0);
-                const int owner = __ffs(mm) - 1;
-                const int k = __shfl_sync(0xffffffffu, idx, owner);
-                if (lane == 0) S.plb[k] = FLT_MAX;
-                __syncwarp();
-                if (vm > (float)fmax(best, 0.0) * 1.00001f + 1e-6f) break;
-                const int o = S.pobj[k];
-                PairOut po;
-                eval_pair(S, W, R, T64, fk64, lane, l, o, nextafter(best, 1e300), po, cnt);
-                if (po.found && (po.d < best || (po.d == best && (l < bl || (l == bl && o < bo))))) {
-                  best = po.d;
-                  bl = l;
-                  bo = o;
-                  bp = po;
-                }
+              np = gather_objects(S, W, R, lane, l, fminf(bound, reach), lower, np, top);
+              if (top > 0) {
+                // list full: evaluate what it holds, then keep gathering
+                eval_list(np);
+                np = 0;
               }
             }
           }
         }
+        eval_list(np);
         if (best <= round_bound || round_bound >= A.cutoff) break;
         lower = bound;
         round_bound = fmin(A.cutoff, round_bound * 4.0);
@@ -842,7 +893,20 @@ __global__ void __launch_bounds__(kDW * 32, 2) k_dist(const KWorldDev* __restric
       pullback(S, R, lane, A.grad ? A.grad + (size_t)b * nl : nullptr);
     }
   }
-  (void)cnt;
+  // counters: pairs are counted once per warp (lane 0), the rest per lane
+  unsigned long long nd = cnt.nodes, tp = cnt.tri, bd = cnt.band;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    nd += __shfl_down_sync(0xffffffffu, nd, o);
+    tp += __shfl_down_sync(0xffffffffu, tp, o);
+    bd += __shfl_down_sync(0xffffffffu, bd, o);
+  }
+  if (lane == 0 && W->stats) {
+    atomicAdd(W->stats + 8, cnt.pairs);
+    atomicAdd(W->stats + 9, nd);
+    atomicAdd(W->stats + 10, tp);
+    atomicAdd(W->stats + 11, bd);
+  }
 }
 
 // per-trajectory minimum of the waypoint minima

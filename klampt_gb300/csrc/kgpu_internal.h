@@ -41,6 +41,8 @@ struct HostBvh {
   std::vector<KNode> nodes;          // local indices (root = 0)
   std::vector<double> node_c64;      // 3 per node, FP64 center
   std::vector<double> node_h64;      // 3 per node, FP64 half extent
+  std::vector<double> node_r;        // per node: radius of the sphere about the box
+                                     // centre that holds the node's vertices
   std::vector<int> order;            // triangle ids in leaf order
   std::vector<int> node_obj;         // object owning each node (-1 above objects)
 };
@@ -83,6 +85,7 @@ struct KWorldDev {
   const float4* ltri32;      // 3 per tri
   const double* ltri64;      // 9 per tri
   const double* lnode64;     // 6 per node (c, h) FP64 (plain kernel)
+  const float* lnode_r;      // per link node: radius about its FP32 centre holding its vertices
   const int* ltri_orig;      // per link triangle: index in its link's mesh order
   const float4* lvert32;     // unique link vertices (link frame), mesh order
   const double* lvert64;     // 3 per unique link vertex
@@ -193,6 +196,7 @@ struct kgpu_world_s {
   float4* d_ltri32 = nullptr;
   double* d_ltri64 = nullptr;
   double* d_lnode64 = nullptr;
+  float* d_lnode_r = nullptr;
   int* d_ltri_orig = nullptr;
   float4* d_lvert32 = nullptr;
   double* d_lvert64 = nullptr;
