@@ -154,7 +154,9 @@ kgpu_status kgpu_world_enable_self_pair(kgpu_world world, int32_t robot, int32_t
 /* Named options: "eps_extra" (m, additional inflation of every FP32 test on
  * top of the computed error bounds, default 0), "blocks_per_sm" (2, 3 or 4
  * resident engine blocks per SM), "grab" (work items per queue atomic, 1..16),
- * "job_flush" (triangle-pair jobs batched before testing, 8..64), read-only
+ * "job_flush" (triangle-pair jobs batched before testing, 8..64),
+ * "edge_chunk" (consecutive steps of an edge checked in order by one work
+ * item, 1..64, default 4), read-only
  * "eps_env", "warps_per_block", "num_sms".  The autotuner
  * (klampt_gb300/autotune.py) sets blocks_per_sm, grab and job_flush.
  * Unknown names are KGPU_ERR_INVALID. */

@@ -618,7 +618,7 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.counters, 64 * sizeof(unsigned int));
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_hist, (kMaxSteps + 2) * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_round_off, (kMaxSteps + 2) * sizeof(int));
-  if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_meta, (4 + kMaxSteps + 2) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_meta, (4 + 2 * (kMaxSteps + 2)) * sizeof(int));
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&w->host_stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     free_world_device(w);
@@ -729,6 +729,10 @@ kgpu_status kgpu_world_set_option(kgpu_world w, const char* name, double v)
     int k = (int)v;
     if (k < 8 || k > 64) return fail(KGPU_ERR_INVALID, "job_flush must be in [8,64]");
     w->job_flush = k;
+  } else if (!strcmp(name, "edge_chunk")) {
+    int k = (int)v;
+    if (k < 1 || k > 64) return fail(KGPU_ERR_INVALID, "edge_chunk must be in [1,64]");
+    w->edge_chunk = k;
   } else {
     return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
   }
@@ -746,6 +750,7 @@ kgpu_status kgpu_world_get_option(kgpu_world w, const char* name, double* v)
   else if (!strcmp(name, "blocks_per_sm")) *v = w->blocks_per_sm;
   else if (!strcmp(name, "grab")) *v = w->grab;
   else if (!strcmp(name, "job_flush")) *v = w->job_flush;
+  else if (!strcmp(name, "edge_chunk")) *v = w->edge_chunk;
   else if (!strcmp(name, "num_sms")) *v = w->num_sms;
   else return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
   return KGPU_OK;
@@ -855,7 +860,7 @@ kgpu_status kgpu_check_edges(kgpu_world w, int32_t robot, const float* qa, const
   if (E < 0 || (E > 0 && (!qa || !qb || !nsteps || !first_hit))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if ((st = ensure_edge_scratch(w, E))) return st;
   return launch_status(launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
-                                          w->blocks_per_sm, (cudaStream_t)s, w->grab, w->job_flush),
+                                          w->blocks_per_sm, (cudaStream_t)s, w->grab, w->job_flush, w->edge_chunk),
                        "kgpu_check_edges");
 }
 
@@ -1000,7 +1005,7 @@ kgpu_status kgpu_edge_plan_create(kgpu_world w, int32_t robot, const float* qa, 
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
-                                        w->blocks_per_sm, cs, w->grab, w->job_flush);
+                                        w->blocks_per_sm, cs, w->grab, w->job_flush, w->edge_chunk);
     e = cudaStreamEndCapture(cs, &p->graph);
     if (e == cudaSuccess && le != cudaSuccess) e = le;
   }

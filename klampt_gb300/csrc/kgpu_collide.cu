@@ -13,9 +13,10 @@
 // Execution model
 //   * One warp processes one work item (a configuration or an edge step) at
 //     a time and pulls items from a device work queue (persistent grid sized
-//     to the SM count).  Edge steps are ordered step-major across edges, so
-//     every edge's early steps run first and a step beyond an edge's first
-//     collision is skipped.
+//     to the SM count).  An edge item is a chunk of consecutive steps
+//     (`chunk`, default 4) checked in order; chunks are ordered round-major
+//     across edges, so every edge's early steps run first and a step beyond
+//     an edge's first collision is skipped.
 //   * FK: lane i owns link i (warp_fk32); transforms go to shared memory.
 //   * All queries of the item — (link, env group) and (link, link) pairs —
 //     share one warp stack of BVH node pairs tagged with their query, so the
@@ -43,6 +44,9 @@ constexpr int kStackCap = 384;
 constexpr int kJobCap = 96;
 constexpr int kGrab = 2;  // items taken from the queue per atomic
 constexpr int kWarps = 8; // warps per block
+constexpr int kMaxChunk = 64;  // most consecutive edge steps per work item
+constexpr int kDefaultChunk = 4;
+constexpr int kTailItemsPerWarp = 16;  // single-step rounds once fewer items than this per warp remain
 
 enum Mode { MODE_CONFIGS = 0, MODE_FEASIBLE = 1, MODE_EDGES = 2 };
 
@@ -55,6 +59,7 @@ struct __align__(16) WarpSmem {
   uint32_t jobOff[kJobCap + 1];
   float T[kMaxLinks][12];
   float delta[kMaxLinks];     // per-link bound on |FP32 - exact| world coordinates
+  float gerr[kMaxLinks];      // per-link max |R^T R - I| of the FP32 rotation (+ rounding)
   double q64[kMaxLinks];      // canonical FP64 joint values (filled with T64)
   const float* item_qa;       // the item's joint values: configuration, or edge
   const float* item_qb;       //   endpoints qa/qb (item_qb null for configurations)
@@ -105,9 +110,11 @@ struct EngineArgs {
   unsigned int* head;
   uint2* spill;
   int spill_per_warp;
-  // work split (autotuned): items per queue grab, triangle-job flush size
+  // work split (autotuned): items per queue grab, triangle-job flush size,
+  // consecutive edge steps per work item
   int grab;
   int job_flush;
+  int chunk;
 };
 
 struct Cnt {
@@ -215,6 +222,39 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
   return false;
 }
 
+// Separation of two link boxes along their six face axes (the columns of the
+// two FP32 rotations), for self pairs: the world boxes of two rotated link
+// nodes are loose, and nearly parallel links would otherwise be traversed
+// down to most of their leaves.  Both boxes are the exact images of their
+// local boxes under the FP32 transforms; a column a has |a| <= 1 + g and
+// |a_i . a_k| <= g (i != k), so a box's projection onto its own axis i is at
+// most h_i + g (hx + hy + hz) and a gap along a overstates the Euclidean one
+// by at most the factor 1 + g.  16 u covers the rounding of the centres,
+// the products and the sums.
+__device__ __forceinline__ bool obb_separated(const float* TA, const float* TB, float4 hA, float4 hB, float3 cA,
+                                              float3 cB, float tol, float g)
+{
+  const float dx = cB.x - cA.x, dy = cB.y - cA.y, dz = cB.z - cA.z;
+  const float sa = hA.x + hA.y + hA.z, sb = hB.x + hB.y + hB.z;
+  const float slack = tol * (1.f + g) + 2.f * g * (sa + sb) +
+                      16.f * kU * (fabsf(cA.x) + fabsf(cA.y) + fabsf(cA.z) + fabsf(cB.x) + fabsf(cB.y) + fabsf(cB.z) +
+                                   sa + sb + 1e-3f);
+  float C[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j) C[i][j] = fabsf(TA[i] * TB[j] + TA[3 + i] * TB[3 + j] + TA[6 + i] * TB[6 + j]);
+  const float ha[3] = {hA.x, hA.y, hA.z}, hb[3] = {hB.x, hB.y, hB.z};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float pa = fabsf(TA[i] * dx + TA[3 + i] * dy + TA[6 + i] * dz);
+    if (pa > ha[i] + hb[0] * C[i][0] + hb[1] * C[i][1] + hb[2] * C[i][2] + slack) return true;
+    const float pb = fabsf(TB[i] * dx + TB[3 + i] * dy + TB[6 + i] * dz);
+    if (pb > hb[i] + ha[0] * C[0][i] + ha[1] * C[1][i] + ha[2] * C[2][i] + slack) return true;
+  }
+  return false;
+}
+
 // Node-pair test for one stack entry; returns 0 (culled), 1 (children in c0,
 // c1) or 2 (leaf job in jA, jB, jM).
 // box-test tolerance of a (link la, target tgt) pair: error bounds of both
@@ -246,7 +286,10 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
     Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z);
     Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z);
   }
-  if (!boxes_overlap(A, Bx, pair_tol(S, W, R, la, tgt))) return 0;
+  const float tol = pair_tol(S, W, R, la, tgt);
+  if (!boxes_overlap(A, Bx, tol)) return 0;
+  if (self && obb_separated(S.T[la], S.T[tgt], na.b, nb.b, A.c, Bx.c, tol, fmaxf(S.gerr[la], S.gerr[tgt])))
+    return 0;
   const int cntA = f2i(na.b.w), cntB = f2i(nb.b.w);
   const int ia = f2i(na.a.w), ib = f2i(nb.a.w);
   if (cntA > 0 && cntB > 0) {
@@ -394,9 +437,12 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
   Cnt cnt;
   unsigned long long items = 0;
   const int total = A.mode == MODE_EDGES ? A.meta[1] : A.B;
-  const int maxn = A.mode == MODE_EDGES ? A.meta[0] : 0;
+  const int maxn = A.mode == MODE_EDGES ? A.meta[0] : 0;  // last round index
   const int grab = A.grab >= 1 && A.grab <= 16 ? A.grab : kGrab;
   const int job_flush = A.job_flush >= 8 && A.job_flush <= kJobCap - 32 ? A.job_flush : kJobCap - 32;
+  const int chunk = A.chunk >= 1 && A.chunk <= kMaxChunk ? A.chunk : 1;
+  const int nchunked = A.mode == MODE_EDGES ? A.meta[2] : 0;
+  const int split = A.mode == MODE_EDGES ? A.meta[3] : 0;
 
 #pragma unroll 1
   for (;;) {
@@ -408,112 +454,127 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
     for (unsigned it = base; it < base + grab && it < (unsigned)total; ++it) {
       // ---- decode the item
       int rid = A.robot;
-      int b = (int)it, e = 0, k = 0, n = 0;
+      int b = (int)it, e = 0, k0 = 0, k1 = 0, n = 0;
       if (A.mode == MODE_EDGES) {
+        // rounds r < J: steps [r*chunk, r*chunk + chunk) of every edge that
+        // reaches r*chunk, checked in order; rounds r >= J: the single step
+        // split + (r - J)
         int lo = 0, hi = maxn;
         while (lo < hi) {
           int mid = (lo + hi + 1) >> 1;
           if (__ldg(A.round_off + mid) <= (int)it) lo = mid; else hi = mid - 1;
         }
-        k = lo;
-        e = __ldg(A.perm + ((int)it - __ldg(A.round_off + k)));
-        int fh = 0;
-        if (lane == 0) fh = *((volatile int*)(A.first_hit + e));
-        fh = __shfl_sync(0xffffffffu, fh, 0);
-        if (fh < k) continue;  // an earlier step of this edge already hit
+        e = __ldg(A.perm + ((int)it - __ldg(A.round_off + lo)));
         n = __ldg(A.nsteps + e);
+        if (n < 1 || n > kMaxSteps) n = 0;
+        if (lo < nchunked) {
+          k0 = lo * chunk;
+          k1 = min(k0 + chunk - 1, n);
+        } else {
+          k0 = k1 = split + (lo - nchunked);
+        }
       } else if (rid < 0) {
         rid = __ldg(A.robot_ids + b);
       }
-      const KRobotDev& R = W->robots[rid];
-      const int nl = R.nlinks;
-      // joint values in FP32 with an error bound e_q against the canonical
-      // FP64 values (exact for configurations; FMA interpolation for edges)
-      if (lane == 0) {
+#pragma unroll 1
+      for (int k = k0; k <= k1; ++k) {
         if (A.mode == MODE_EDGES) {
-          S.item_qa = A.qa + (size_t)e * nl;
-          S.item_qb = A.qb + (size_t)e * nl;
-        } else {
-          S.item_qa = A.q + (size_t)b * A.q_stride;
-          S.item_qb = nullptr;
+          int fh = 0;
+          if (lane == 0) fh = *((volatile int*)(A.first_hit + e));
+          fh = __shfl_sync(0xffffffffu, fh, 0);
+          if (fh < k) break;  // this or an earlier step of the edge already hit
         }
-        S.item_k = k;
-        S.item_n = n;
-      }
-      float q = 0.f, e_q = 0.f;
-      if (lane < nl) {
-        if (A.mode == MODE_EDGES) {
-          const float a = __ldg(A.qa + (size_t)e * nl + lane), bq = __ldg(A.qb + (size_t)e * nl + lane);
-          const float d = bq - a;
-          q = fmaf((float)k / (float)n, d, a);
-          e_q = kU * (fabsf(d) + fabsf(q) + fabsf(a)) * 1.01f + 1e-30f;
-        } else {
-          q = __ldg(A.q + (size_t)b * A.q_stride + lane);
-        }
-      }
-      __syncwarp();
-      items++;
-      const bool nonfinite = __any_sync(0xffffffffu, lane < nl && !(fabsf(q) < 1.0e6f));
-      if (nonfinite) {
-        if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
-        continue;
-      }
-      if (A.mode != MODE_CONFIGS) {
-        // joint limits: certain in FP32 away from the bounds, canonical FP64
-        // comparison (RobotCSpace.cpp:610-630) within rounding of them
-        bool unsure = false;
-        if (lane < nl) {
-          const float lo = R.qmin[lane], hi = R.qmax[lane];
-          const float tolq = e_q + 4.f * kU * (fabsf(q) + fmaxf(fabsf(lo), fabsf(hi))) + 1e-30f;
-          unsure = !((q - lo) > tolq && (hi - q) > tolq);
-        }
-        bool viol = false;
-        if (unsure) {
-          const double q64 = item_q64(S, lane);
-          viol = q64 < R.qmin64[lane] || q64 > R.qmax64[lane];
-        }
-        if (__any_sync(0xffffffffu, viol)) {
-          if (lane == 0) {
-            if (A.mode == MODE_EDGES) atomicMin(A.first_hit + e, k);
-            else A.feasible[b] = 0;
+        const KRobotDev& R = W->robots[rid];
+        const int nl = R.nlinks;
+        // joint values in FP32 with an error bound e_q against the canonical
+        // FP64 values (exact for configurations; FMA interpolation for edges)
+        if (lane == 0) {
+          if (A.mode == MODE_EDGES) {
+            S.item_qa = A.qa + (size_t)e * nl;
+            S.item_qb = A.qb + (size_t)e * nl;
+          } else {
+            S.item_qa = A.q + (size_t)b * A.q_stride;
+            S.item_qb = nullptr;
           }
+          S.item_k = k;
+          S.item_n = n;
+        }
+        float q = 0.f, e_q = 0.f;
+        if (lane < nl) {
+          if (A.mode == MODE_EDGES) {
+            const float a = __ldg(A.qa + (size_t)e * nl + lane), bq = __ldg(A.qb + (size_t)e * nl + lane);
+            const float d = bq - a;
+            q = fmaf((float)k / (float)n, d, a);
+            e_q = kU * (fabsf(d) + fabsf(q) + fabsf(a)) * 1.01f + 1e-30f;
+          } else {
+            q = __ldg(A.q + (size_t)b * A.q_stride + lane);
+          }
+        }
+        __syncwarp();
+        items++;
+        const bool nonfinite = __any_sync(0xffffffffu, lane < nl && !(fabsf(q) < 1.0e6f));
+        if (nonfinite) {
+          if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
           continue;
         }
-      }
-      float P[12], delta;
-      warp_fk32(R, lane, q, e_q, P, &delta);
-      if (lane < nl) {
-#pragma unroll
-        for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
-        S.delta[lane] = delta;
-      }
-      __syncwarp();
-      int env_res = TR_FREE, self_res = TR_FREE;
-      int fk64 = 0;
-      const bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
-      const bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
-      if (want_env && R.nqueries_env > 0)
-        env_res = traverse(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, job_flush,
-                           cnt);
-      const bool stop = A.mode != MODE_CONFIGS && env_res != TR_FREE;
-      if (!stop && want_self && R.nqueries_self > 0)
-        self_res = traverse(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill, spill_cap,
-                            T64, fk64, job_flush, cnt);
-      if (env_res == TR_OVERFLOW || self_res == TR_OVERFLOW) {
-        if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
-        continue;
-      }
-      if (lane == 0) {
-        if (A.mode == MODE_CONFIGS) {
-          if (A.env_hit) A.env_hit[b] = env_res == TR_HIT;
-          if (A.self_hit) A.self_hit[b] = self_res == TR_HIT;
-        } else if (A.mode == MODE_FEASIBLE) {
-          A.feasible[b] = (env_res == TR_FREE && self_res == TR_FREE) ? 1 : 0;
-        } else if (env_res == TR_HIT || self_res == TR_HIT) {
-          atomicMin(A.first_hit + e, k);
+        if (A.mode != MODE_CONFIGS) {
+          // joint limits: certain in FP32 away from the bounds, canonical FP64
+          // comparison (RobotCSpace.cpp:610-630) within rounding of them
+          bool unsure = false;
+          if (lane < nl) {
+            const float lo = R.qmin[lane], hi = R.qmax[lane];
+            const float tolq = e_q + 4.f * kU * (fabsf(q) + fmaxf(fabsf(lo), fabsf(hi))) + 1e-30f;
+            unsure = !((q - lo) > tolq && (hi - q) > tolq);
+          }
+          bool viol = false;
+          if (unsure) {
+            const double q64 = item_q64(S, lane);
+            viol = q64 < R.qmin64[lane] || q64 > R.qmax64[lane];
+          }
+          if (__any_sync(0xffffffffu, viol)) {
+            if (lane == 0) {
+              if (A.mode == MODE_EDGES) atomicMin(A.first_hit + e, k);
+              else A.feasible[b] = 0;
+            }
+            continue;
+          }
         }
-      }
-      __syncwarp();
+        float P[12], delta;
+        warp_fk32(R, lane, q, e_q, P, &delta);
+        if (lane < nl) {
+#pragma unroll
+          for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
+          S.delta[lane] = delta;
+          S.gerr[lane] = rot_gram_err32(P);
+        }
+        __syncwarp();
+        int env_res = TR_FREE, self_res = TR_FREE;
+        int fk64 = 0;
+        const bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
+        const bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
+        if (want_env && R.nqueries_env > 0)
+          env_res = traverse(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, job_flush,
+                             cnt);
+        const bool stop = A.mode != MODE_CONFIGS && env_res != TR_FREE;
+        if (!stop && want_self && R.nqueries_self > 0)
+          self_res = traverse(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill, spill_cap,
+                              T64, fk64, job_flush, cnt);
+        if (env_res == TR_OVERFLOW || self_res == TR_OVERFLOW) {
+          if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
+          continue;
+        }
+        if (lane == 0) {
+          if (A.mode == MODE_CONFIGS) {
+            if (A.env_hit) A.env_hit[b] = env_res == TR_HIT;
+            if (A.self_hit) A.self_hit[b] = self_res == TR_HIT;
+          } else if (A.mode == MODE_FEASIBLE) {
+            A.feasible[b] = (env_res == TR_FREE && self_res == TR_FREE) ? 1 : 0;
+          } else if (env_res == TR_HIT || self_res == TR_HIT) {
+            atomicMin(A.first_hit + e, k);
+          }
+        }
+        __syncwarp();
+      }  // steps of the item
     }
   }
   unsigned long long np = cnt.node_pairs, tp = cnt.tri_pairs, bd = cnt.band;
@@ -535,6 +596,16 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
 }
 
 // ---- edge preparation ------------------------------------------------------
+// Work items of an edge batch.  Edges are sorted by descending step count n
+// (perm), so the edges with n >= s are exactly perm[0, count_ge[s]).  The
+// steps are grouped in rounds: while much work remains, a round is a chunk of
+// `chunk` consecutive steps [r*chunk, r*chunk + chunk) of every edge that
+// reaches it (one work item per edge, its steps checked in order); from step
+// S_split on, a round is one step, so that the last items in the queue are
+// short and the launch does not end on one warp's long chunk.  S_split is
+// the first multiple of `chunk` from which fewer than `tail_items` items
+// remain.  meta: [0] last round index, [1] total items, [2] number of chunked
+// rounds J, [3] S_split (= J * chunk).
 __global__ void k_edges_prep1(const int* nsteps, int E, int* hist, int* meta, int* first_hit,
                               int* status)
 {
@@ -567,54 +638,77 @@ __device__ __forceinline__ long long block_scan_incl(long long v, long long* sh)
   return r;
 }
 
-// One block of 1024 threads.  count_ge[v] = edges with n >= v (suffix sum of
-// the histogram); hist[v] becomes the base position of the edges with n == v
-// in the descending-n order (= count_ge[v+1]); round_off[k] = number of items
-// in rounds < k (prefix sum of count_ge); meta[1] = total items.
-__global__ void __launch_bounds__(1024) k_edges_prep2(int* hist, int* round_off, int* meta, int* status)
+// One block of 1024 threads.  hist[v] (edges with n == v) becomes the base
+// position of those edges in perm (= count_ge[v+1]); cge[v] = count_ge[v];
+// round_off[r] = items in rounds < r.
+__global__ void __launch_bounds__(1024) k_edges_prep2(int* hist, int* cge, int* round_off, int* meta, int* status,
+                                                      int chunk, long long tail_items)
 {
   __shared__ long long sh[1024];
+  __shared__ int s_star;
   const int t = threadIdx.x;
   const int maxn = meta[0];
   const int len = maxn + 1;
-  const int chunk = (len + 1023) / 1024;
-  // suffix sums: thread t owns bins [t*chunk, (t+1)*chunk) counted from the top
+  const int per = (len + 1023) / 1024;
+  // suffix sums of the histogram: thread t owns steps [maxn - (t+1)*per, maxn - t*per)
   long long local = 0;
-  for (int i = 0; i < chunk; ++i) {
-    int v = maxn - (t * chunk + i);
+  for (int i = 0; i < per; ++i) {
+    const int v = maxn - (t * per + i);
     if (v >= 0) local += hist[v];
   }
-  long long before = block_scan_incl(local, sh) - local;  // edges with larger n
-  long long run = before;
-  for (int i = 0; i < chunk; ++i) {
-    int v = maxn - (t * chunk + i);
+  long long run = block_scan_incl(local, sh) - local;  // edges with larger n
+  for (int i = 0; i < per; ++i) {
+    const int v = maxn - (t * per + i);
     if (v >= 0) {
-      int h = hist[v];
+      const int h = hist[v];
       hist[v] = (int)run;  // base = count_ge[v+1]
       run += h;
-      round_off[v + 1] = (int)run;  // count_ge[v], scanned below
+      cge[v] = (int)run;   // count_ge[v]
     }
   }
+  if (t == 0) s_star = len;
   __syncthreads();
-  // prefix sums of count_ge over k = 0..maxn, thread t owns [t*chunk, ...)
+  // items remaining from step v on: rem(v) = sum of count_ge over [v, maxn];
+  // S* = the first v with rem(v) < tail_items (rem is non-increasing)
   local = 0;
-  for (int i = 0; i < chunk; ++i) {
-    int k = t * chunk + i;
-    if (k <= maxn) local += round_off[k + 1];
+  for (int i = 0; i < per; ++i) {
+    const int v = maxn - (t * per + i);
+    if (v >= 0) local += cge[v];
   }
-  __syncthreads();
-  long long acc = block_scan_incl(local, sh) - local;
-  for (int i = 0; i < chunk; ++i) {
-    int k = t * chunk + i;
-    if (k <= maxn) {
-      acc += round_off[k + 1];
-      round_off[k + 1] = acc > INT_MAX ? INT_MAX : (int)acc;
+  long long rem = block_scan_incl(local, sh) - local;
+  for (int i = 0; i < per; ++i) {
+    const int v = maxn - (t * per + i);
+    if (v >= 0) {
+      rem += cge[v];
+      if (rem < tail_items) atomicMin(&s_star, v);
     }
   }
-  if (t == 0) round_off[0] = 0;
+  __syncthreads();
+  const int J = s_star / chunk;            // chunked rounds cover steps [0, J*chunk)
+  const int split = J * chunk;
+  const int rounds = J + (len - split);    // then one round per step up to maxn
+  const int rper = (rounds + 1023) / 1024;
+  // prefix sums of the round sizes; thread t owns rounds [t*rper, (t+1)*rper)
+  local = 0;
+  for (int i = 0; i < rper; ++i) {
+    const int r = t * rper + i;
+    if (r < rounds) local += cge[r < J ? r * chunk : split + (r - J)];
+  }
+  long long acc = block_scan_incl(local, sh) - local;
+  for (int i = 0; i < rper; ++i) {
+    const int r = t * rper + i;
+    if (r < rounds) {
+      round_off[r] = acc > INT_MAX ? INT_MAX : (int)acc;
+      acc += cge[r < J ? r * chunk : split + (r - J)];
+    }
+  }
   if (t == 1023) {
     if (acc > INT_MAX) atomicCAS(status, 0, KGPU_ERR_INVALID);
+    round_off[rounds] = acc > INT_MAX ? INT_MAX : (int)acc;
+    meta[0] = rounds - 1;
     meta[1] = acc > INT_MAX ? INT_MAX : (int)acc;
+    meta[2] = J;
+    meta[3] = split;
   }
 }
 
@@ -730,7 +824,7 @@ cudaError_t launch_check_configs(const KWorldDev* W, const Scratch& S, int robot
 
 cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S, int robot, const float* qa,
                                const float* qb, const int* nsteps, int E, int* first_hit, int blocks,
-                               int per_sm, cudaStream_t s, int grab, int job_flush)
+                               int per_sm, cudaStream_t s, int grab, int job_flush, int chunk)
 {
   if (E <= 0) return cudaSuccess;
   cudaError_t err;
@@ -740,13 +834,17 @@ cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S
   int* fill = S.edge_meta + 4;  // kMaxSteps+2 ints after the meta words
   if ((err = cudaMemsetAsync(fill, 0, sizeof(int) * (kMaxSteps + 2), s)) != cudaSuccess) return err;
   int tb = 256, gb = (E + tb - 1) / tb;
+  chunk = chunk >= 1 && chunk <= kMaxChunk ? chunk : kDefaultChunk;
+  int* cge = fill + kMaxSteps + 2;  // count_ge table after the fill counters
+  const long long tail_items = (long long)kTailItemsPerWarp * blocks * kWarps;
   k_edges_prep1<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, S.edge_meta, first_hit, status);
-  k_edges_prep2<<<1, 1024, 0, s>>>(S.edge_hist, S.edge_round_off, S.edge_meta, status);
+  k_edges_prep2<<<1, 1024, 0, s>>>(S.edge_hist, cge, S.edge_round_off, S.edge_meta, status, chunk, tail_items);
   k_edges_prep3<<<gb, tb, 0, s>>>(nsteps, E, S.edge_hist, fill, S.edge_perm);
   if ((err = cudaGetLastError()) != cudaSuccess) return err;
   EngineArgs A = {};
   A.grab = grab;
   A.job_flush = job_flush;
+  A.chunk = chunk;
   A.mode = MODE_EDGES;
   A.robot = robot;
   A.qa = qa;

@@ -54,6 +54,15 @@ constexpr float kU = 5.9604645e-08f;  // unit roundoff of FP32, 2^-24
 // arguments reduce in FP64), then the Taylor series of sin to r^9 and cos to
 // r^10 on |r| <= pi/4 (truncation < 2e-9).  |error| <= kSinCosErr.
 constexpr float kSinCosErr = 4.0f * kU;
+// argument reduction for |x| >= 4096 in FP64 (out of line: never on the hot
+// path, and its code would otherwise sit inside every caller's loop)
+static __device__ __noinline__ float2 sincos32_reduce_big(float x)
+{
+  const double kd = rint((double)x * 0.6366197723675814);
+  const float r = (float)(((double)x - kd * 1.5707963267948966) - kd * 6.123233995736766e-17);
+  return make_float2(r, (float)fmod(kd, 4.0));
+}
+
 __device__ __forceinline__ void sincos32(float x, float* s, float* c)
 {
   float k, r;
@@ -61,9 +70,9 @@ __device__ __forceinline__ void sincos32(float x, float* s, float* c)
     k = rintf(x * 0.63661975f);
     r = fmaf(-k, -8.705516e-10f, fmaf(-k, -4.4535846e-06f, fmaf(-k, 1.57080078125f, x)));
   } else {
-    double kd = rint((double)x * 0.6366197723675814);
-    r = (float)(((double)x - kd * 1.5707963267948966) - kd * 6.123233995736766e-17);
-    k = (float)fmod(kd, 4.0);
+    const float2 rk = sincos32_reduce_big(x);
+    r = rk.x;
+    k = rk.y;
   }
   float r2 = r * r;
   float ps = fmaf(fmaf(fmaf(fmaf(2.7557319e-06f, r2, -1.98412698e-04f), r2, 8.33333333e-03f), r2,
@@ -181,6 +190,21 @@ __device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, float q,
 }
 
 // ---- boxes -------------------------------------------------------------
+// max |R^T R - I| over the entries for the rotation rows P[0..8] of an FP32
+// transform, plus 8 u for the rounding of the Gram products
+__device__ __forceinline__ float rot_gram_err32(const float* P)
+{
+  float g = 0.f;
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = i; j < 3; ++j) {
+      const float v = P[i] * P[j] + P[3 + i] * P[3 + j] + P[6 + i] * P[6 + j];
+      g = fmaxf(g, fabsf(i == j ? v - 1.f : v));
+    }
+  return g + 8.f * kU;
+}
+
 struct Box32 {
   float3 c, h;
 };
@@ -265,14 +289,15 @@ __device__ __forceinline__ bool tri_separated32(const float3* P, const float3* Q
   const float3 eq0 = sub3(q[1], q[0]), eq1 = sub3(q[2], q[1]), eq2 = sub3(q[0], q[2]);
   const float3 np = cross3(ep0, ep1);
   const float3 nq = cross3(eq0, eq1);
-  if (sep_axis32(np, p, q, eps, margin)) return true;
-  if (sep_axis32(nq, p, q, eps, margin)) return true;
+  // one rolled loop over the 17 axes: the two face normals first (the most
+  // frequent separators), then edge x edge, then the in-plane axes
 #pragma unroll 1
-  for (int k = 0; k < 15; ++k) {
+  for (int k = 0; k < 17; ++k) {
     float3 a;
-    if (k < 9) a = cross3(sel3(k / 3, ep0, ep1, ep2), sel3(k % 3, eq0, eq1, eq2));
-    else if (k < 12) a = cross3(np, sel3(k - 9, ep0, ep1, ep2));
-    else a = cross3(nq, sel3(k - 12, eq0, eq1, eq2));
+    if (k < 2) a = k == 0 ? np : nq;
+    else if (k < 11) a = cross3(sel3((k - 2) / 3, ep0, ep1, ep2), sel3((k - 2) % 3, eq0, eq1, eq2));
+    else if (k < 14) a = cross3(np, sel3(k - 11, ep0, ep1, ep2));
+    else a = cross3(nq, sel3(k - 14, eq0, eq1, eq2));
     if (sep_axis32(a, p, q, eps, margin)) return true;
   }
   return false;

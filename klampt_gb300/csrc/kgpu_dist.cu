@@ -114,6 +114,10 @@ __device__ __forceinline__ float warp_min(float v)
 }
 
 // ---- FP32 triangle distance (value only; features come from FP64) --------
+// The parameters use the fast reciprocal divide (__fdividef): a parameter off
+// by a few ulp moves the evaluated points along their segments by a few ulp of
+// the edge length, well inside the 128 u x span band the callers allow for the
+// FP32 value (at an interior optimum the error is even second order).
 __device__ __forceinline__ float clamp01f(float x) { return fminf(1.f, fmaxf(0.f, x)); }
 
 __device__ float seg_seg2_32(float3 p1, float3 d1, float3 p2, float3 d2)
@@ -124,18 +128,18 @@ __device__ float seg_seg2_32(float3 p1, float3 d1, float3 p2, float3 d2)
   if (a <= 1e-30f && e <= 1e-30f) {
     s = 0.f; t = 0.f;
   } else if (a <= 1e-30f) {
-    s = 0.f; t = clamp01f(f / e);
+    s = 0.f; t = clamp01f(__fdividef(f, e));
   } else {
     const float c = dot3(d1, r);
     if (e <= 1e-30f) {
-      t = 0.f; s = clamp01f(-c / a);
+      t = 0.f; s = clamp01f(__fdividef(-c, a));
     } else {
       const float b = dot3(d1, d2);
       const float den = a * e - b * b;
-      s = den > 0.f ? clamp01f((b * f - c * e) / den) : 0.f;
-      t = (b * s + f) / e;
-      if (t < 0.f) { t = 0.f; s = clamp01f(-c / a); }
-      else if (t > 1.f) { t = 1.f; s = clamp01f((b - c) / a); }
+      s = den > 0.f ? clamp01f(__fdividef(b * f - c * e, den)) : 0.f;
+      t = __fdividef(b * s + f, e);
+      if (t < 0.f) { t = 0.f; s = clamp01f(__fdividef(-c, a)); }
+      else if (t > 1.f) { t = 1.f; s = clamp01f(__fdividef(b - c, a)); }
     }
   }
   const float3 w = make_float3(r.x + d1.x * s - d2.x * t, r.y + d1.y * s - d2.y * t, r.z + d1.z * s - d2.z * t);
@@ -154,7 +158,7 @@ __device__ float pt_tri2_32(float3 p, float3 a, float3 b, float3 c)
     if (d3 >= 0.f && d4 <= d3) { q = b; goto done; }
     const float vc = d1 * d4 - d3 * d2;
     if (vc <= 0.f && d1 >= 0.f && d3 <= 0.f) {
-      const float v = d1 / (d1 - d3);
+      const float v = __fdividef(d1, d1 - d3);
       q = make_float3(a.x + ab.x * v, a.y + ab.y * v, a.z + ab.z * v);
       goto done;
     }
@@ -163,17 +167,17 @@ __device__ float pt_tri2_32(float3 p, float3 a, float3 b, float3 c)
     if (d6 >= 0.f && d5 <= d6) { q = c; goto done; }
     const float vb = d5 * d2 - d1 * d6;
     if (vb <= 0.f && d2 >= 0.f && d6 <= 0.f) {
-      const float w = d2 / (d2 - d6);
+      const float w = __fdividef(d2, d2 - d6);
       q = make_float3(a.x + ac.x * w, a.y + ac.y * w, a.z + ac.z * w);
       goto done;
     }
     const float va = d3 * d6 - d5 * d4;
     if (va <= 0.f && (d4 - d3) >= 0.f && (d5 - d6) >= 0.f) {
-      const float w = (d4 - d3) / ((d4 - d3) + (d5 - d6));
+      const float w = __fdividef(d4 - d3, (d4 - d3) + (d5 - d6));
       q = make_float3(b.x + (c.x - b.x) * w, b.y + (c.y - b.y) * w, b.z + (c.z - b.z) * w);
       goto done;
     }
-    const float den = 1.f / (va + vb + vc);
+    const float den = __fdividef(1.f, va + vb + vc);
     const float v = vb * den, w = vc * den;
     q = make_float3(a.x + ab.x * v + ac.x * w, a.y + ab.y * v + ac.y * w, a.z + ab.z * v + ac.z * w);
   }
@@ -268,6 +272,32 @@ __device__ __noinline__ void flush_cands(DistSmem& S, const KWorldDev* __restric
     }
     __syncwarp();
   }
+}
+
+// Lower bound on the distance of two triangles from the separating direction
+// through their centroids (projections onto a unit vector are 1-Lipschitz);
+// nearly tight for facing triangles, which the box bound is not.  The FP32
+// rounding of the centroids, the normalisation and the projections is
+// covered by the (1 - 8u) factor and the 16 u span term.
+__device__ __forceinline__ float tri_axis_lb32(const float3* P, const float3* Q, float span)
+{
+  const float k3 = 1.f / 3.f;
+  const float3 cP = make_float3((P[0].x + P[1].x + P[2].x) * k3, (P[0].y + P[1].y + P[2].y) * k3,
+                                (P[0].z + P[1].z + P[2].z) * k3);
+  const float3 cQ = make_float3((Q[0].x + Q[1].x + Q[2].x) * k3, (Q[0].y + Q[1].y + Q[2].y) * k3,
+                                (Q[0].z + Q[1].z + Q[2].z) * k3);
+  float3 u = sub3(cQ, cP);
+  const float nn = sqrtf(dot3(u, u));
+  if (!(nn > 1e-20f)) return 0.f;
+  const float inv = 1.f / nn;
+  u = make_float3(u.x * inv, u.y * inv, u.z * inv);
+  float pm = -FLT_MAX, qm = FLT_MAX;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    pm = fmaxf(pm, dot3(sub3(P[k], cP), u));
+    qm = fminf(qm, dot3(sub3(Q[k], cP), u));
+  }
+  return (qm - pm) * (1.f - 8.f * kU) - 16.f * kU * span;
 }
 
 struct PairOut {
@@ -369,7 +399,8 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
           const float gy = fmaxf(0.f, fmaxf(ql.y - ph.y, pl.y - qh.y));
           const float gz = fmaxf(0.f, fmaxf(ql.z - ph.z, pl.z - qh.z));
           const float blb = sqrtf(gx * gx + gy * gy + gz * gz) * (1.f - 4.f * kU);
-          if (blb - e > fminf(m32 * (1.f + 2e-5f) + 2.f * e, fb + e)) {
+          const float skip = fminf(m32 * (1.f + 2e-5f) + 2.f * e, fb + e);
+          if (blb - e > skip || tri_axis_lb32(P, Q, span) - e > skip) {
             d32 = FLT_MAX;  // not a candidate (and no better than the running minimum)
           } else if (!tri_separated32(P, Q, dl + de, 0.f)) {
             d32 = 0.f;
@@ -410,8 +441,12 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
       if (overlap) break;
       continue;
     }
-    // ---- node pairs
-    const int n = min(top, 32);
+    // ---- node pairs.  A batch of n pops grows the stack by at most n; near
+    // the capacity the batch narrows down to plain depth-first order (one
+    // pair), whose growth is bounded by the depth of the two trees, so a
+    // wide front (a link deep inside an obstacle, where no box is pruned)
+    // does not overflow the stack
+    const int n = min(min(top, 32), max(1, kDStack - 64 - top));
     const bool have = lane < n;
     uint2 en = make_uint2(0, 0);
     if (have) en = S.stack[top - 1 - lane];

@@ -128,7 +128,7 @@ struct Scratch {
   int* edge_hist = nullptr;          // kMaxSteps+2
   int* edge_round_off = nullptr;     // kMaxSteps+2
   int* edge_perm = nullptr;
-  int* edge_meta = nullptr;          // [0] max n, [1] total items
+  int* edge_meta = nullptr;          // 4 meta words, fill counters, count_ge (2 x (kMaxSteps+2))
   size_t edge_cap = 0;
   double* dist_work = nullptr;       // soft-min per-waypoint minima, sums, trajectory minima
   size_t dist_work_cap = 0;
@@ -213,6 +213,7 @@ struct kgpu_world_s {
   int blocks_per_sm = 3;   // resident 8-warp engine blocks per SM (2, 3 or 4)
   int grab = 2;            // work items per queue atomic (1..16)
   int job_flush = 64;      // triangle-pair jobs collected before testing them (8..64)
+  int edge_chunk = 4;      // consecutive steps of an edge per work item (1..64)
   int num_sms = 0;
   bool tables_dirty = true;
   // pinned staging for the host-buffer entry points
@@ -245,7 +246,7 @@ cudaError_t launch_check_configs(const KWorldDev* Wd, const Scratch& S, int robo
 cudaError_t launch_check_edges(const KWorldDev* Wd, int* status, const Scratch& S, int robot,
                                const float* qa, const float* qb, const int* nsteps, int E,
                                int* first_hit, int blocks, int per_sm, cudaStream_t s,
-                               int grab = 0, int job_flush = 0);
+                               int grab = 0, int job_flush = 0, int chunk = 0);
 cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q, int B,
                                    uint8_t* env_hit, uint8_t* self_hit, cudaStream_t s);
 cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,

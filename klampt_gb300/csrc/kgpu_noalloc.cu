@@ -54,7 +54,7 @@ Layout layout()
   L.counters = o; o = align256(o + 64 * sizeof(unsigned int));
   L.hist = o; o = align256(o + (kgpu::kMaxSteps + 2) * sizeof(int));
   L.round_off = o; o = align256(o + (kgpu::kMaxSteps + 2) * sizeof(int));
-  L.meta = o; o = align256(o + (4 + kgpu::kMaxSteps + 2) * sizeof(int));
+  L.meta = o; o = align256(o + (4 + 2 * (kgpu::kMaxSteps + 2)) * sizeof(int));
   L.perm = o; o = align256(o + (size_t)KGPU_NOALLOC_MAX_EDGES * sizeof(int));
   L.per_warp_entries = (size_t)kgpu::engine_scratch_doubles() + kNoAllocSpill;  // uint2 entries
   L.warps = o; o = align256(o + (size_t)kNoAllocMaxWarps * L.per_warp_entries * sizeof(uint2));
