@@ -156,7 +156,11 @@ kgpu_status kgpu_world_enable_self_pair(kgpu_world world, int32_t robot, int32_t
  * resident engine blocks per SM), "grab" (work items per queue atomic, 1..16),
  * "job_flush" (triangle-pair jobs batched before testing, 8..64),
  * "edge_chunk" (consecutive steps of an edge checked in order by one work
- * item, 1..64, default 4), read-only
+ * item, 1..64, default 4), "fp64_inline" (1: triangle pairs the FP32 tests
+ * leave undecided get the FP64 test inside the traversal kernel; 0: they are
+ * listed and decided by a second kernel, keeping FP64 code out of the
+ * traversal kernel; -1, the default: 0 for edge batches, 1 for configuration
+ * batches), read-only
  * "eps_env", "warps_per_block", "num_sms".  The autotuner
  * (klampt_gb300/autotune.py) sets blocks_per_sm, grab and job_flush.
  * Unknown names are KGPU_ERR_INVALID. */

@@ -5,6 +5,10 @@ Tries, on a sample of the caller's own workload, every combination of
                             of the engine instantiation: 128 / 80 / 64)
   grab           1, 2, 4   (work items a warp takes per queue atomic)
   job_flush      32, 64    (triangle-pair jobs collected before testing)
+  fp64_inline    0, 1      (FP64 triangle tests deferred to a second kernel,
+                            or inline in the traversal)
+and, for edge batches,
+  edge_chunk     2, 4, 8   (consecutive steps of an edge per work item)
 times each with CUDA events (best of `reps` after one warm-up) and leaves the
 fastest setting in the world.  Results are identical for every setting; only
 the time changes.
@@ -19,7 +23,8 @@ import torch
 
 from .engine import World
 
-GRID = {"blocks_per_sm": (2, 3, 4), "grab": (1, 2, 4), "job_flush": (32, 64)}
+GRID = {"blocks_per_sm": (2, 3, 4), "grab": (1, 2, 4), "job_flush": (32, 64), "fp64_inline": (0, 1)}
+GRID_EDGES = dict(GRID, edge_chunk=(2, 4, 8))
 
 
 def _time(fn: Callable[[], None], reps: int) -> float:
@@ -37,12 +42,13 @@ def _time(fn: Callable[[], None], reps: int) -> float:
     return best
 
 
-def tune(world: World, run: Callable[[], None], reps: int = 3) -> Tuple[Dict[str, int], List[Tuple[Dict[str, int], float]]]:
+def tune(world: World, run: Callable[[], None], reps: int = 3,
+         grid: Dict[str, tuple] = GRID) -> Tuple[Dict[str, int], List[Tuple[Dict[str, int], float]]]:
     """Times `run` (a closure launching the workload on `world`) under every
-    setting; applies and returns the best plus the full table (ms)."""
+    setting of `grid`; applies and returns the best plus the full table (ms)."""
     table = []
-    keys = list(GRID)
-    for values in itertools.product(*(GRID[k] for k in keys)):
+    keys = list(grid)
+    for values in itertools.product(*(grid[k] for k in keys)):
         cfg = dict(zip(keys, values))
         for k, v in cfg.items():
             world.set_option(k, v)
@@ -58,7 +64,7 @@ def tune_edges(world: World, qa, qb, nsteps, robot: int = 0, reps: int = 3):
     a = torch.as_tensor(qa).cuda()
     b = torch.as_tensor(qb).cuda()
     n = torch.as_tensor(nsteps).cuda()
-    return tune(world, lambda: world.check_edges(a, b, n, robot=robot, sync=False), reps)
+    return tune(world, lambda: world.check_edges(a, b, n, robot=robot, sync=False), reps, GRID_EDGES)
 
 
 def tune_configs(world: World, q, robot: int = 0, reps: int = 3):

@@ -142,6 +142,7 @@ void free_world_device(kgpu_world w)
   dfree(w->d_stats);
   dfree(w->scratch.spill);
   dfree(w->scratch.counters);
+  dfree(w->scratch.pend);
   dfree(w->scratch.edge_hist);
   dfree(w->scratch.edge_round_off);
   dfree(w->scratch.edge_perm);
@@ -616,6 +617,8 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   S.spill_per_warp = 8192;
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.spill, (size_t)S.max_warps * S.spill_per_warp * sizeof(uint2));
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.counters, 64 * sizeof(unsigned int));
+  S.pend_cap = 1 << 18;
+  if (e == cudaSuccess) e = cudaMalloc((void**)&S.pend, (size_t)S.pend_cap * sizeof(uint4));
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_hist, (kMaxSteps + 2) * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_round_off, (kMaxSteps + 2) * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc((void**)&S.edge_meta, (4 + 2 * (kMaxSteps + 2)) * sizeof(int));
@@ -729,6 +732,10 @@ kgpu_status kgpu_world_set_option(kgpu_world w, const char* name, double v)
     int k = (int)v;
     if (k < 8 || k > 64) return fail(KGPU_ERR_INVALID, "job_flush must be in [8,64]");
     w->job_flush = k;
+  } else if (!strcmp(name, "fp64_inline")) {
+    int k = (int)v;
+    if (k < -1 || k > 1) return fail(KGPU_ERR_INVALID, "fp64_inline must be -1, 0 or 1");
+    w->fp64_inline = k;
   } else if (!strcmp(name, "edge_chunk")) {
     int k = (int)v;
     if (k < 1 || k > 64) return fail(KGPU_ERR_INVALID, "edge_chunk must be in [1,64]");
@@ -751,6 +758,7 @@ kgpu_status kgpu_world_get_option(kgpu_world w, const char* name, double* v)
   else if (!strcmp(name, "grab")) *v = w->grab;
   else if (!strcmp(name, "job_flush")) *v = w->job_flush;
   else if (!strcmp(name, "edge_chunk")) *v = w->edge_chunk;
+  else if (!strcmp(name, "fp64_inline")) *v = w->fp64_inline;
   else if (!strcmp(name, "num_sms")) *v = w->num_sms;
   else return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
   return KGPU_OK;
@@ -818,7 +826,7 @@ kgpu_status kgpu_check_configs(kgpu_world w, int32_t robot, const float* q, int3
   if (!env_hit && !self_hit) return KGPU_OK;
   return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
                                             env_hit, self_hit, nullptr, grid_blocks(w), w->blocks_per_sm,
-                                            (cudaStream_t)s, w->grab, w->job_flush),
+                                            (cudaStream_t)s, w->grab, w->job_flush, w->fp64_inline),
                        "kgpu_check_configs");
 }
 
@@ -836,7 +844,7 @@ kgpu_status kgpu_check_configs_multi(kgpu_world w, const int32_t* robot_ids, con
   if (!env_hit && !self_hit) return KGPU_OK;
   return launch_status(launch_check_configs(w->d_dev, w->scratch, -1, robot_ids, q, q_stride, B, env_hit, self_hit,
                                             nullptr, grid_blocks(w), w->blocks_per_sm, (cudaStream_t)s, w->grab,
-                                            w->job_flush),
+                                            w->job_flush, w->fp64_inline),
                        "kgpu_check_configs_multi");
 }
 
@@ -848,7 +856,7 @@ kgpu_status kgpu_is_feasible(kgpu_world w, int32_t robot, const float* q, int32_
   if (B < 0 || (B > 0 && (!q || !feasible))) return fail(KGPU_ERR_INVALID, "bad buffers");
   return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
                                             nullptr, nullptr, feasible, grid_blocks(w), w->blocks_per_sm,
-                                            (cudaStream_t)s, w->grab, w->job_flush),
+                                            (cudaStream_t)s, w->grab, w->job_flush, w->fp64_inline),
                        "kgpu_is_feasible");
 }
 
@@ -860,7 +868,8 @@ kgpu_status kgpu_check_edges(kgpu_world w, int32_t robot, const float* qa, const
   if (E < 0 || (E > 0 && (!qa || !qb || !nsteps || !first_hit))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if ((st = ensure_edge_scratch(w, E))) return st;
   return launch_status(launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
-                                          w->blocks_per_sm, (cudaStream_t)s, w->grab, w->job_flush, w->edge_chunk),
+                                          w->blocks_per_sm, (cudaStream_t)s, w->grab, w->job_flush, w->edge_chunk,
+                                          w->fp64_inline),
                        "kgpu_check_edges");
 }
 
@@ -1005,7 +1014,7 @@ kgpu_status kgpu_edge_plan_create(kgpu_world w, int32_t robot, const float* qa, 
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
     cudaError_t le = launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
-                                        w->blocks_per_sm, cs, w->grab, w->job_flush, w->edge_chunk);
+                                        w->blocks_per_sm, cs, w->grab, w->job_flush, w->edge_chunk, w->fp64_inline);
     e = cudaStreamEndCapture(cs, &p->graph);
     if (e == cudaSuccess && le != cudaSuccess) e = le;
   }

@@ -64,7 +64,25 @@ struct __align__(16) WarpSmem {
   const float* item_qa;       // the item's joint values: configuration, or edge
   const float* item_qb;       //   endpoints qa/qb (item_qb null for configurations)
   int item_k, item_n;         // edge step k of n
+  int item_id;                // configuration index b, or edge index e
+  int item_rid;               // robot of the item
+  int don_top;                // stack entries handed over by a sibling warp
 };
+
+// Work sharing inside a block once the queue is drained (edge batches, whose
+// long items would otherwise end the launch on one warp; a contact found by
+// any part settles the step through first_hit): a warp with nothing
+// left sets flag 0 (waiting) and counts itself in `idle`; a sibling whose
+// traversal stack is deep claims it (flag 0 -> 3), copies the item context and
+// the bottom half of its stack into the waiting warp's shared memory and
+// releases it (flag 1).  A waiting warp leaves (flag 0 -> 4, so it can no
+// longer be claimed) once every warp of the block waits.  Flag 2: busy.
+struct BlockShare {
+  int idle;
+  int flag[kWarps];
+};
+constexpr int kDonateMin = 64;     // stack entries a warp needs before it shares
+constexpr int kShareSpins = 1 << 20;  // bound on a waiting warp's polls (~0.3 s)
 
 // canonical FP64 joint values of the current item (lane < nl), as the oracle
 // forms them: float input widened, or the FP64 edge interpolation
@@ -115,6 +133,12 @@ struct EngineArgs {
   int grab;
   int job_flush;
   int chunk;
+  // deferred FP64 re-tests: triangle pairs the FP32 tests left undecided,
+  // {item (b or e), k | la << 16 | tgt << 21, tA, tB}
+  uint4* pend;
+  unsigned int* pend_count;
+  int pend_cap;
+  int inline64;          // 1: one pass with the FP64 test inline (no list)
 };
 
 struct Cnt {
@@ -132,10 +156,16 @@ __device__ __forceinline__ uint2 make_entry(int nodeA, int la, int tgt, int node
 // Tests the triangle-pair jobs of the warp, one triangle pair per lane;
 // returns true on a confirmed contact.  Per pair: FP32 separating-axis filter
 // (separated beyond the band: done), FP32 intersection certificate (crossing
-// beyond the band: contact), otherwise the FP64 re-test on transforms
-// computed once per configuration (fk64 tracks whether S.T64 is valid).
+// beyond the band: contact), otherwise the pair is undecided in FP32.  The
+// main pass (FP64 = false) appends such a pair to A.pend and goes on (k_band
+// decides it afterwards); the fallback pass (FP64 = true) decides it here
+// with the FP64 test on transforms computed once per configuration (fk64
+// tracks whether T64 is valid).  Keeping the FP64 code out of the main
+// pass's kernel keeps that kernel's hot loop in the instruction cache.
+template <bool FP64>
 __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
-                                      int njobs, int lane, double (*T64)[12], int& fk64, Cnt& cnt)
+                                      int njobs, int lane, double (*T64)[12], int& fk64, const EngineArgs& A,
+                                      Cnt& cnt)
 {
   // exclusive prefix over job sizes
   uint32_t carry = 0;
@@ -207,15 +237,25 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
     }
     const bool need64 = band && !certain;
     if (__any_sync(0xffffffffu, need64)) {
-      ensure_fk64(S, R, T64, lane, fk64);
-      int hit = 0;
-      if (need64) {
-        cnt.band++;
-        hit = band_retest(W, R, T64, la, tA, tgt, tB);
-      }
-      if (__any_sync(0xffffffffu, hit)) {
-        cnt.hit64++;
-        return true;
+      if (!FP64) {
+        const unsigned m = __ballot_sync(0xffffffffu, need64);
+        unsigned at = 0;
+        if (lane == 0) at = atomicAdd(A.pend_count, (unsigned)__popc(m));
+        at = __shfl_sync(0xffffffffu, at, 0) + __popc(m & lanemask_lt());
+        if (need64 && at < (unsigned)A.pend_cap)
+          A.pend[at] = make_uint4((unsigned)S.item_id, (unsigned)S.item_k | ((unsigned)la << 16) | ((unsigned)tgt << 21),
+                                  (unsigned)tA, (unsigned)tB);
+      } else {
+        ensure_fk64(S, R, T64, lane, fk64);
+        int hit = 0;
+        if (need64) {
+          cnt.band++;
+          hit = band_retest(W, R, T64, la, tA, tgt, tB);
+        }
+        if (__any_sync(0xffffffffu, hit)) {
+          cnt.hit64++;
+          return true;
+        }
       }
     }
   }
@@ -309,14 +349,57 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
   return 1;
 }
 
+// Gives the bottom half of this warp's stack (and the item context) to a
+// waiting sibling, if one can be claimed; returns the entries given.
+__device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, int lane, int top, int nl)
+{
+  int t = -1;
+  if (lane == 0) {
+    for (int w = 0; w < kWarps && t < 0; ++w)
+      if (w != me && *((volatile int*)&B.flag[w]) == 0 && atomicCAS(&B.flag[w], 0, 3) == 0) t = w;
+  }
+  t = __shfl_sync(0xffffffffu, t, 0);
+  if (t < 0) return 0;
+  WarpSmem& S = all[me];
+  WarpSmem& D = all[t];
+  const int h = top / 2;
+  for (int k = lane; k < h; k += 32) D.stack[k] = S.stack[k];
+  for (int i = lane; i < nl * 12; i += 32) D.T[i / 12][i % 12] = S.T[i / 12][i % 12];
+  if (lane < nl) {
+    D.delta[lane] = S.delta[lane];
+    D.gerr[lane] = S.gerr[lane];
+  }
+  if (lane == 0) {
+    D.item_qa = S.item_qa;
+    D.item_qb = S.item_qb;
+    D.item_k = S.item_k;
+    D.item_n = S.item_n;
+    D.item_id = S.item_id;
+    D.item_rid = S.item_rid;
+    D.don_top = h;
+  }
+  __syncwarp();
+  for (int k = lane; k < top - h; k += 32) S.stack[k] = S.stack[h + k];
+  __syncwarp();
+  if (lane == 0) {
+    __threadfence_block();
+    atomicExch(&B.flag[t], 1);
+  }
+  return h;
+}
+
 // Traverses queries [qbase, qbase+qcount) of robot R for the configuration
-// whose FP32 link transforms are in S.T.  Warp-uniform control flow.
+// whose FP32 link transforms are in S.T, or (preset > 0) the preset entries
+// S.stack[0, preset) handed over by a sibling.  Warp-uniform control flow.
+template <bool FP64>
 __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
                                      int qbase, int qcount, int lane, uint2* spill, int spill_cap,
-                                     double (*T64)[12], int& fk64, int job_flush, Cnt& cnt)
+                                     double (*T64)[12], int& fk64, const EngineArgs& A, int job_flush,
+                                     Cnt& cnt, WarpSmem* all, int me, BlockShare& B, int preset)
 {
   const unsigned lt = lanemask_lt();
-  int top = 0, njobs = 0, spill_top = 0;
+  int top = preset, njobs = 0, spill_top = 0;
+  if (preset > 0) qcount = 0;
 
   // root pairs of every query, tested in parallel
 #pragma unroll 1
@@ -373,7 +456,7 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
       }
     }
     if (njobs >= job_flush || (top == 0 && njobs > 0)) {
-      const bool hit = run_jobs(S, W, R, njobs, lane, T64, fk64, cnt);
+      const bool hit = run_jobs<FP64>(S, W, R, njobs, lane, T64, fk64, A, cnt);
       __syncwarp();
       njobs = 0;
       if (hit) return TR_HIT;
@@ -389,6 +472,11 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
       spill_top += H;
       top -= H;
       cnt.spills++;
+    }
+    if (A.mode == MODE_EDGES && top >= kDonateMin) {
+      int idle = 0;
+      if (lane == 0) idle = *((volatile int*)&B.idle);
+      if (__shfl_sync(0xffffffffu, idle, 0) > 0) top -= share_stack(all, me, B, lane, top, R.nlinks);
     }
     const int n = min(top, 32);
     const bool have = lane < n;
@@ -421,7 +509,13 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
 
 // MINB: resident blocks of kWarps warps per SM the register allocation is
 // sized for (2 -> 128 registers/thread, 3 -> 80, 4 -> 64).
-template <int MINB>
+// FP64 = false: the main pass over all items; undecided triangle pairs go to
+// A.pend for k_band.  FP64 = true: every item with the FP64 triangle test
+// inline, either as the only pass (A.inline64, for batches where undecided
+// pairs are common and an inline FP64 contact ends an item early) or as the
+// fallback after a main pass whose list overflowed (otherwise it returns at
+// once); its verdicts overwrite the main pass's.
+template <int MINB, bool FP64>
 __global__ void __launch_bounds__(kWarps * 32, MINB)
     k_engine(const KWorldDev* __restrict__ W, const EngineArgs A)
 {
@@ -436,6 +530,14 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
   const int spill_cap = A.spill_per_warp - kT64Doubles;
   Cnt cnt;
   unsigned long long items = 0;
+  if (FP64 && !A.inline64 && *((volatile unsigned int*)A.pend_count) <= (unsigned)A.pend_cap)
+    return;  // k_band decided the list
+  BlockShare& B = *reinterpret_cast<BlockShare*>(smem_raw + sizeof(WarpSmem) * kWarps);
+  if (threadIdx.x == 0) {
+    B.idle = 0;
+    for (int w = 0; w < kWarps; ++w) B.flag[w] = 2;
+  }
+  __syncthreads();
   const int total = A.mode == MODE_EDGES ? A.meta[1] : A.B;
   const int maxn = A.mode == MODE_EDGES ? A.meta[0] : 0;  // last round index
   const int grab = A.grab >= 1 && A.grab <= 16 ? A.grab : kGrab;
@@ -476,6 +578,10 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
       } else if (rid < 0) {
         rid = __ldg(A.robot_ids + b);
       }
+      // FK of up to G consecutive steps at once (G = 32 / L groups of L lanes,
+      // L the link count rounded up to 8, 16 or 32): rows [g L, g L + nl) of
+      // S.T hold step fk_base + g; a later step's rows are moved to 0..nl-1
+      int fk_base = -1, fk_cnt = 0;
 #pragma unroll 1
       for (int k = k0; k <= k1; ++k) {
         if (A.mode == MODE_EDGES) {
@@ -498,6 +604,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           }
           S.item_k = k;
           S.item_n = n;
+          S.item_id = A.mode == MODE_EDGES ? e : b;
+          S.item_rid = rid;
         }
         float q = 0.f, e_q = 0.f;
         if (lane < nl) {
@@ -511,7 +619,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           }
         }
         __syncwarp();
-        items++;
+        if (!FP64) items++;
         const bool nonfinite = __any_sync(0xffffffffu, lane < nl && !(fabsf(q) < 1.0e6f));
         if (nonfinite) {
           if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
@@ -539,13 +647,38 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
             continue;
           }
         }
-        float P[12], delta;
-        warp_fk32(R, lane, q, e_q, P, &delta);
-        if (lane < nl) {
+        const int L = nl <= 8 ? 8 : (nl <= 16 ? 16 : 32);
+        if (k < fk_base || k >= fk_base + fk_cnt) {
+          fk_base = k;
+          fk_cnt = A.mode == MODE_EDGES ? min(32 / L, k1 - k + 1) : 1;
+          const int g = lane / L, link = lane & (L - 1);
+          const bool valid = g < fk_cnt && link < nl;
+          float qg = 0.f, eg = 0.f;
+          if (valid) {
+            if (A.mode == MODE_EDGES) {
+              const float a = __ldg(A.qa + (size_t)e * nl + link), bq = __ldg(A.qb + (size_t)e * nl + link);
+              const float d = bq - a;
+              qg = fmaf((float)(k + g) / (float)n, d, a);
+              eg = kU * (fabsf(d) + fabsf(qg) + fabsf(a)) * 1.01f + 1e-30f;
+            } else {
+              qg = q;
+              eg = e_q;
+            }
+          }
+          float P[12], delta;
+          warp_fk32_group(R, lane, L, valid, qg, eg, P, &delta);
+          if (valid) {
 #pragma unroll
-          for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
-          S.delta[lane] = delta;
-          S.gerr[lane] = rot_gram_err32(P);
+            for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
+            S.delta[lane] = delta;
+            S.gerr[lane] = rot_gram_err32(P);
+          }
+        } else if (lane < nl) {
+          const int row = (k - fk_base) * L + lane;
+#pragma unroll
+          for (int i = 0; i < 12; ++i) S.T[lane][i] = S.T[row][i];
+          S.delta[lane] = S.delta[row];
+          S.gerr[lane] = S.gerr[row];
         }
         __syncwarp();
         int env_res = TR_FREE, self_res = TR_FREE;
@@ -553,22 +686,25 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
         const bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
         const bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
         if (want_env && R.nqueries_env > 0)
-          env_res = traverse(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, job_flush,
-                             cnt);
+          env_res = traverse<FP64>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, A,
+                                   job_flush, cnt, all, warp, B, 0);
         const bool stop = A.mode != MODE_CONFIGS && env_res != TR_FREE;
         if (!stop && want_self && R.nqueries_self > 0)
-          self_res = traverse(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill, spill_cap,
-                              T64, fk64, job_flush, cnt);
+          self_res = traverse<FP64>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill,
+                                    spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0);
         if (env_res == TR_OVERFLOW || self_res == TR_OVERFLOW) {
           if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
           continue;
         }
         if (lane == 0) {
+          // verdicts only ever turn into contacts (the outputs start as
+          // "free"), so shared traversals and the FP64 pass can add theirs
+          // in any order
           if (A.mode == MODE_CONFIGS) {
-            if (A.env_hit) A.env_hit[b] = env_res == TR_HIT;
-            if (A.self_hit) A.self_hit[b] = self_res == TR_HIT;
+            if (A.env_hit && env_res == TR_HIT) A.env_hit[b] = 1;
+            if (A.self_hit && self_res == TR_HIT) A.self_hit[b] = 1;
           } else if (A.mode == MODE_FEASIBLE) {
-            A.feasible[b] = (env_res == TR_FREE && self_res == TR_FREE) ? 1 : 0;
+            if (env_res == TR_HIT || self_res == TR_HIT) A.feasible[b] = 0;
           } else if (env_res == TR_HIT || self_res == TR_HIT) {
             atomicMin(A.first_hit + e, k);
           }
@@ -576,6 +712,69 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
         __syncwarp();
       }  // steps of the item
     }
+  }
+
+  // ---- queue drained: take over halves of the block's deep traversals
+  if (lane == 0) {
+    atomicExch(&B.flag[warp], 0);
+    atomicAdd(&B.idle, 1);
+  }
+  __syncwarp();
+#pragma unroll 1
+  for (int spins = 0, waits = 0;;) {
+    int f = 0;
+    if (lane == 0) f = *((volatile int*)&B.flag[warp]);
+    f = __shfl_sync(0xffffffffu, f, 0);
+    if (f == 1) {
+      __threadfence_block();
+      if (lane == 0) atomicSub(&B.idle, 1);
+      __syncwarp();
+      const KRobotDev& R = W->robots[S.item_rid];
+      int fh = INT_MAX;
+      if (A.mode == MODE_EDGES && lane == 0) fh = *((volatile int*)(A.first_hit + S.item_id));
+      fh = __shfl_sync(0xffffffffu, fh, 0);
+      if (fh > S.item_k) {  // not decided yet
+        int fk64 = 0;
+        const bool self = ((S.stack[0].y >> 25) & 63u) < 32u;
+        const int res = traverse<FP64>(S, W, R, 0, 0, lane, spill, spill_cap, T64, fk64, A, job_flush, cnt, all,
+                                       warp, B, S.don_top);
+        if (lane == 0) {
+          if (res == TR_OVERFLOW) {
+            set_status(W->status, KGPU_ERR_OVERFLOW);
+          } else if (res == TR_HIT) {
+            if (A.mode == MODE_EDGES) atomicMin(A.first_hit + S.item_id, S.item_k);
+            else if (A.mode == MODE_FEASIBLE) A.feasible[S.item_id] = 0;
+            else if (self && A.self_hit) A.self_hit[S.item_id] = 1;
+            else if (!self && A.env_hit) A.env_hit[S.item_id] = 1;
+          }
+        }
+      }
+      if (lane == 0) {
+        atomicExch(&B.flag[warp], 0);
+        atomicAdd(&B.idle, 1);
+      }
+      __syncwarp();
+      spins = 0;
+      waits = 0;
+      continue;
+    }
+    if (f == 0) {
+      int idle = 0;
+      if (lane == 0) idle = *((volatile int*)&B.idle);
+      idle = __shfl_sync(0xffffffffu, idle, 0);
+      if (idle >= kWarps || spins >= kShareSpins) {
+        int old = 0;
+        if (lane == 0) old = atomicCAS(&B.flag[warp], 0, 4);
+        if (__shfl_sync(0xffffffffu, old, 0) == 0) break;  // left: no longer claimable
+        continue;  // claimed meanwhile: the hand-over is in progress
+      }
+    } else if (++waits > kShareSpins) {
+      // a hand-over that does not complete: report it and stop
+      if (lane == 0) set_status(W->status, KGPU_ERR_TIMEOUT);
+      break;
+    }
+    ++spins;
+    __nanosleep(256);
   }
   unsigned long long np = cnt.node_pairs, tp = cnt.tri_pairs, bd = cnt.band;
 #pragma unroll
@@ -592,6 +791,89 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
     atomicAdd(W->stats + 4, cnt.spills);
     atomicAdd(W->stats + 5, cnt.cert);
     atomicAdd(W->stats + 6, cnt.hit64);
+  }
+}
+
+// FP64 decision of the triangle pairs the main pass left undecided.  A warp
+// takes 32 consecutive records (one per lane); records of the same item are
+// contiguous (a warp appends its batch with one atomic), so for each item in
+// the batch the warp computes the FP64 transforms once (canonical joint
+// values: the float input widened, or the FP64 edge interpolation) and the
+// item's lanes run the FP64 triangle test (band_retest) in parallel.  A
+// contact sets the item's verdict: first_hit = min(first_hit, k) for an edge
+// step, env_hit / self_hit = 1 or feasible = 0 for a configuration (the main
+// pass wrote the verdict from the decided pairs; these writes only turn it
+// into a contact).  Does nothing when the list overflowed (the fallback pass
+// re-checks every item then).
+__global__ void __launch_bounds__(kWarps * 32) k_band(const KWorldDev* __restrict__ W, const EngineArgs A)
+{
+  __shared__ double q64s[kWarps][kMaxLinks];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int gwarp = blockIdx.x * kWarps + warp;
+  const unsigned npend = *((volatile unsigned int*)A.pend_count);
+  if (npend > (unsigned)A.pend_cap) return;
+  double(*T64)[12] = reinterpret_cast<double(*)[12]>(A.spill + (size_t)gwarp * A.spill_per_warp);
+  unsigned long long band = 0, hits = 0;
+#pragma unroll 1
+  for (unsigned base = (unsigned)gwarp * 32u; base < npend; base += gridDim.x * kWarps * 32u) {
+    const bool have = base + lane < npend;
+    const uint4 r = have ? A.pend[base + lane] : make_uint4(0u, 0u, 0u, 0u);
+    const int item = (int)r.x, k = (int)(r.y & 0xffffu);
+    unsigned todo = __ballot_sync(0xffffffffu, have);
+#pragma unroll 1
+    while (todo) {
+      const int src = __ffs(todo) - 1;
+      const int gi = __shfl_sync(0xffffffffu, item, src), gk = __shfl_sync(0xffffffffu, k, src);
+      const bool mine = have && item == gi && k == gk;
+      todo &= ~__ballot_sync(0xffffffffu, mine);
+      if (A.mode == MODE_EDGES && *((volatile int*)(A.first_hit + gi)) <= gk) continue;  // decided already
+      int rid = A.robot;
+      if (A.mode != MODE_EDGES && rid < 0) rid = __ldg(A.robot_ids + gi);
+      const KRobotDev& R = W->robots[rid];
+      const int nl = R.nlinks;
+      if (lane < nl) {
+        double q;
+        if (A.mode == MODE_EDGES) {
+          int n = __ldg(A.nsteps + gi);
+          if (n < 1 || n > kMaxSteps) n = 0;
+          q = kx_interp((double)__ldg(A.qa + (size_t)gi * nl + lane), (double)__ldg(A.qb + (size_t)gi * nl + lane),
+                        gk, n);
+        } else {
+          q = (double)__ldg(A.q + (size_t)gi * A.q_stride + lane);
+        }
+        q64s[warp][lane] = q;
+      }
+      __syncwarp();
+      warp_fk64(R, q64s[warp], T64, lane);
+      __syncwarp();
+      int hit = 0, tgt = 0;
+      if (mine) {
+        band++;
+        tgt = (int)((r.y >> 21) & 63u);
+        hit = band_retest(W, R, T64, (int)((r.y >> 16) & 31u), (int)r.z, tgt, (int)r.w);
+        hits += hit ? 1 : 0;
+      }
+      const bool env_hit = __any_sync(0xffffffffu, hit && tgt >= 32);
+      const bool self_hit = __any_sync(0xffffffffu, hit && tgt < 32);
+      if (lane == 0 && (env_hit || self_hit)) {
+        if (A.mode == MODE_EDGES) atomicMin(A.first_hit + gi, gk);
+        else if (A.mode == MODE_FEASIBLE) A.feasible[gi] = 0;
+        else {
+          if (env_hit) A.env_hit[gi] = 1;
+          if (self_hit) A.self_hit[gi] = 1;
+        }
+      }
+      __syncwarp();
+    }
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    band += __shfl_down_sync(0xffffffffu, band, o);
+    hits += __shfl_down_sync(0xffffffffu, hits, o);
+  }
+  if (lane == 0 && W->stats && band) {
+    atomicAdd(W->stats + 3, band);
+    atomicAdd(W->stats + 6, hits);
   }
 }
 
@@ -743,32 +1025,50 @@ __global__ void k_fk(const KWorldDev* __restrict__ W, int robot, const float* q,
   }
 }
 
-template <int MINB>
+template <int MINB, bool FP64>
 cudaError_t init_engine()
 {
-  return cudaFuncSetAttribute(k_engine<MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)(sizeof(WarpSmem) * kWarps));
+  return cudaFuncSetAttribute(k_engine<MINB, FP64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(sizeof(WarpSmem) * kWarps + sizeof(BlockShare)));
 }
 
 // the shared-memory attribute is set once per process by engine_init(), so
 // that launches can be captured into CUDA graphs
-template <int MINB>
+template <int MINB, bool FP64>
 cudaError_t launch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, cudaStream_t s)
 {
-  size_t smem = sizeof(WarpSmem) * kWarps;
-  k_engine<MINB><<<blocks, kWarps * 32, smem, s>>>(W, A);
+  size_t smem = sizeof(WarpSmem) * kWarps + sizeof(BlockShare);
+  k_engine<MINB, FP64><<<blocks, kWarps * 32, smem, s>>>(W, A);
   return cudaGetLastError();
 }
 
-// `blocks` = SMs x blocks per SM; the blocks-per-SM value selects the
-// register budget of the instantiation
-cudaError_t dispatch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, int per_sm, cudaStream_t s)
+// Main pass, FP64 decision of its undecided pairs (k_band), and the fallback
+// pass (which returns at once unless the pair list overflowed).  `blocks` =
+// SMs x blocks per SM; the blocks-per-SM value selects the register budget
+// of the main pass's instantiation.  Queue heads and the list count live in
+// S.counters ([0] main head, [1] pair count, [2] fallback head), cleared
+// here.
+cudaError_t dispatch_engine(const KWorldDev* W, EngineArgs A, const Scratch& S, int blocks, int per_sm,
+                            cudaStream_t s)
 {
+  cudaError_t err = cudaMemsetAsync(S.counters, 0, 3 * sizeof(unsigned int), s);
+  if (err != cudaSuccess) return err;
+  A.head = S.counters;
+  A.pend_count = S.counters + 1;
+  A.pend = S.pend;
+  A.pend_cap = S.pend_cap;
+  if (A.inline64) return per_sm == 3 ? launch_engine<3, true>(W, A, blocks, s) : launch_engine<2, true>(W, A, blocks, s);
   switch (per_sm) {
-    case 3: return launch_engine<3>(W, A, blocks, s);
-    case 4: return launch_engine<4>(W, A, blocks, s);
-    default: return launch_engine<2>(W, A, blocks, s);
+    case 3: err = launch_engine<3, false>(W, A, blocks, s); break;
+    case 4: err = launch_engine<4, false>(W, A, blocks, s); break;
+    default: err = launch_engine<2, false>(W, A, blocks, s); break;
   }
+  if (err != cudaSuccess) return err;
+  const int sms = per_sm > 0 && blocks / per_sm > 0 ? blocks / per_sm : 1;
+  k_band<<<2 * sms, kWarps * 32, 0, s>>>(W, A);
+  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  A.head = S.counters + 2;
+  return launch_engine<2, true>(W, A, 2 * sms, s);
 }
 
 }  // namespace
@@ -779,9 +1079,11 @@ int engine_scratch_doubles() { return kT64Doubles; }
 
 cudaError_t engine_init()
 {
-  cudaError_t e = init_engine<2>();
-  if (e == cudaSuccess) e = init_engine<3>();
-  if (e == cudaSuccess) e = init_engine<4>();
+  cudaError_t e = init_engine<2, false>();
+  if (e == cudaSuccess) e = init_engine<3, false>();
+  if (e == cudaSuccess) e = init_engine<4, false>();
+  if (e == cudaSuccess) e = init_engine<2, true>();
+  if (e == cudaSuccess) e = init_engine<3, true>();
   return e;
 }
 
@@ -799,10 +1101,14 @@ cudaError_t launch_fk(const KWorldDev* W, int robot, const float* q, int B, floa
 cudaError_t launch_check_configs(const KWorldDev* W, const Scratch& S, int robot, const int* robot_ids,
                                  const float* q, int q_stride, int B, uint8_t* env_hit, uint8_t* self_hit,
                                  uint8_t* feasible, int blocks, int per_sm, cudaStream_t s, int grab,
-                                 int job_flush)
+                                 int job_flush, int fp64_inline)
 {
   if (B <= 0) return cudaSuccess;
-  cudaError_t err = cudaMemsetAsync(S.counters, 0, sizeof(unsigned int), s);
+  // the kernels only ever record contacts: start from "free"
+  cudaError_t err = cudaSuccess;
+  if (env_hit) err = cudaMemsetAsync(env_hit, 0, (size_t)B, s);
+  if (err == cudaSuccess && self_hit) err = cudaMemsetAsync(self_hit, 0, (size_t)B, s);
+  if (err == cudaSuccess && feasible) err = cudaMemsetAsync(feasible, 1, (size_t)B, s);
   if (err != cudaSuccess) return err;
   EngineArgs A = {};
   A.grab = grab;
@@ -816,19 +1122,18 @@ cudaError_t launch_check_configs(const KWorldDev* W, const Scratch& S, int robot
   A.env_hit = env_hit;
   A.self_hit = self_hit;
   A.feasible = feasible;
-  A.head = S.counters;
+  A.inline64 = fp64_inline != 0;  // default (-1): inline for configuration batches
   A.spill = S.spill;
   A.spill_per_warp = (int)S.spill_per_warp;
-  return dispatch_engine(W, A, blocks, per_sm, s);
+  return dispatch_engine(W, A, S, blocks, per_sm, s);
 }
 
 cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S, int robot, const float* qa,
                                const float* qb, const int* nsteps, int E, int* first_hit, int blocks,
-                               int per_sm, cudaStream_t s, int grab, int job_flush, int chunk)
+                               int per_sm, cudaStream_t s, int grab, int job_flush, int chunk, int fp64_inline)
 {
   if (E <= 0) return cudaSuccess;
   cudaError_t err;
-  if ((err = cudaMemsetAsync(S.counters, 0, sizeof(unsigned int), s)) != cudaSuccess) return err;
   if ((err = cudaMemsetAsync(S.edge_hist, 0, sizeof(int) * (kMaxSteps + 2), s)) != cudaSuccess) return err;
   if ((err = cudaMemsetAsync(S.edge_meta, 0, sizeof(int) * 4, s)) != cudaSuccess) return err;
   int* fill = S.edge_meta + 4;  // kMaxSteps+2 ints after the meta words
@@ -845,6 +1150,7 @@ cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S
   A.grab = grab;
   A.job_flush = job_flush;
   A.chunk = chunk;
+  A.inline64 = fp64_inline == 1;  // default (-1): deferred for edge batches
   A.mode = MODE_EDGES;
   A.robot = robot;
   A.qa = qa;
@@ -855,10 +1161,9 @@ cudaError_t launch_check_edges(const KWorldDev* W, int* status, const Scratch& S
   A.round_off = S.edge_round_off;
   A.perm = S.edge_perm;
   A.meta = S.edge_meta;
-  A.head = S.counters;
   A.spill = S.spill;
   A.spill_per_warp = (int)S.spill_per_warp;
-  if ((err = dispatch_engine(W, A, blocks, per_sm, s)) != cudaSuccess) return err;
+  if ((err = dispatch_engine(W, A, S, blocks, per_sm, s)) != cudaSuccess) return err;
   k_edges_finalize<<<gb, tb, 0, s>>>(first_hit, E);
   return cudaGetLastError();
 }

@@ -152,15 +152,19 @@ __device__ __forceinline__ void joint_local32(const KRobotDev& R, int i, float q
 //   delta = rho r + tau + u (12 r + 6 |t|),
 // r the largest vertex norm of the link in its own frame (the u-term covers
 // the FP32 rounding of the vertex and box transforms).
-__device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, float q, float e_q, float* P,
-                                          float* delta)
+//
+// warp_fk32_group runs G = 32 / L independent configurations at once: lanes
+// [g L, g L + L) hold configuration g, lane g L + i link i (active when
+// `valid`); warp_fk32 is the single-configuration case (L = 32).
+__device__ __forceinline__ void warp_fk32_group(const KRobotDev& R, int lane, int L, bool valid, float q,
+                                                float e_q, float* P, float* delta)
 {
-  int nl = R.nlinks;
+  const int link = lane & (L - 1), gbase = lane & ~(L - 1);
   int anc = -1;
   float rho = 0.f, tau = 0.f;
-  if (lane < nl) {
-    joint_local32(R, lane, q, e_q, P, &rho, &tau);
-    anc = R.parents[lane];
+  if (valid) {
+    joint_local32(R, link, q, e_q, P, &rho, &tau);
+    anc = R.parents[link] >= 0 ? gbase + R.parents[link] : -1;
   } else {
 #pragma unroll
     for (int k = 0; k < 12; ++k) P[k] = 0.f;
@@ -185,8 +189,14 @@ __device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, float q,
       anc = anc2;
     }
   }
-  const float rl = lane < nl ? R.link_r[lane] : 0.f;
+  const float rl = valid ? R.link_r[link] : 0.f;
   *delta = (rho * rl + tau + kU * (12.f * rl + 6.f * tnorm(P))) * 1.001f + 1e-9f;
+}
+
+__device__ __forceinline__ void warp_fk32(const KRobotDev& R, int lane, float q, float e_q, float* P,
+                                          float* delta)
+{
+  warp_fk32_group(R, lane, 32, lane < R.nlinks, q, e_q, P, delta);
 }
 
 // ---- boxes -------------------------------------------------------------

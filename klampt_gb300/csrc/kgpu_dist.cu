@@ -980,7 +980,7 @@ cudaError_t launch_distance(const KWorldDev* Wd, const Scratch& S, int robot, co
                             double* d, int* pair, double* cp, float* grad, int num_sms, cudaStream_t s)
 {
   if (B <= 0) return cudaSuccess;
-  cudaError_t e = cudaMemsetAsync(S.counters + 1, 0, sizeof(unsigned int), s);
+  cudaError_t e = cudaMemsetAsync(S.counters + 8, 0, sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
   DistArgs A = {};
   A.mode = 0;
@@ -992,7 +992,7 @@ cudaError_t launch_distance(const KWorldDev* Wd, const Scratch& S, int robot, co
   A.pair = pair;
   A.cp = cp;
   A.grad = grad;
-  A.head = S.counters + 1;
+  A.head = S.counters + 8;
   A.scratch = S.spill;
   A.scratch_per_warp = (int)S.spill_per_warp;
   k_dist<<<num_sms * 2, kDW * 32, sizeof(DistSmem) * kDW, s>>>(Wd, A);
@@ -1007,7 +1007,7 @@ cudaError_t launch_softmin(const KWorldDev* Wd, const Scratch& S, int robot, con
   double* dwp = work;            // [B]
   double* mt = work + B;         // [T]
   double* wsum = work + B + T;   // [B]
-  cudaError_t e = cudaMemsetAsync(S.counters + 1, 0, 2 * sizeof(unsigned int), s);
+  cudaError_t e = cudaMemsetAsync(S.counters + 8, 0, 2 * sizeof(unsigned int), s);
   if (e != cudaSuccess) return e;
   DistArgs A = {};
   A.robot = robot;
@@ -1019,7 +1019,7 @@ cudaError_t launch_softmin(const KWorldDev* Wd, const Scratch& S, int robot, con
   A.mode = 1;
   A.cutoff = 1e3;
   A.d = dwp;
-  A.head = S.counters + 1;
+  A.head = S.counters + 8;
   k_dist<<<num_sms * 2, kDW * 32, sizeof(DistSmem) * kDW, s>>>(Wd, A);
   k_traj_min<<<(T + 127) / 128, 128, 0, s>>>(dwp, T, Wn, mt);
   // pass 2: every pair below m + K tau, unnormalised gradients
@@ -1029,7 +1029,7 @@ cudaError_t launch_softmin(const KWorldDev* Wd, const Scratch& S, int robot, con
   A.W = Wn;
   A.tau = tau;
   A.grad = dLdq;
-  A.head = S.counters + 2;
+  A.head = S.counters + 9;
   k_dist<<<num_sms * 2, kDW * 32, sizeof(DistSmem) * kDW, s>>>(Wd, A);
   k_softmin_final<<<(T + 127) / 128, 128, 0, s>>>(wsum, mt, T, Wn, nl, tau, L, dLdq);
   return cudaGetLastError();

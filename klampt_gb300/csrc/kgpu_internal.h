@@ -124,7 +124,9 @@ struct Scratch {
   uint2* spill = nullptr;          // per-warp spill stacks
   size_t spill_per_warp = 0;
   int max_warps = 0;
-  unsigned int* counters = nullptr;  // work-queue heads
+  unsigned int* counters = nullptr;  // work-queue heads and the re-test list count
+  uint4* pend = nullptr;             // triangle pairs left to the FP64 re-test
+  int pend_cap = 0;
   int* edge_hist = nullptr;          // kMaxSteps+2
   int* edge_round_off = nullptr;     // kMaxSteps+2
   int* edge_perm = nullptr;
@@ -214,6 +216,7 @@ struct kgpu_world_s {
   int grab = 2;            // work items per queue atomic (1..16)
   int job_flush = 64;      // triangle-pair jobs collected before testing them (8..64)
   int edge_chunk = 4;      // consecutive steps of an edge per work item (1..64)
+  int fp64_inline = -1;    // FP64 triangle tests inline (1) or deferred to k_band (0); -1: by batch kind
   int num_sms = 0;
   bool tables_dirty = true;
   // pinned staging for the host-buffer entry points
@@ -242,11 +245,11 @@ cudaError_t launch_check_configs(const KWorldDev* Wd, const Scratch& S, int robo
                                  const int* robot_ids, const float* q, int q_stride, int B,
                                  uint8_t* env_hit, uint8_t* self_hit, uint8_t* feasible,
                                  int blocks, int per_sm, cudaStream_t s, int grab = 0,
-                                 int job_flush = 0);
+                                 int job_flush = 0, int fp64_inline = -1);
 cudaError_t launch_check_edges(const KWorldDev* Wd, int* status, const Scratch& S, int robot,
                                const float* qa, const float* qb, const int* nsteps, int E,
                                int* first_hit, int blocks, int per_sm, cudaStream_t s,
-                               int grab = 0, int job_flush = 0, int chunk = 0);
+                               int grab = 0, int job_flush = 0, int chunk = 0, int fp64_inline = -1);
 cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q, int B,
                                    uint8_t* env_hit, uint8_t* self_hit, cudaStream_t s);
 cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,

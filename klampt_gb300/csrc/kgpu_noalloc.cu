@@ -10,7 +10,9 @@
 // instead works entirely inside one fixed, file-scope device array.
 //
 // The array (kNoAllocBytes, 20 MiB) holds the work-queue heads, the edge
-// ordering tables for at most KGPU_NOALLOC_MAX_EDGES edges, and per-warp
+// ordering tables for at most KGPU_NOALLOC_MAX_EDGES edges, the list of
+// triangle pairs left to the FP64 re-test (65,536 entries; a longer list
+// makes a fallback pass re-check every step), and per-warp
 // regions (FP64 link transforms + a 1,024-entry traversal spill stack) for
 // one block of 8 warps per SM.  Every GPU that loads the library keeps this
 // array until the process exits.
@@ -37,11 +39,12 @@ namespace {
 constexpr size_t kNoAllocBytes = 20u << 20;
 constexpr int kNoAllocSpill = 1024;   // traversal spill entries per warp
 constexpr int kNoAllocMaxWarps = 1536;
+constexpr int kNoAllocPend = 1 << 16;  // triangle pairs left to the FP64 re-test
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
 struct Layout {
-  size_t counters, hist, round_off, meta, perm, warps, end;
+  size_t counters, hist, round_off, meta, perm, pend, warps, end;
   size_t per_warp_entries;
 };
 
@@ -56,6 +59,7 @@ Layout layout()
   L.round_off = o; o = align256(o + (kgpu::kMaxSteps + 2) * sizeof(int));
   L.meta = o; o = align256(o + (4 + 2 * (kgpu::kMaxSteps + 2)) * sizeof(int));
   L.perm = o; o = align256(o + (size_t)KGPU_NOALLOC_MAX_EDGES * sizeof(int));
+  L.pend = o; o = align256(o + (size_t)kNoAllocPend * sizeof(uint4));
   L.per_warp_entries = (size_t)kgpu::engine_scratch_doubles() + kNoAllocSpill;  // uint2 entries
   L.warps = o; o = align256(o + (size_t)kNoAllocMaxWarps * L.per_warp_entries * sizeof(uint2));
   L.end = o;
@@ -112,6 +116,8 @@ extern "C" kgpu_status kgpu_check_edges_noalloc(kgpu_world w, int32_t robot, con
   S.edge_round_off = (int*)(base + L.round_off);
   S.edge_meta = (int*)(base + L.meta);
   S.edge_perm = (int*)(base + L.perm);
+  S.pend = (uint4*)(base + L.pend);
+  S.pend_cap = kNoAllocPend;
   S.edge_cap = KGPU_NOALLOC_MAX_EDGES;
   S.spill = (uint2*)(base + L.warps);
   S.spill_per_warp = L.per_warp_entries;

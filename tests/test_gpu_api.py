@@ -101,7 +101,7 @@ def test_autotuner_keeps_results(world0):
     w = W.engine
     before = w.check_configs(q[:512])
     best, table = autotune.tune_configs(w, q[:512], reps=1)
-    assert len(table) == 18 and set(best) == {"blocks_per_sm", "grab", "job_flush"}
+    assert len(table) == 36 and set(best) == {"blocks_per_sm", "grab", "job_flush", "fp64_inline"}
     assert all(w.get_option(k) == v for k, v in best.items())
     after = w.check_configs(q[:512])
     assert all(np.array_equal(x.cpu().numpy(), y.cpu().numpy()) for x, y in zip(before, after))
