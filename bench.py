@@ -294,7 +294,7 @@ def main():
         # tuned on a separately seeded batch of the same size and distribution
         # (the timed edges are not used for tuning)
         ta, tb, tn = sc.random_edges(robot, args.edges, np.random.default_rng(2001))
-        tuned, _ = autotune.tune_edges(w, ta, tb, tn, reps=2)
+        tuned, _ = autotune.tune_edges(w, ta, tb, tn, reps=3)
     out = torch.empty(args.edges, dtype=torch.int32, device="cuda")
     plan = w.edge_plan(a, b, n, out)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")

@@ -5,12 +5,13 @@ Tries, on a sample of the caller's own workload, every combination of
                             of the engine instantiation: 128 / 80 / 64)
   grab           1, 2, 4   (work items a warp takes per queue atomic)
   job_flush      32, 64    (triangle-pair jobs collected before testing)
+and, for configuration batches,
   fp64_inline    0, 1      (FP64 triangle tests deferred to a second kernel,
                             or inline in the traversal)
-and, for edge batches,
+or, for edge batches (FP64 tests always deferred there),
   edge_chunk     2, 4, 8   (consecutive steps of an edge per work item)
-times each with CUDA events (best of `reps` after one warm-up) and leaves the
-fastest setting in the world.  Results are identical for every setting; only
+times each with CUDA events (median of `reps` after one warm-up) and leaves
+the fastest setting in the world.  Results are identical for every setting; only
 the time changes.
 """
 
@@ -23,14 +24,15 @@ import torch
 
 from .engine import World
 
-GRID = {"blocks_per_sm": (2, 3, 4), "grab": (1, 2, 4), "job_flush": (32, 64), "fp64_inline": (0, 1)}
-GRID_EDGES = dict(GRID, edge_chunk=(2, 4, 8))
+_BASE = {"blocks_per_sm": (2, 3, 4), "grab": (1, 2, 4), "job_flush": (32, 64)}
+GRID = dict(_BASE, fp64_inline=(0, 1))
+GRID_EDGES = dict(_BASE, fp64_inline=(0,), edge_chunk=(2, 4, 8))
 
 
 def _time(fn: Callable[[], None], reps: int) -> float:
     fn()
     torch.cuda.synchronize()
-    best = float("inf")
+    times = []
     for _ in range(reps):
         s = torch.cuda.Event(enable_timing=True)
         e = torch.cuda.Event(enable_timing=True)
@@ -38,8 +40,8 @@ def _time(fn: Callable[[], None], reps: int) -> float:
         fn()
         e.record()
         torch.cuda.synchronize()
-        best = min(best, s.elapsed_time(e))
-    return best
+        times.append(s.elapsed_time(e))
+    return sorted(times)[len(times) // 2]
 
 
 def tune(world: World, run: Callable[[], None], reps: int = 3,

@@ -795,9 +795,11 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
 }
 
 // FP64 decision of the triangle pairs the main pass left undecided.  A warp
-// takes 32 consecutive records (one per lane); records of the same item are
-// contiguous (a warp appends its batch with one atomic), so for each item in
-// the batch the warp computes the FP64 transforms once (canonical joint
+// takes `per` consecutive records (one per lane; per = the list length over
+// the warps, 1..32, so a short list is spread over all warps and its latency
+// is one record's); records of the same item are contiguous (a warp appends
+// its batch with one atomic), so for each item in its records the warp
+// computes the FP64 transforms once (canonical joint
 // values: the float input widened, or the FP64 edge interpolation) and the
 // item's lanes run the FP64 triangle test (band_retest) in parallel.  A
 // contact sets the item's verdict: first_hit = min(first_hit, k) for an edge
@@ -814,9 +816,11 @@ __global__ void __launch_bounds__(kWarps * 32) k_band(const KWorldDev* __restric
   if (npend > (unsigned)A.pend_cap) return;
   double(*T64)[12] = reinterpret_cast<double(*)[12]>(A.spill + (size_t)gwarp * A.spill_per_warp);
   unsigned long long band = 0, hits = 0;
+  const unsigned nwarps = gridDim.x * kWarps;
+  const unsigned per = min(32u, max(1u, (npend + nwarps - 1) / nwarps));
 #pragma unroll 1
-  for (unsigned base = (unsigned)gwarp * 32u; base < npend; base += gridDim.x * kWarps * 32u) {
-    const bool have = base + lane < npend;
+  for (unsigned base = (unsigned)gwarp * per; base < npend; base += nwarps * per) {
+    const bool have = (unsigned)lane < per && base + lane < npend;
     const uint4 r = have ? A.pend[base + lane] : make_uint4(0u, 0u, 0u, 0u);
     const int item = (int)r.x, k = (int)(r.y & 0xffffu);
     unsigned todo = __ballot_sync(0xffffffffu, have);
