@@ -224,6 +224,27 @@ def secondary_metrics(reps: int = 2) -> dict:
     out["hetero_configs"] = {"value": len(ids) / (ms / 1e3), "unit": "configs/s",
                              "sample": "65,536 configs of 6/7/12/30-DOF robots (40/30/20/10%), 1.0M-tri environment, one launch"}
     w3.close()
+    # ray casting: four 640x480 pinhole cameras into the icosphere field
+    robot1, env1, _ = sc.scene_cfg1(n_edges=2)
+    w1 = World(env1, [robot1])
+    rays = [sc.camera_rays(eye, sc.SPHERE_FIELD_CENTER, 640, 480) for eye in sc.CAMERA_EYES]
+    Sd = torch.as_tensor(np.concatenate([r[0] for r in rays])).cuda()
+    Dd = torch.as_tensor(np.concatenate([r[1] for r in rays])).cuda()
+    ms = _event_ms(lambda: w1.raycast(Sd, Dd, sync=False), reps)
+    w1.sync()
+    from oracle.oracle_py import Oracle, raycast
+    o1 = Oracle(robot1, env1)
+    s_cpu, d_cpu = sc.camera_rays(sc.CAMERA_EYES[0], sc.SPHERE_FIELD_CENTER, 160, 120)
+    cores = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    raycast(o1, s_cpu, d_cpu, nthreads=cores)
+    cpu_rate = len(s_cpu) / (time.perf_counter() - t0)
+    out["raycast"] = {"value": Sd.shape[0] / (ms / 1e3), "unit": "rays/s",
+                      "sample": "4 pinhole cameras x 640x480 rays into 2,000 icospheres (640k tris); first hit, "
+                                "FP64 parameter and point",
+                      "cpu_port": {"value": cpu_rate, "unit": "rays/s", "cores": cores,
+                                   "sample": "one 160x120 camera, FP64 oracle"}}
+    w1.close()
     return out
 
 

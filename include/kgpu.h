@@ -246,6 +246,19 @@ kgpu_status kgpu_distance(kgpu_world world, int32_t robot, const float* q, int32
 kgpu_status kgpu_softmin_grad(kgpu_world world, int32_t robot, const float* q, int32_t T,
                               int32_t W, double tau, double* L, float* dLdq, kgpu_stream stream);
 
+/* Batched ray casting against every object of the world's environment: ray
+ * i is s[3i..3i+2] + t d[3i..3i+2], t >= 0.  Per ray: obj = index of the
+ * object hit first (-1: none), tri = the hit triangle's index in that
+ * object's mesh, t = the ray parameter (FP64, +inf on a miss), point = the
+ * hit point s + t d (FP64).  Nearest hit, ties to the smaller object, then
+ * triangle; a ray in a triangle's plane does not hit it.  Replaces
+ * Geometry3D::rayCast / rayCast_ext (Python/klampt/src/robotsim.cpp:
+ * 1821-1852), the environment part of WorldModel::RayCast
+ * (Cpp/Modeling/World.cpp:465-515) and collide.ray_cast
+ * (Python/klampt/model/collide.py:219-243), one call for R rays. */
+kgpu_status kgpu_raycast(kgpu_world world, const float* s, const float* d, int32_t R, int32_t* obj,
+                         int32_t* tri, double* t, double* point, kgpu_stream stream);
+
 /* ---- host-buffer variants (pinned staging inside; synchronous) ------------ */
 kgpu_status kgpu_check_configs_host(kgpu_world world, int32_t robot, const float* q, int32_t B,
                                     uint8_t* env_hit, uint8_t* self_hit);

@@ -35,6 +35,10 @@
  *   kx_tri_tri_dist2   squared distance between two triangles with the
  *                      closest points (9 segment-segment + 6 point-triangle
  *                      candidates; 0 when they intersect).
+ *   kx_ray_tri         ray s + t d (t >= 0) against a closed triangle by the
+ *                      triple-product form of Moller-Trumbore (divisions
+ *                      deferred to the one for t); a ray in the triangle's
+ *                      plane (determinant exactly 0) does not hit.
  *
  * Rigid transforms are 12 doubles: R row-major (R[3*r+c]) followed by t.
  */
@@ -391,6 +395,34 @@ KX_HD double kx_tri_tri_dist2(const double* P, const double* Q, double* cp, doub
     cq[t] = kx_add(bq[t], o[t]);
   }
   return best;
+}
+
+/* ---- ray / triangle ----------------------------------------------------- */
+/* With e1 = b - a, e2 = c - a, w = s - a, p = d x e2, q = w x e1:
+   det = e1 . p, U = w . p, V = d . q, Tn = e2 . q; the ray meets the closed
+   triangle at t = Tn / det iff U, V, det - (U + V) and Tn all have the sign
+   of det (zero allowed).  T: 9 doubles (a, b, c).  Returns 1 and *t on a hit. */
+KX_HD int kx_ray_tri(const double* s, const double* d, const double* T, double* t)
+{
+  double e1[3], e2[3], w[3], p[3], q[3];
+  kx_sub3(T + 3, T, e1);
+  kx_sub3(T + 6, T, e2);
+  kx_sub3(s, T, w);
+  kx_cross3(d, e2, p);
+  const double det = kx_dot3(e1, p);
+  if (det == 0.0) return 0;
+  const double U = kx_dot3(w, p);
+  kx_cross3(w, e1, q);
+  const double V = kx_dot3(d, q);
+  const double Tn = kx_dot3(e2, q);
+  const double UV = kx_add(U, V);
+  if (det > 0.0) {
+    if (U < 0.0 || V < 0.0 || UV > det || Tn < 0.0) return 0;
+  } else {
+    if (U > 0.0 || V > 0.0 || UV < det || Tn > 0.0) return 0;
+  }
+  *t = kx_div(Tn, det);
+  return 1;
 }
 
 #endif /* KGPU_EXACT_H */

@@ -505,6 +505,7 @@ kgpu_status kgpu_env_create(const kgpu_env_desc* d, kgpu_env* out)
   if (e == cudaSuccess) e = upload(&E->d_face32, face32.data(), face32.size());
   if (e == cudaSuccess) e = upload(&E->d_obj_leaf_first, obj_leaf_first.data(), obj_leaf_first.size());
   if (e == cudaSuccess) e = upload(&E->d_obj_leaf_count, obj_leaf_count.data(), obj_leaf_count.size());
+  if (e == cudaSuccess && N > 0) e = upload(&E->d_obj_tri_first, d->tri_offset, (size_t)N);
   if (e != cudaSuccess) {
     kgpu_env_destroy(E);
     return cuda_fail(e, "environment upload");
@@ -531,6 +532,7 @@ kgpu_status kgpu_env_destroy(kgpu_env E)
   dfree(E->d_face64);
   dfree(E->d_face32);
   dfree(E->d_obj_leaf_first);
+  dfree(E->d_obj_tri_first);
   dfree(E->d_obj_leaf_count);
   delete E;
   return KGPU_OK;
@@ -660,6 +662,7 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
     D.eface64 = env->d_face64;
     D.obj_leaf_first = env->d_obj_leaf_first;
     D.obj_leaf_count = env->d_obj_leaf_count;
+    D.obj_tri_first = env->d_obj_tri_first;
     D.num_objects = env->nobj;
     for (int g = 0; g < kMaxGroups; ++g) {
       D.group_root[g] = env->group_root[g];
@@ -924,6 +927,16 @@ kgpu_status kgpu_softmin_grad(kgpu_world w, int32_t robot, const float* q, int32
   return launch_status(launch_softmin(w->d_dev, w->scratch, robot, q, T, Wn, tau, L, dLdq, w->robots[robot]->nlinks,
                                       w->scratch.dist_work, w->num_sms, (cudaStream_t)s),
                        "kgpu_softmin_grad");
+}
+
+kgpu_status kgpu_raycast(kgpu_world w, const float* s, const float* d, int32_t R, int32_t* obj, int32_t* tri,
+                         double* t, double* point, kgpu_stream st)
+{
+  if (!w) return fail(KGPU_ERR_INVALID, "null world");
+  if (R < 0 || (R > 0 && (!s || !d || !obj || !tri || !t || !point))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  kgpu_status e = refresh_tables(w);
+  if (e) return e;
+  return launch_status(launch_raycast(w->d_dev, s, d, R, obj, tri, t, point, (cudaStream_t)st), "kgpu_raycast");
 }
 
 // ---- host-buffer variants ----------------------------------------------------

@@ -830,7 +830,13 @@ __global__ void __launch_bounds__(kWarps * 32) k_band(const KWorldDev* __restric
       const int gi = __shfl_sync(0xffffffffu, item, src), gk = __shfl_sync(0xffffffffu, k, src);
       const bool mine = have && item == gi && k == gk;
       todo &= ~__ballot_sync(0xffffffffu, mine);
-      if (A.mode == MODE_EDGES && *((volatile int*)(A.first_hit + gi)) <= gk) continue;  // decided already
+      if (A.mode == MODE_EDGES) {
+        // one read, broadcast: lanes reading separately could see another
+        // warp's update at different times and split the warp
+        int fh = 0;
+        if (lane == 0) fh = *((volatile int*)(A.first_hit + gi));
+        if (__shfl_sync(0xffffffffu, fh, 0) <= gk) continue;  // decided already
+      }
       int rid = A.robot;
       if (A.mode != MODE_EDGES && rid < 0) rid = __ldg(A.robot_ids + gi);
       const KRobotDev& R = W->robots[rid];

@@ -106,6 +106,7 @@ struct KWorldDev {
   const double* eface64;     // 4 per env triangle: the same in canonical FP64
   const int* obj_leaf_first; // per object: its triangles' leaf-order range
   const int* obj_leaf_count;
+  const int* obj_tri_first;  // per object: its first triangle in the input order
   int group_root[kMaxGroups];
   float group_margin[kMaxGroups];
   int num_objects;
@@ -181,6 +182,7 @@ struct kgpu_env_s {
   double* d_face64 = nullptr;
   int* d_obj_leaf_first = nullptr;
   int* d_obj_leaf_count = nullptr;
+  int* d_obj_tri_first = nullptr;
   int group_root[kgpu::kMaxGroups];
   float group_margin[kgpu::kMaxGroups];
   size_t n_nodes = 0, n_tris = 0;
@@ -255,6 +257,8 @@ cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q
 cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,
                                  const float* qb, const int* nsteps, int E, int* first_hit,
                                  cudaStream_t s);
+cudaError_t launch_raycast(const KWorldDev* Wd, const float* s, const float* d, int R, int* obj, int* tri,
+                           double* t, double* point, cudaStream_t st);
 cudaError_t dist_init();
 cudaError_t launch_distance(const KWorldDev* Wd, const Scratch& S, int robot, const float* q, int B,
                             double cutoff, double* d, int* pair, double* cp, float* grad, int num_sms,

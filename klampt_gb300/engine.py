@@ -277,6 +277,24 @@ class World:
             self.sync()
         return out, g
 
+    def raycast(self, s, d, sync: bool = True):
+        """Rays s[i] + t d[i] (t >= 0) against the environment: (obj, tri, t,
+        point) per ray; obj -1 and t = inf on a miss."""
+        sd = _dev(s, torch.float32).reshape(-1, 3).contiguous()
+        dd = _dev(d, torch.float32).reshape(-1, 3).contiguous()
+        R = sd.shape[0]
+        if dd.shape[0] != R:
+            raise ValueError("s and d must hold the same number of rays")
+        obj = torch.empty(R, dtype=torch.int32, device="cuda")
+        tri = torch.empty(R, dtype=torch.int32, device="cuda")
+        t = torch.empty(R, dtype=torch.float64, device="cuda")
+        pt = torch.empty((R, 3), dtype=torch.float64, device="cuda")
+        check(lib().kgpu_raycast(self.handle, _dptr(sd), _dptr(dd), R, _dptr(obj), _dptr(tri), _dptr(t), _dptr(pt),
+                                 _stream()))
+        if sync:
+            self.sync()
+        return obj, tri, t, pt
+
     # ---- queries (host buffers, through the C ABI's pinned staging) -----------
     def check_configs_host(self, q: np.ndarray, robot: int = 0):
         L = self.robots[robot].num_links

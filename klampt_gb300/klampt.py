@@ -12,8 +12,11 @@ Mirrors (paths relative to the Klamp't tree):
   RobotCSpace.feasible / isFeasible / isVisible / eps
                                    Python/klampt/plan/robotcspace.py:31-118,
                                    cspace.py:81,185-200, motionplanning.cpp:789-809
+  WorldModel.rayCast, WorldCollider.rayCast
+                                   Cpp/Modeling/World.cpp:465-515 (environment
+                                   part), Python/klampt/model/collide.py:219-243
 Batched overloads: RobotModel.setConfigs, WorldCollider.check_configs /
-distance_batch, RobotCSpace.isFeasibleBatch / isVisibleBatch.
+distance_batch / rayCastBatch, RobotCSpace.isFeasibleBatch / isVisibleBatch.
 
 Rotations follow Klamp't's so3 convention in this layer (9 numbers,
 column-major); the engine's ABI uses row-major.  Errors raise RuntimeError, as
@@ -81,6 +84,12 @@ class WorldModel:
 
     def numTerrains(self) -> int:
         return int(np.sum(self.env_spec.groups == GROUP_TERRAIN)) if self.env_spec is not None else 0
+
+    def rayCast(self, s: Sequence[float], d: Sequence[float]) -> Tuple[int, List[float]]:
+        """WorldModel::RayCast over the environment: (object index, world hit
+        point), or (-1, [0, 0, 0]) when nothing is hit."""
+        obj, _, _, pt = self._world.raycast(np.asarray(s, np.float32)[None], np.asarray(d, np.float32)[None])
+        return int(obj.cpu()[0]), pt.cpu().numpy()[0].tolist()
 
     def close(self):
         self._world.close()
@@ -222,6 +231,18 @@ class WorldCollider:
                 res.grad1 = u.tolist()
                 res.grad2 = (-u).tolist()
         return res
+
+    def rayCast(self, s: Sequence[float], d: Sequence[float]) -> Optional[Tuple[int, List[float]]]:
+        """collide.ray_cast over the environment's objects: (object index,
+        hit point) of the first hit, or None."""
+        o, p = self.world.rayCast(s, d)
+        return None if o < 0 else (o, p)
+
+    def rayCastBatch(self, S, D):
+        """Rays S[i] + t D[i]: (object [R] (-1 = none), triangle [R], t [R],
+        hit point [R, 3])."""
+        obj, tri, t, pt = self.world.engine.raycast(S, D)
+        return obj.cpu().numpy(), tri.cpu().numpy(), t.cpu().numpy(), pt.cpu().numpy()
 
     def distance_batch(self, Q, cutoff: float = 1.0, robot: int = 0):
         """(d [B], (link, object) [B, 2], closest points [B, 6], dd/dq [B, L])."""

@@ -417,6 +417,27 @@ def sphere_field(rng: np.random.Generator, n: int = 2000, subdiv: int = 2,
                             info=dict(center=list(center), side=side, subdiv=subdiv))
 
 
+def camera_rays(eye: Sequence[float], target: Sequence[float], w: int, h: int, fov: float = 1.0):
+    """Pinhole-camera rays (sources [w*h, 3], unnormalised directions
+    [w*h, 3], FP32) from `eye` looking at `target`, vertical field of view
+    `fov` radians, z up."""
+    eye = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - eye
+    f /= np.linalg.norm(f)
+    r = np.cross(f, [0, 0, 1.0])
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    xs = (np.arange(w) + 0.5) / w * 2 - 1
+    ys = (np.arange(h) + 0.5) / h * 2 - 1
+    X, Y = np.meshgrid(xs * np.tan(fov / 2) * w / h, ys * np.tan(fov / 2), indexing="xy")
+    d = f[None, None] + X[..., None] * r + Y[..., None] * u
+    s = np.broadcast_to(eye, d.shape)
+    return s.reshape(-1, 3).astype(np.float32), d.reshape(-1, 3).astype(np.float32)
+
+
+CAMERA_EYES = ((-1.0, -1.5, 1.2), (-1.2, 1.5, 1.0), (0.2, 0.1, 2.6), (3.6, 0.3, 0.8))
+
+
 def scene_cfg1(seed: int = 1001, n_edges: int = 16384):
     """7-DOF arm (2,112 tris/link), 2,000 icospheres (subdivision 2 = 320
     tris each, 640k tris), 16,384 edges of 2..400 steps at 0.01 rad."""

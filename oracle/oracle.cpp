@@ -35,6 +35,12 @@
  *                        penetration for convex obstacles (see below)
  *   soft-min, gradient   Python/klampt/math/autodiff/geometry_ad.py:613-814
  *                        (MinDistance), here as a log-sum-exp soft-min
+ *   ray casting          first hit of s + t d (t >= 0) over the environment's
+ *                        objects: Geometry3D::rayCast_ext (robotsim.cpp:
+ *                        1821-1852), WorldModel::RayCast (Cpp/Modeling/
+ *                        World.cpp:465-515), collide.ray_cast (Python/klampt/
+ *                        model/collide.py:219-243); nearest hit, ties to the
+ *                        smaller object, then triangle
  *
  * The FP64 values that decide verdicts and distances come from the canonical
  * arithmetic in include/kgpu_exact.h; everything else here (BVH build,
@@ -980,6 +986,82 @@ int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, i
       Lout[t] = m - tau * log(sum);
       if (grad) {
         for (size_t k = 0; k < g.size(); ++k) grad[(size_t)t * W * R->L + k] = g[k] / sum;
+      }
+    }
+  });
+  return 0;
+}
+
+/* Ray casting against every object of the environment.  s, d: R rays (FP32,
+   widened exactly); per ray obj (-1: no hit), tri (triangle index within the
+   object's mesh), t (FP64) and the hit point s + t d.  Nearest t, ties to the
+   smaller global triangle index (= smaller object, then triangle). */
+int orc_raycast(void* env, const float* s, const float* d, int R, int* obj, int* tri, double* tout,
+                double* point, int nthreads)
+{
+  Env* E = (Env*)env;
+  parallel_for(R, nthreads, [&](int, int r0, int r1) {
+    std::vector<int> st;
+    for (int r = r0; r < r1; ++r) {
+      double S[3], D[3];
+      for (int i = 0; i < 3; ++i) {
+        S[i] = (double)s[3 * (size_t)r + i];
+        D[i] = (double)d[3 * (size_t)r + i];
+      }
+      double best = INFINITY;
+      int bt = -1;
+      for (int g = 0; g < 32; ++g) {
+        const Bvh& B = E->group_bvh[g];
+        if (B.empty()) continue;
+        st.assign(1, 0);
+        while (!st.empty()) {
+          const Node& n = B.nodes[st.back()];
+          st.pop_back();
+          // slab test, widened by a relative 1e-9 so that rounding never
+          // drops a box the ray touches
+          double tn = 0.0, tf = best;
+          bool miss = false;
+          for (int i = 0; i < 3 && !miss; ++i) {
+            const double pad = 1e-9 * (fabs(n.c[i]) + n.h[i] + 1.0);
+            const double lo = n.c[i] - n.h[i] - pad, hi = n.c[i] + n.h[i] + pad;
+            if (D[i] == 0.0) {
+              if (S[i] < lo || S[i] > hi) miss = true;
+              continue;
+            }
+            double a = (lo - S[i]) / D[i], b = (hi - S[i]) / D[i];
+            if (a > b) std::swap(a, b);
+            a -= 1e-9 * (fabs(a) + 1e-9);
+            b += 1e-9 * (fabs(b) + 1e-9);
+            tn = std::max(tn, a);
+            tf = std::min(tf, b);
+            if (tn > tf) miss = true;
+          }
+          if (miss) continue;
+          if (n.left < 0) {
+            for (int k = n.first; k < n.first + n.count; ++k) {
+              const int t = B.order[k];
+              double tt;
+              if (kx_ray_tri(S, D, &E->tri[9 * (size_t)t], &tt) && (tt < best || (tt == best && t < bt))) {
+                best = tt;
+                bt = t;
+              }
+            }
+          } else {
+            st.push_back(n.left + 1);
+            st.push_back(n.left);
+          }
+        }
+      }
+      if (bt < 0) {
+        obj[r] = -1;
+        tri[r] = -1;
+        tout[r] = INFINITY;
+        for (int i = 0; i < 3; ++i) point[3 * (size_t)r + i] = 0.0;
+      } else {
+        obj[r] = E->tri_obj[bt];
+        tri[r] = bt - E->obj_first[obj[r]];
+        tout[r] = best;
+        for (int i = 0; i < 3; ++i) point[3 * (size_t)r + i] = kx_add(S[i], kx_mul(best, D[i]));
       }
     }
   });

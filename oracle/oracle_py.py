@@ -40,7 +40,7 @@ def lib():
         L.orc_robot_create.restype = P
         L.orc_env_create.restype = P
         for name in ("orc_check_configs", "orc_check_edges", "orc_is_feasible", "orc_pair_distance",
-                     "orc_min_distance", "orc_softmin", "orc_tri_tri"):
+                     "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast"):
             getattr(L, name).restype = ctypes.c_int
         L.orc_robot_destroy.argtypes = [P]
         L.orc_env_destroy.argtypes = [P]
@@ -186,6 +186,20 @@ class Oracle:
                           _p(q), ctypes.c_int(T), ctypes.c_int(W), ctypes.c_double(tau),
                           _p(Lout), _p(grad), ctypes.c_int(nthreads))
         return Lout, grad
+
+
+def raycast(oracle: "Oracle", s, d, nthreads: int = 1):
+    """Environment ray casting: (obj, tri, t, point) per ray (obj -1: no hit)."""
+    s = np.ascontiguousarray(s, dtype=np.float32).reshape(-1, 3)
+    d = np.ascontiguousarray(d, dtype=np.float32).reshape(-1, 3)
+    R = s.shape[0]
+    obj = np.zeros(R, np.int32)
+    tri = np.zeros(R, np.int32)
+    t = np.zeros(R, np.float64)
+    pt = np.zeros((R, 3), np.float64)
+    lib().orc_raycast(ctypes.c_void_p(oracle.env), _p(s), _p(d), ctypes.c_int(R), _p(obj), _p(tri), _p(t),
+                      _p(pt), ctypes.c_int(nthreads))
+    return obj, tri, t, pt
 
 
 def sincos(x) -> tuple:

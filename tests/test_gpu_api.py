@@ -75,6 +75,24 @@ def test_collider_distance_result(world0):
         assert abs(np.linalg.norm(res.grad1) - 1.0) < 1e-6
 
 
+def test_world_and_collider_raycast(world0):
+    from klampt_gb300.klampt import WorldCollider
+    from oracle.oracle_py import raycast
+    W, robot, env, q, o = world0
+    col = WorldCollider(W)
+    rng = np.random.default_rng(21)
+    S = rng.uniform(-1.5, 1.5, (2048, 3)).astype(np.float32)
+    D = rng.normal(size=(2048, 3)).astype(np.float32)
+    obj, tri, t, pt = col.rayCastBatch(S, D)
+    ro, rt, rtt, rp = raycast(o, S, D, nthreads=NT)
+    assert np.array_equal(obj, ro) and np.array_equal(tri, rt) and np.array_equal(t, rtt) and np.array_equal(pt, rp)
+    k = int(np.argmax(obj >= 0))
+    assert col.rayCast(S[k], D[k]) == (int(ro[k]), rp[k].tolist())
+    miss = int(np.argmax(obj < 0))
+    assert col.rayCast(S[miss], D[miss]) is None
+    assert W.rayCast(S[miss], D[miss])[0] == -1
+
+
 def test_autograd_wrappers():
     import torch
     from klampt_gb300.autodiff import MinDistance, SoftMinDistance

@@ -231,3 +231,19 @@ def test_masks_exclude_terrain_for_base_links():
     env2 = sc.env_from_objects("o", [terrain], groups=[0], convex=[1])
     eh, _, _ = op.Oracle(robot, env2).check_configs(q)
     assert eh[0] == 1
+
+
+def test_oracle_raycast_box_known_answers():
+    """Ray casting on a unit box: face, edge and corner hits, a ray from
+    inside, a scaled direction, a miss, a zero direction."""
+    from oracle.oracle_py import Oracle, raycast
+    box = sc.box_mesh((0, 0, 0), (0.5, 0.5, 0.5))
+    env = sc.env_from_objects("box", [box])
+    o = Oracle(sc.arm(2), env)
+    s = np.array([[2, 0, 0], [2, 0.5, 0.5], [0, 0, 0], [2, 2, 2], [2, 0, 0], [2, 0, 0]], np.float32)
+    d = np.array([[-1, 0, 0], [-1, 0, 0], [1, 0, 0], [1, 0, 0], [-2, 0, 0], [0, 0, 0]], np.float32)
+    obj, tri, t, pt = raycast(o, s, d)
+    assert obj.tolist() == [0, 0, 0, -1, 0, -1]
+    assert t[0] == 1.5 and t[1] == 1.5 and t[2] == 0.5 and t[4] == 0.75
+    assert np.isinf(t[3]) and np.isinf(t[5])
+    assert np.array_equal(pt[0], [0.5, 0, 0]) and np.array_equal(pt[1], [0.5, 0.5, 0.5])
