@@ -184,6 +184,16 @@ kgpu_status kgpu_world_reset_stats(kgpu_world world);
 kgpu_status kgpu_fk(kgpu_world world, int32_t robot, const float* q, int32_t B, float* T_out,
                     float* err_out, kgpu_stream stream);
 
+/* Full Jacobians of points on links at B configurations: J[b] is 6 x
+ * num_links (row-major), rows 0-2 the angular part, rows 3-5 the linear
+ * part of the world velocity of the point plocal[b] (link frame) on link
+ * links[b] (or `link` for every configuration when links is NULL).
+ * Replaces RobotModelLink::getJacobian / getPositionJacobian
+ * (Python/klampt/src/robotsim.cpp:4817-4845; KrisLibrary GetFullJacobian),
+ * one call for B configurations.  FP32, from the error-bounded FK. */
+kgpu_status kgpu_jacobian(kgpu_world world, int32_t robot, const float* q, int32_t B, const int32_t* links,
+                          int32_t link, const float* plocal, float* J, kgpu_stream stream);
+
 /* Environment and self collision verdicts of B configurations, FP32 BVH
  * traversal with the FP64 band re-test.  Replaces, per configuration,
  * WorldPlannerSettings::CheckCollision(world, {robot}, others)

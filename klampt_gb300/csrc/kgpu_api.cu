@@ -929,6 +929,18 @@ kgpu_status kgpu_softmin_grad(kgpu_world w, int32_t robot, const float* q, int32
                        "kgpu_softmin_grad");
 }
 
+kgpu_status kgpu_jacobian(kgpu_world w, int32_t robot, const float* q, int32_t B, const int32_t* links,
+                          int32_t link, const float* plocal, float* J, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && (!q || !plocal || !J))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  const int nl = w->robots[robot]->nlinks;
+  if (!links && (link < 0 || link >= nl)) return fail(KGPU_ERR_INVALID, "link %d out of range [0,%d)", link, nl);
+  return launch_status(launch_jacobian(w->d_dev, robot, q, links, link, plocal, B, J, (cudaStream_t)s),
+                       "kgpu_jacobian");
+}
+
 kgpu_status kgpu_raycast(kgpu_world w, const float* s, const float* d, int32_t R, int32_t* obj, int32_t* tri,
                          double* t, double* point, kgpu_stream st)
 {

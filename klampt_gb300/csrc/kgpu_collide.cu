@@ -24,8 +24,11 @@
 //     push children with ballot/popc compaction; leaf/leaf pairs become
 //     triangle-pair jobs that are expanded one triangle pair per lane.
 //   * A triangle pair the FP32 filter cannot separate is either certified
-//     as a contact in FP32 (tri_certain_hit32) or re-tested in FP64
-//     (band_retest on FP64 transforms computed once per configuration).
+//     as a contact in FP32 (tri_certain_hit32) or listed for the FP64 test
+//     (band_retest on FP64 transforms), run by k_band after the main pass or
+//     inline in the single-pass variant.
+//   * After the queue drains, idle warps of a block take over halves of their
+//     siblings' deep traversal stacks (edge batches).
 //   * The shared-memory stack spills its lower half to a per-warp region of
 //     global scratch when full; exhausting that region sets
 //     KGPU_ERR_OVERFLOW instead of dropping work.
@@ -1035,6 +1038,60 @@ __global__ void k_fk(const KWorldDev* __restrict__ W, int robot, const float* q,
   }
 }
 
+// Full Jacobian of a point on a link, one warp per configuration: rows 0-2
+// the angular part (column j = world axis of joint j for a revolute ancestor,
+// 0 otherwise), rows 3-5 the linear part (w_j x (p - o_j) revolute, w_j
+// prismatic), p = T_link * plocal, o_j the origin of link j's frame; columns
+// of links that are not the link or its ancestors are 0
+// (RobotModelLink::getJacobian, Python/klampt/src/robotsim.cpp:4817-4825).
+__global__ void k_jacobian(const KWorldDev* __restrict__ W, int robot, const float* q, const int* links,
+                           int link_all, const float* plocal, int B, float* J)
+{
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= B) return;
+  const KRobotDev& R = W->robots[robot];
+  const int nl = R.nlinks;
+  const int li = links ? __ldg(links + warp) : link_all;
+  float* Jb = J + (size_t)warp * 6 * nl;
+  if (li < 0 || li >= nl) {
+    if (lane == 0) set_status(W->status, KGPU_ERR_INVALID);
+    return;
+  }
+  const float qv = lane < nl ? __ldg(q + (size_t)warp * nl + lane) : 0.f;
+  float P[12], delta;
+  warp_fk32(R, lane, qv, 0.f, P, &delta);
+  // the point in world coordinates, from link li's transform
+  float Ti[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) Ti[k] = __shfl_sync(0xffffffffu, P[k], li);
+  const float px = plocal[3 * (size_t)warp], py = plocal[3 * (size_t)warp + 1], pz = plocal[3 * (size_t)warp + 2];
+  const float3 p = xform32(Ti, make_float3(px, py, pz));
+  if (lane < nl) {
+    bool anc = false;
+    for (int j = li; j >= 0; j = R.parents[j])
+      if (j == lane) { anc = true; break; }
+    float c[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (anc && R.jtype[lane] != KX_JOINT_WELD) {
+      const float ax = R.axis[lane][0], ay = R.axis[lane][1], az = R.axis[lane][2];
+      const float wx = P[0] * ax + P[1] * ay + P[2] * az;
+      const float wy = P[3] * ax + P[4] * ay + P[5] * az;
+      const float wz = P[6] * ax + P[7] * ay + P[8] * az;
+      if (R.jtype[lane] == KX_JOINT_REVOLUTE) {
+        const float rx = p.x - P[9], ry = p.y - P[10], rz = p.z - P[11];
+        c[0] = wx; c[1] = wy; c[2] = wz;
+        c[3] = wy * rz - wz * ry;
+        c[4] = wz * rx - wx * rz;
+        c[5] = wx * ry - wy * rx;
+      } else {
+        c[3] = wx; c[4] = wy; c[5] = wz;
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < 6; ++r) Jb[(size_t)r * nl + lane] = c[r];
+  }
+}
+
 template <int MINB, bool FP64>
 cudaError_t init_engine()
 {
@@ -1105,6 +1162,16 @@ cudaError_t launch_fk(const KWorldDev* W, int robot, const float* q, int B, floa
   long long warps = B;
   int blocks = (int)((warps * 32 + threads - 1) / threads);
   k_fk<<<blocks, threads, 0, s>>>(W, robot, q, B, T, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_jacobian(const KWorldDev* W, int robot, const float* q, const int* links, int link_all,
+                            const float* plocal, int B, float* J, cudaStream_t s)
+{
+  if (B <= 0) return cudaSuccess;
+  const int threads = 256;
+  const int blocks = (int)(((long long)B * 32 + threads - 1) / threads);
+  k_jacobian<<<blocks, threads, 0, s>>>(W, robot, q, links, link_all, plocal, B, J);
   return cudaGetLastError();
 }
 

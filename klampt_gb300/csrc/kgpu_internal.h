@@ -257,6 +257,8 @@ cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q
 cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,
                                  const float* qb, const int* nsteps, int E, int* first_hit,
                                  cudaStream_t s);
+cudaError_t launch_jacobian(const KWorldDev* W, int robot, const float* q, const int* links, int link_all,
+                            const float* plocal, int B, float* J, cudaStream_t s);
 cudaError_t launch_raycast(const KWorldDev* Wd, const float* s, const float* d, int R, int* obj, int* tri,
                            double* t, double* point, cudaStream_t st);
 cudaError_t dist_init();

@@ -277,6 +277,27 @@ class World:
             self.sync()
         return out, g
 
+    def jacobian(self, q, links, plocal, robot: int = 0, sync: bool = True):
+        """Full Jacobians [B, 6, L] (angular rows, then linear) of points
+        plocal [B, 3] (link frame) on links [B] (or one int for all)."""
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L).contiguous()
+        B = qd.shape[0]
+        pd = _dev(plocal, torch.float32).reshape(-1, 3)
+        if pd.shape[0] == 1 and B > 1:
+            pd = pd.expand(B, 3)
+        pd = pd.contiguous()
+        J = torch.empty((B, 6, L), dtype=torch.float32, device="cuda")
+        if isinstance(links, (int, np.integer)):
+            check(lib().kgpu_jacobian(self.handle, robot, _dptr(qd), B, None, int(links), _dptr(pd), _dptr(J),
+                                      _stream()))
+        else:
+            ld = _dev(links, torch.int32).reshape(B).contiguous()
+            check(lib().kgpu_jacobian(self.handle, robot, _dptr(qd), B, _dptr(ld), 0, _dptr(pd), _dptr(J), _stream()))
+        if sync:
+            self.sync()
+        return J
+
     def raycast(self, s, d, sync: bool = True):
         """Rays s[i] + t d[i] (t >= 0) against the environment: (obj, tri, t,
         point) per ray; obj -1 and t = inf on a miss."""

@@ -15,7 +15,9 @@ Mirrors (paths relative to the Klamp't tree):
   WorldModel.rayCast, WorldCollider.rayCast
                                    Cpp/Modeling/World.cpp:465-515 (environment
                                    part), Python/klampt/model/collide.py:219-243
-Batched overloads: RobotModel.setConfigs, WorldCollider.check_configs /
+  RobotModelLink.getJacobian / getPositionJacobian / getOrientationJacobian
+                                   Python/klampt/src/robotsim.cpp:4817-4860
+Batched overloads: RobotModel.setConfigs / getJacobians, WorldCollider.check_configs /
 distance_batch / rayCastBatch, RobotCSpace.isFeasibleBatch / isVisibleBatch.
 
 Rotations follow Klamp't's so3 convention in this layer (9 numbers,
@@ -33,6 +35,7 @@ import numpy as np
 
 from . import engine
 from ._kgpu import GROUP_RIGID_OBJECT, GROUP_TERRAIN
+from .model_io import load_robot
 
 
 @dataclass
@@ -61,9 +64,12 @@ class DistanceQueryResult:
 
 
 class WorldModel:
-    """Robots and a static environment resident on the current CUDA device."""
+    """Robots and a static environment resident on the current CUDA device.
+    Robots may be given as specs or as .rob / .urdf file names
+    (WorldModel::LoadRobot, Cpp/Modeling/World.cpp; model_io.load_robot)."""
 
     def __init__(self, robots: Sequence, env):
+        robots = [load_robot(r) if isinstance(r, str) else r for r in robots]
         self.env_spec = env
         self.robot_specs = list(robots)
         self._world = engine.World(env, self.robot_specs)
@@ -118,6 +124,21 @@ class RobotModelLink:
         R = np.asarray(T[:9], np.float64).reshape(3, 3)
         return (R @ np.asarray(plocal, np.float64) + np.asarray(T[9:], np.float64)).tolist()
 
+    def getJacobian(self, plocal: Sequence[float]) -> np.ndarray:
+        """6 x n Jacobian of the point plocal at the current configuration,
+        orientation rows first (robotsim.cpp:4817-4825)."""
+        r = self.robot
+        J = r.world.engine.jacobian(r._q[None], self.index, np.asarray(plocal, np.float32)[None], robot=r.index)
+        return J.cpu().numpy()[0].astype(np.float64)
+
+    def getPositionJacobian(self, plocal: Sequence[float]) -> np.ndarray:
+        """3 x n position Jacobian (robotsim.cpp:4837-4845)."""
+        return self.getJacobian(plocal)[3:]
+
+    def getOrientationJacobian(self) -> np.ndarray:
+        """3 x n orientation Jacobian."""
+        return self.getJacobian([0.0, 0.0, 0.0])[:3]
+
 
 class RobotModel:
     """robotmodel.h:537; one DOF per link."""
@@ -154,6 +175,11 @@ class RobotModel:
     def setConfigs(self, Q) -> np.ndarray:
         """Batched FK: world transforms [B, L, 12] (R row-major, t)."""
         return self.world.engine.fk(Q, robot=self.index).cpu().numpy()
+
+    def getJacobians(self, Q, links, plocal) -> np.ndarray:
+        """Batched full Jacobians [B, 6, n] of points plocal [B, 3] on links
+        [B] (or one link) at configurations Q [B, n]."""
+        return self.world.engine.jacobian(Q, links, plocal, robot=self.index).cpu().numpy()
 
     def _current_transforms(self) -> np.ndarray:
         if self._T is None:

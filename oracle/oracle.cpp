@@ -992,6 +992,48 @@ int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, i
   return 0;
 }
 
+/* Full Jacobians (KrisLibrary GetFullJacobian as called by
+   RobotModelLink::getJacobian, Python/klampt/src/robotsim.cpp:4817-4825):
+   J[b] = 6 x L row-major, rows 0-2 angular (world axis of each revolute
+   ancestor joint), rows 3-5 linear (w x (p - o) revolute, w prismatic) for
+   the point plocal[b] on link links[b]. */
+int orc_jacobian(void* robot, const float* q, int B, const int* links, const float* plocal, double* J)
+{
+  Robot* R = (Robot*)robot;
+  const int L = R->L;
+  std::vector<double> T((size_t)L * 12), qd(L);
+  for (int b = 0; b < B; ++b) {
+    for (int i = 0; i < L; ++i) qd[i] = (double)q[(size_t)b * L + i];
+    orc_fk(R, qd.data(), T.data());
+    const int li = links[b];
+    double pl[3] = {plocal[3 * (size_t)b], plocal[3 * (size_t)b + 1], plocal[3 * (size_t)b + 2]}, p[3];
+    kx_xform_point(&T[12 * (size_t)li], pl, p);
+    double* Jb = J + (size_t)b * 6 * L;
+    for (int k = 0; k < 6 * L; ++k) Jb[k] = 0.0;
+    for (int j = li; j >= 0; j = R->parents[j]) {
+      if (R->jtypes[j] == KX_JOINT_WELD) continue;
+      const double* Tj = &T[12 * (size_t)j];
+      const double* a = &R->axes[3 * (size_t)j];
+      double w[3];
+      for (int r = 0; r < 3; ++r) w[r] = Tj[3 * r] * a[0] + Tj[3 * r + 1] * a[1] + Tj[3 * r + 2] * a[2];
+      if (R->jtypes[j] == KX_JOINT_REVOLUTE) {
+        const double rx = p[0] - Tj[9], ry = p[1] - Tj[10], rz = p[2] - Tj[11];
+        Jb[0 * L + j] = w[0];
+        Jb[1 * L + j] = w[1];
+        Jb[2 * L + j] = w[2];
+        Jb[3 * L + j] = w[1] * rz - w[2] * ry;
+        Jb[4 * L + j] = w[2] * rx - w[0] * rz;
+        Jb[5 * L + j] = w[0] * ry - w[1] * rx;
+      } else {
+        Jb[3 * L + j] = w[0];
+        Jb[4 * L + j] = w[1];
+        Jb[5 * L + j] = w[2];
+      }
+    }
+  }
+  return 0;
+}
+
 /* Ray casting against every object of the environment.  s, d: R rays (FP32,
    widened exactly); per ray obj (-1: no hit), tri (triangle index within the
    object's mesh), t (FP64) and the hit point s + t d.  Nearest t, ties to the

@@ -40,7 +40,7 @@ def lib():
         L.orc_robot_create.restype = P
         L.orc_env_create.restype = P
         for name in ("orc_check_configs", "orc_check_edges", "orc_is_feasible", "orc_pair_distance",
-                     "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast"):
+                     "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian"):
             getattr(L, name).restype = ctypes.c_int
         L.orc_robot_destroy.argtypes = [P]
         L.orc_env_destroy.argtypes = [P]
@@ -186,6 +186,18 @@ class Oracle:
                           _p(q), ctypes.c_int(T), ctypes.c_int(W), ctypes.c_double(tau),
                           _p(Lout), _p(grad), ctypes.c_int(nthreads))
         return Lout, grad
+
+
+def jacobian(oracle: "Oracle", q, links, plocal):
+    """Full 6 x L Jacobians (angular rows first) of points plocal[b] on links[b]."""
+    L = oracle.nl
+    q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, L)
+    B = q.shape[0]
+    links = np.ascontiguousarray(links, dtype=np.int32).reshape(B)
+    plocal = np.ascontiguousarray(plocal, dtype=np.float32).reshape(B, 3)
+    J = np.zeros((B, 6, L), np.float64)
+    lib().orc_jacobian(ctypes.c_void_p(oracle.robot), _p(q), ctypes.c_int(B), _p(links), _p(plocal), _p(J))
+    return J
 
 
 def raycast(oracle: "Oracle", s, d, nthreads: int = 1):

@@ -42,6 +42,20 @@ def test_robotmodel_set_config_and_transforms(world0):
     assert r.selfCollides() == bool(sh[0])
 
 
+def test_link_jacobian_methods(world0):
+    from oracle.oracle_py import jacobian
+    W, robot, env, q, o = world0
+    r = W.robot(0)
+    r.setConfig(q[7].astype(np.float64))
+    pl = [0.01, -0.02, 0.15]
+    J = r.link(4).getJacobian(pl)
+    Jo = jacobian(o, q[7:8], [4], [pl])[0]
+    assert J.shape == (6, r.numLinks()) and np.abs(J - Jo).max() < 2e-5
+    assert np.array_equal(r.link(4).getPositionJacobian(pl), J[3:])
+    Jb = r.getJacobians(q[:32], 4, np.tile(pl, (32, 1)))
+    assert np.abs(Jb - jacobian(o, q[:32], np.full(32, 4), np.tile(pl, (32, 1)))).max() < 2e-5
+
+
 def test_collider_and_cspace(world0):
     from klampt_gb300.klampt import RobotCSpace, WorldCollider
     W, robot, env, q, o = world0
@@ -142,3 +156,32 @@ def test_heterogeneous_batch_matches_oracle():
         assert np.array_equal(sh[sel], so), r
     assert 0 < eh.mean() < 1 and 0 < sh.mean() < 1
     w.close()
+
+
+def test_jacobian_matches_oracle():
+    """Batched full Jacobians (FP32) against the FP64 oracle on a 7-DOF arm
+    and a 31-link tree with weld and prismatic joints."""
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle, jacobian
+    box = sc.box_mesh((5, 5, 5), (0.1, 0.1, 0.1))
+    env = sc.env_from_objects("far", [box])
+    hum = sc.humanoid()
+    hum.joint_types = hum.joint_types.copy()
+    hum.joint_types[3] = 1
+    rng = np.random.default_rng(9)
+    for robot in (sc.arm(7, rings=8, segments=8), hum):
+        w = World(env, [robot])
+        o = Oracle(robot, env)
+        L = robot.num_links
+        B = 2048
+        q = rng.uniform(-math.pi, math.pi, (B, L)).astype(np.float32)
+        links = rng.integers(0, L, B).astype(np.int32)
+        pl = rng.uniform(-0.2, 0.2, (B, 3)).astype(np.float32)
+        J = w.jacobian(q, links, pl).cpu().numpy()
+        Jo = jacobian(o, q, links, pl)
+        scale = max(1.0, float(np.abs(Jo).max()))
+        assert np.abs(J - Jo).max() <= 2e-5 * scale
+        # one link for every configuration
+        J1 = w.jacobian(q[:16], L - 1, pl[:16]).cpu().numpy()
+        assert np.abs(J1 - jacobian(o, q[:16], np.full(16, L - 1), pl[:16])).max() <= 2e-5 * scale
+        w.close()

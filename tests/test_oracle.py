@@ -247,3 +247,35 @@ def test_oracle_raycast_box_known_answers():
     assert t[0] == 1.5 and t[1] == 1.5 and t[2] == 0.5 and t[4] == 0.75
     assert np.isinf(t[3]) and np.isinf(t[5])
     assert np.array_equal(pt[0], [0.5, 0, 0]) and np.array_equal(pt[1], [0.5, 0.5, 0.5])
+
+
+def test_oracle_jacobian_matches_finite_differences():
+    """Oracle Jacobians (angular and linear rows) against central differences
+    of the oracle's own FK on a tree robot with revolute, prismatic and weld
+    joints."""
+    from oracle.oracle_py import Oracle, jacobian
+    robot = sc.humanoid()
+    robot.joint_types = robot.joint_types.copy()
+    robot.joint_types[3] = 1  # one prismatic joint
+    box = sc.box_mesh((5, 5, 5), (0.1, 0.1, 0.1))
+    o = Oracle(robot, sc.env_from_objects("far", [box]))
+    rng = np.random.default_rng(3)
+    L = robot.num_links
+    q = rng.uniform(-1, 1, (4, L)).astype(np.float32)
+    links = rng.integers(0, L, 4).astype(np.int32)
+    pl = rng.uniform(-0.1, 0.1, (4, 3)).astype(np.float32)
+    J = jacobian(o, q, links, pl)
+    h = 1e-6
+    for b in range(4):
+        for j in range(L):
+            qp = q[b].astype(np.float64).copy(); qm = qp.copy()
+            qp[j] += h; qm[j] -= h
+            Tp, Tm = o.fk(qp), o.fk(qm)
+            li = links[b]
+            pp = Tp[li, :9].reshape(3, 3) @ pl[b] + Tp[li, 9:]
+            pm = Tm[li, :9].reshape(3, 3) @ pl[b] + Tm[li, 9:]
+            assert np.allclose((pp - pm) / (2 * h), J[b, 3:, j], atol=1e-6)
+            # angular velocity from dR R^T
+            dR = (Tp[li, :9] - Tm[li, :9]).reshape(3, 3) / (2 * h)
+            Om = dR @ o.fk(q[b].astype(np.float64))[li, :9].reshape(3, 3).T
+            assert np.allclose([Om[2, 1], Om[0, 2], Om[1, 0]], J[b, :3, j], atol=1e-6)
