@@ -271,10 +271,11 @@ def run_reference(args, rank):
     dt = time.perf_counter() - t0
     v = total / dt
     line = {
-        "impl": "reference", "metric": METRIC, "value": v, "unit": "configs/s", "n_gpus": 0,
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "configs/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "edges_per_step": int(E)},
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "edges_per_step": int(E), "device": "host CPU cores (FP64 oracle port)"},
         "cpu_baseline": {"value": v, "unit": "configs/s", "cores": cores, "kind": "port",
                          "sample": f"{E} of {args.edges} edges per step (rotating), all steps of each edge "
                                    "up to its first collision"},

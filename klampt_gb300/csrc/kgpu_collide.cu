@@ -273,8 +273,9 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
 // |a_i . a_k| <= g (i != k), so a box's projection onto its own axis i is at
 // most h_i + g (hx + hy + hz) and a gap along a overstates the Euclidean one
 // by at most the factor 1 + g.  16 u covers the rounding of the centres,
-// the products and the sums.
-__device__ __forceinline__ bool obb_separated(const float* TA, const float* TB, float4 hA, float4 hB, float3 cA,
+// the products and the sums.  Out of line: only link-link pairs take it, and
+// inlined it lengthens the hot loop of every pair.
+__device__ __noinline__ bool obb_separated(const float* TA, const float* TB, float4 hA, float4 hB, float3 cA,
                                               float3 cB, float tol, float g)
 {
   const float dx = cB.x - cA.x, dy = cB.y - cA.y, dz = cB.z - cA.z;
