@@ -184,6 +184,16 @@ kgpu_status kgpu_world_reset_stats(kgpu_world world);
 kgpu_status kgpu_fk(kgpu_world world, int32_t robot, const float* q, int32_t B, float* T_out,
                     float* err_out, kgpu_stream stream);
 
+/* Self-collision pairs that occur in a batch of B configurations: for every
+ * enabled link pair (i < j) found colliding in some configuration, bit j of
+ * pair_mask[i] is set (pair_mask: num_links words, OR-accumulated, so calls
+ * can continue a sampling run).  Replaces the sampling loop of
+ * RandomizedSelfCollisionPairs (Cpp/Modeling/RandomizedSelfCollisions.cpp:
+ * 19-38): the caller supplies the configurations (uniform samples within the
+ * joint limits there). */
+kgpu_status kgpu_self_collision_pairs(kgpu_world world, int32_t robot, const float* q, int32_t B,
+                                      uint32_t* pair_mask, kgpu_stream stream);
+
 /* Full Jacobians of points on links at B configurations: J[b] is 6 x
  * num_links (row-major), rows 0-2 the angular part, rows 3-5 the linear
  * part of the world velocity of the point plocal[b] (link frame) on link

@@ -798,6 +798,77 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
   }
 }
 
+// Which self-collision pairs occur over a batch of configurations
+// (RandomizedSelfCollisionPairs, Cpp/Modeling/RandomizedSelfCollisions.cpp:
+// 19-38, batched): per configuration, FK then every enabled link pair on its
+// own, FP64 decisions inline; a pair found colliding sets bit tgt of
+// pair_mask[a] (OR-accumulated across calls), and pairs already set are not
+// tested again.
+__global__ void __launch_bounds__(kWarps * 32, 2) k_self_pairs(const KWorldDev* __restrict__ W, const EngineArgs A,
+                                                                 unsigned int* pair_mask)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  WarpSmem* all = reinterpret_cast<WarpSmem*>(smem_raw);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  WarpSmem& S = all[warp];
+  BlockShare& B = *reinterpret_cast<BlockShare*>(smem_raw + sizeof(WarpSmem) * kWarps);
+  const int gwarp = blockIdx.x * kWarps + warp;
+  uint2* wscratch = A.spill + (size_t)gwarp * A.spill_per_warp;
+  double(*T64)[12] = reinterpret_cast<double(*)[12]>(wscratch);
+  uint2* spill = wscratch + kT64Doubles;
+  const int spill_cap = A.spill_per_warp - kT64Doubles;
+  const int job_flush = kJobCap - 32;
+  Cnt cnt;
+  const KRobotDev& R = W->robots[A.robot];
+  const int nl = R.nlinks;
+#pragma unroll 1
+  for (;;) {
+    unsigned int b = 0;
+    if (lane == 0) b = atomicAdd(A.head, 1u);
+    b = __shfl_sync(0xffffffffu, b, 0);
+    if (b >= (unsigned)A.B) break;
+    const float q = lane < nl ? __ldg(A.q + (size_t)b * nl + lane) : 0.f;
+    if (__any_sync(0xffffffffu, lane < nl && !(fabsf(q) < 1.0e6f))) {
+      if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
+      continue;
+    }
+    if (lane == 0) {
+      S.item_qa = A.q + (size_t)b * nl;
+      S.item_qb = nullptr;
+      S.item_k = 0;
+      S.item_n = 0;
+      S.item_id = (int)b;
+      S.item_rid = A.robot;
+    }
+    float P[12], delta;
+    warp_fk32(R, lane, q, 0.f, P, &delta);
+    if (lane < nl) {
+#pragma unroll
+      for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
+      S.delta[lane] = delta;
+      S.gerr[lane] = rot_gram_err32(P);
+    }
+    __syncwarp();
+    int fk64 = 0;
+#pragma unroll 1
+    for (int qi = 0; qi < R.nqueries_self; ++qi) {
+      const int qidx = R.query_off + R.nqueries_env + qi;
+      const uint32_t qw = __ldg(W->queries + qidx);
+      const int a = qw & 0xff, tgt = (qw >> 8) & 0xff;
+      unsigned int known = 0;
+      if (lane == 0) known = *((volatile unsigned int*)(pair_mask + a));
+      if ((__shfl_sync(0xffffffffu, known, 0) >> tgt) & 1u) continue;
+      const int res = traverse<true>(S, W, R, qidx, 1, lane, spill, spill_cap, T64, fk64, A, job_flush, cnt, all,
+                                     warp, B, 0);
+      if (lane == 0) {
+        if (res == TR_OVERFLOW) set_status(W->status, KGPU_ERR_OVERFLOW);
+        else if (res == TR_HIT) atomicOr(pair_mask + a, 1u << tgt);
+      }
+      __syncwarp();
+    }
+  }
+}
+
 // FP64 decision of the triangle pairs the main pass left undecided.  A warp
 // takes `per` consecutive records (one per lane; per = the list length over
 // the warps, 1..32, so a short list is spread over all warps and its latency
@@ -1152,6 +1223,9 @@ cudaError_t engine_init()
   if (e == cudaSuccess) e = init_engine<4, false>();
   if (e == cudaSuccess) e = init_engine<2, true>();
   if (e == cudaSuccess) e = init_engine<3, true>();
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_self_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(sizeof(WarpSmem) * kWarps + sizeof(BlockShare)));
   return e;
 }
 
@@ -1163,6 +1237,27 @@ cudaError_t launch_fk(const KWorldDev* W, int robot, const float* q, int B, floa
   long long warps = B;
   int blocks = (int)((warps * 32 + threads - 1) / threads);
   k_fk<<<blocks, threads, 0, s>>>(W, robot, q, B, T, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_self_pairs(const KWorldDev* W, const Scratch& S, int robot, const float* q, int B,
+                              unsigned int* pair_mask, int num_sms, cudaStream_t s)
+{
+  if (B <= 0) return cudaSuccess;
+  cudaError_t err = cudaMemsetAsync(S.counters, 0, sizeof(unsigned int), s);
+  if (err != cudaSuccess) return err;
+  EngineArgs A = {};
+  A.mode = MODE_CONFIGS;
+  A.robot = robot;
+  A.q = q;
+  A.q_stride = 0;
+  A.B = B;
+  A.head = S.counters;
+  A.spill = S.spill;
+  A.spill_per_warp = (int)S.spill_per_warp;
+  A.inline64 = 1;
+  const size_t smem = sizeof(WarpSmem) * kWarps + sizeof(BlockShare);
+  k_self_pairs<<<2 * num_sms, kWarps * 32, smem, s>>>(W, A, pair_mask);
   return cudaGetLastError();
 }
 

@@ -277,6 +277,18 @@ class World:
             self.sync()
         return out, g
 
+    def self_collision_pairs(self, q, robot: int = 0, mask=None, sync: bool = True):
+        """Self pairs colliding in some configuration of q [B, L]: uint32
+        words [L] (bit j of word i: pair (i, j)), OR-accumulated into `mask`
+        (a CUDA int32 tensor) when given."""
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L).contiguous()
+        m = torch.zeros(L, dtype=torch.int32, device="cuda") if mask is None else mask
+        check(lib().kgpu_self_collision_pairs(self.handle, robot, _dptr(qd), qd.shape[0], _dptr(m), _stream()))
+        if sync:
+            self.sync()
+        return m
+
     def jacobian(self, q, links, plocal, robot: int = 0, sync: bool = True):
         """Full Jacobians [B, 6, L] (angular rows, then linear) of points
         plocal [B, 3] (link frame) on links [B] (or one int for all)."""

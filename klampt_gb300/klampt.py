@@ -276,6 +276,21 @@ class WorldCollider:
         return d.cpu().numpy(), pair.cpu().numpy(), cp.cpu().numpy(), g.cpu().numpy()
 
 
+def RandomizedSelfCollisionPairs(robot: "RobotModel", numSamples: int, seed: int = 0) -> np.ndarray:
+    """collision[i, j] = True iff enabled pair (i, j) collided in one of
+    numSamples configurations drawn uniformly within the finite joint limits
+    (Cpp/Modeling/RandomizedSelfCollisions.cpp:9-38; DOFs with an infinite
+    limit keep their current value)."""
+    spec = robot.spec
+    rng = np.random.default_rng(seed)
+    L = spec.num_links
+    Q = np.tile(robot._q, (numSamples, 1)).astype(np.float32)
+    fin = np.isfinite(spec.qmin) & np.isfinite(spec.qmax)
+    Q[:, fin] = rng.uniform(spec.qmin[fin], spec.qmax[fin], (numSamples, int(fin.sum())))
+    words = robot.world.engine.self_collision_pairs(Q, robot=robot.index).cpu().numpy().astype(np.uint32)
+    return np.array([[bool((words[i] >> j) & 1) for j in range(L)] for i in range(L)])
+
+
 class RobotCSpace:
     """robotcspace.py:31: feasibility = joint limits, then environment, then
     self collision (RobotCSpace.cpp:786-823); visibility = every

@@ -992,6 +992,37 @@ int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, i
   return 0;
 }
 
+/* Self-collision pairs occurring over B configurations (the sampling loop of
+   RandomizedSelfCollisionPairs, Cpp/Modeling/RandomizedSelfCollisions.cpp:
+   19-38): bit j of mask[i] (i < j) is set when enabled pair (i, j) collides
+   in some configuration.  mask is OR-accumulated. */
+int orc_self_pairs(void* robot, void* env, const float* q, int B, unsigned* mask, int nthreads)
+{
+  Robot* R = (Robot*)robot;
+  Env* E = (Env*)env;
+  const int L = R->L;
+  std::vector<std::vector<unsigned>> part((size_t)std::max(1, nthreads), std::vector<unsigned>(L, 0u));
+  parallel_for(B, nthreads, [&](int t, int b0, int b1) {
+    Ctx c;
+    std::vector<uint32_t> masks(L, 0u);
+    c.init(R, E, masks.data());
+    std::vector<double> qd(L);
+    std::vector<unsigned>& m = part[t];
+    for (int b = b0; b < b1; ++b) {
+      for (int i = 0; i < L; ++i) qd[i] = (double)q[(size_t)b * L + i];
+      c.set_config(qd.data());
+      for (int i = 0; i < L; ++i)
+        for (int j = i + 1; j < L; ++j)
+          if (R->self_mask[i * L + j] && !((m[i] >> j) & 1u) && !R->tloc[i].empty() && !R->tloc[j].empty() &&
+              bvtt_collide(c, i, j, -1))
+            m[i] |= 1u << j;
+    }
+  });
+  for (auto& m : part)
+    for (int i = 0; i < L; ++i) mask[i] |= m[i];
+  return 0;
+}
+
 /* Full Jacobians (KrisLibrary GetFullJacobian as called by
    RobotModelLink::getJacobian, Python/klampt/src/robotsim.cpp:4817-4825):
    J[b] = 6 x L row-major, rows 0-2 angular (world axis of each revolute

@@ -40,7 +40,7 @@ def lib():
         L.orc_robot_create.restype = P
         L.orc_env_create.restype = P
         for name in ("orc_check_configs", "orc_check_edges", "orc_is_feasible", "orc_pair_distance",
-                     "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian"):
+                     "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian", "orc_self_pairs"):
             getattr(L, name).restype = ctypes.c_int
         L.orc_robot_destroy.argtypes = [P]
         L.orc_env_destroy.argtypes = [P]
@@ -186,6 +186,17 @@ class Oracle:
                           _p(q), ctypes.c_int(T), ctypes.c_int(W), ctypes.c_double(tau),
                           _p(Lout), _p(grad), ctypes.c_int(nthreads))
         return Lout, grad
+
+
+def self_pairs(oracle: "Oracle", q, nthreads: int = 1, mask=None) -> np.ndarray:
+    """OR over configurations of the enabled self pairs' verdicts: uint32
+    words, bit j of word i set when pair (i, j) collides somewhere."""
+    L = oracle.nl
+    q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, L)
+    m = np.zeros(L, np.uint32) if mask is None else np.ascontiguousarray(mask, np.uint32).copy()
+    lib().orc_self_pairs(ctypes.c_void_p(oracle.robot), ctypes.c_void_p(oracle.env), _p(q), ctypes.c_int(q.shape[0]),
+                         _p(m), ctypes.c_int(nthreads))
+    return m
 
 
 def jacobian(oracle: "Oracle", q, links, plocal):

@@ -185,3 +185,29 @@ def test_jacobian_matches_oracle():
         J1 = w.jacobian(q[:16], L - 1, pl[:16]).cpu().numpy()
         assert np.abs(J1 - jacobian(o, q[:16], np.full(16, L - 1), pl[:16])).max() <= 2e-5 * scale
         w.close()
+
+
+def test_self_collision_pair_sampling():
+    """Pairs colliding over a batch of samples: the engine's OR-accumulated
+    pair mask equals the FP64 oracle's, for a 7-DOF arm and the humanoid."""
+    from klampt_gb300.engine import World
+    from klampt_gb300.klampt import RandomizedSelfCollisionPairs, WorldModel
+    from oracle.oracle_py import Oracle, self_pairs
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    rng = np.random.default_rng(17)
+    for robot in (sc.arm(7, rings=8, segments=8), sc.humanoid()):
+        w = World(env, [robot])
+        o = Oracle(robot, env)
+        q = sc.uniform_configs(robot, 3000, rng)
+        m = w.self_collision_pairs(q).cpu().numpy().astype(np.uint32)
+        mo = self_pairs(o, q, nthreads=NT)
+        assert np.array_equal(m, mo) and mo.any()
+        # accumulation: two halves OR to the whole
+        acc = w.self_collision_pairs(q[:1500])
+        acc = w.self_collision_pairs(q[1500:], mask=acc).cpu().numpy().astype(np.uint32)
+        assert np.array_equal(acc, mo)
+        w.close()
+    W = WorldModel([sc.arm(7, rings=8, segments=8)], env)
+    col = RandomizedSelfCollisionPairs(W.robot(0), 500, seed=3)
+    assert col.shape == (7, 7) and not col[0, 1] and col.any()
+    W.close()
