@@ -239,6 +239,23 @@ def secondary_metrics(reps: int = 2) -> dict:
     t0 = time.perf_counter()
     raycast(o1, s_cpu, d_cpu, nthreads=cores)
     cpu_rate = len(s_cpu) / (time.perf_counter() - t0)
+    # batched IK: 65,536 point + rotation targets for the 7-DOF arm
+    B_ik = 65536
+    rng_ik = np.random.default_rng(2002)
+    qt = rng_ik.uniform(-2.5, 2.5, (B_ik, 7)).astype(np.float32)
+    T_ik = w1.fk(qt).cpu().numpy()[:, 6]
+    pl_ik = np.tile(np.array([0.0, 0.0, 0.3], np.float32), (B_ik, 1))
+    pt_ik = (np.einsum("bij,bj->bi", T_ik[:, :9].reshape(B_ik, 3, 3), pl_ik) + T_ik[:, 9:]).astype(np.float32)
+    q0_ik = np.clip(qt + rng_ik.normal(0, 0.3, qt.shape), -np.pi, np.pi).astype(np.float32)
+    q0d, pld, ptd = (torch.as_tensor(x).cuda() for x in (q0_ik, pl_ik, pt_ik))
+    Rtd = torch.as_tensor(np.ascontiguousarray(T_ik[:, :9])).cuda()
+    ik_out = []
+    ms_ik = _event_ms(lambda: ik_out.append(w1.ik_solve(q0d, 6, pld, ptd, Rtarget=Rtd, tol=1e-4, sync=False)), reps)
+    w1.sync()
+    out["ik_solve"] = {"value": B_ik / (ms_ik / 1e3), "unit": "IK solves/s",
+                       "sample": "65,536 point + rotation targets of a 7-DOF arm, starts perturbed by N(0, 0.3) rad, "
+                                 "tol 1e-4, <= 100 iterations",
+                       "solved_fraction": float(ik_out[-1][1].float().mean().item())}
     out["raycast"] = {"value": Sd.shape[0] / (ms / 1e3), "unit": "rays/s",
                       "sample": "4 pinhole cameras x 640x480 rays into 2,000 icospheres (640k tris); first hit, "
                                 "FP64 parameter and point",

@@ -184,6 +184,20 @@ kgpu_status kgpu_world_reset_stats(kgpu_world world);
 kgpu_status kgpu_fk(kgpu_world world, int32_t robot, const float* q, int32_t B, float* T_out,
                     float* err_out, kgpu_stream stream);
 
+/* Batched inverse kinematics: B problems, each moving point plocal[b] (link
+ * frame) of link links[b] (or `link` when links is NULL) to ptarget[b] and,
+ * when Rtarget is not NULL, the link's rotation to Rtarget[b] (row-major).
+ * q [B * num_links]: initial guesses in, results out (clamped to the joint
+ * limits).  ok[b] = 1 when max |residual| <= tol within max_iters
+ * iterations, residual[b] = that maximum, iters[b] (may be NULL) the
+ * iterations used.  Replaces IKSolver.solve over IKObjective point and
+ * transform constraints (Python/klampt/src/robotik.cpp:556-689), one call for
+ * B problems; the iteration is damped least squares (Levenberg-Marquardt) on
+ * the link's ancestor DOFs, the reference's KrisLibrary solver being absent. */
+kgpu_status kgpu_ik_solve(kgpu_world world, int32_t robot, int32_t B, float* q, const int32_t* links, int32_t link,
+                          const float* plocal, const float* ptarget, const float* Rtarget, int32_t max_iters,
+                          float tol, uint8_t* ok, float* residual, int32_t* iters, kgpu_stream stream);
+
 /* Self-collision pairs that occur in a batch of B configurations: for every
  * enabled link pair (i < j) found colliding in some configuration, bit j of
  * pair_mask[i] is set (pair_mask: num_links words, OR-accumulated, so calls

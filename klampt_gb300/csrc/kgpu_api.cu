@@ -929,6 +929,22 @@ kgpu_status kgpu_softmin_grad(kgpu_world w, int32_t robot, const float* q, int32
                        "kgpu_softmin_grad");
 }
 
+kgpu_status kgpu_ik_solve(kgpu_world w, int32_t robot, int32_t B, float* q, const int32_t* links, int32_t link,
+                          const float* plocal, const float* ptarget, const float* Rtarget, int32_t max_iters,
+                          float tol, uint8_t* ok, float* residual, int32_t* iters, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && (!q || !plocal || !ptarget || !ok || !residual)))
+    return fail(KGPU_ERR_INVALID, "bad buffers");
+  const int nl = w->robots[robot]->nlinks;
+  if (!links && (link < 0 || link >= nl)) return fail(KGPU_ERR_INVALID, "link %d out of range [0,%d)", link, nl);
+  if (max_iters < 0 || !(tol > 0)) return fail(KGPU_ERR_INVALID, "max_iters must be >= 0 and tol > 0");
+  return launch_status(launch_ik(w->d_dev, robot, B, q, links, link, plocal, ptarget, Rtarget, max_iters, tol, ok,
+                                 residual, iters, (cudaStream_t)s),
+                       "kgpu_ik_solve");
+}
+
 kgpu_status kgpu_self_collision_pairs(kgpu_world w, int32_t robot, const float* q, int32_t B, uint32_t* pair_mask,
                                       kgpu_stream s)
 {

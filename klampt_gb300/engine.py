@@ -277,6 +277,32 @@ class World:
             self.sync()
         return out, g
 
+    def ik_solve(self, q0, links, plocal, ptarget, Rtarget=None, max_iters: int = 100, tol: float = 1e-3,
+                 robot: int = 0, sync: bool = True):
+        """Batched IK from initial guesses q0 [B, L]: (q [B, L], ok [B],
+        residual [B], iters [B]).  Rtarget [B, 9] (row-major) adds the
+        orientation constraint."""
+        L = self.robots[robot].num_links
+        q = _dev(q0, torch.float32).reshape(-1, L).clone()
+        B = q.shape[0]
+        pl = _dev(plocal, torch.float32).reshape(-1, 3)
+        pl = (pl.expand(B, 3) if pl.shape[0] == 1 else pl).contiguous()
+        pt = _dev(ptarget, torch.float32).reshape(B, 3).contiguous()
+        Rt = None if Rtarget is None else _dev(Rtarget, torch.float32).reshape(B, 9).contiguous()
+        ok = torch.empty(B, dtype=torch.uint8, device="cuda")
+        res = torch.empty(B, dtype=torch.float32, device="cuda")
+        its = torch.empty(B, dtype=torch.int32, device="cuda")
+        if isinstance(links, (int, np.integer)):
+            ld, lk = None, int(links)
+        else:
+            ld, lk = _dev(links, torch.int32).reshape(B).contiguous(), 0
+        check(lib().kgpu_ik_solve(self.handle, robot, B, _dptr(q), None if ld is None else _dptr(ld), lk, _dptr(pl),
+                                  _dptr(pt), None if Rt is None else _dptr(Rt), int(max_iters), float(tol),
+                                  _dptr(ok), _dptr(res), _dptr(its), _stream()))
+        if sync:
+            self.sync()
+        return q, ok, res, its
+
     def self_collision_pairs(self, q, robot: int = 0, mask=None, sync: bool = True):
         """Self pairs colliding in some configuration of q [B, L]: uint32
         words [L] (bit j of word i: pair (i, j)), OR-accumulated into `mask`

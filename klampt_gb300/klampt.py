@@ -17,6 +17,9 @@ Mirrors (paths relative to the Klamp't tree):
                                    part), Python/klampt/model/collide.py:219-243
   RobotModelLink.getJacobian / getPositionJacobian / getOrientationJacobian
                                    Python/klampt/src/robotsim.cpp:4817-4860
+  IKObjective / IKSolver (one objective)
+                                   Python/klampt/src/robotik.h:21-260
+  RandomizedSelfCollisionPairs     Cpp/Modeling/RandomizedSelfCollisions.h:24
 Batched overloads: RobotModel.setConfigs / getJacobians, WorldCollider.check_configs /
 distance_batch / rayCastBatch, RobotCSpace.isFeasibleBatch / isVisibleBatch.
 
@@ -274,6 +277,62 @@ class WorldCollider:
         """(d [B], (link, object) [B, 2], closest points [B, 6], dd/dq [B, L])."""
         d, pair, cp, g = self.world.engine.distance(Q, cutoff, robot=robot)
         return d.cpu().numpy(), pair.cpu().numpy(), cp.cpu().numpy(), g.cpu().numpy()
+
+
+class IKObjective:
+    """One point (or point + rotation) constraint on a link
+    (robotik.h:21-60: setFixedPoint, setFixedTransform)."""
+
+    def __init__(self):
+        self.link = -1
+        self.plocal = [0.0, 0.0, 0.0]
+        self.pworld = [0.0, 0.0, 0.0]
+        self.R = None  # row-major 3x3 when the rotation is constrained
+
+    def setFixedPoint(self, link: int, plocal: Sequence[float], pworld: Sequence[float]):
+        self.link, self.plocal, self.pworld, self.R = int(link), list(plocal), list(pworld), None
+
+    def setFixedTransform(self, link: int, R: Sequence[float], t: Sequence[float]):
+        """R in Klamp't's so3 order (column-major), t the link origin."""
+        Rm = np.asarray(R, np.float64).reshape(3, 3).T
+        self.link, self.plocal, self.pworld, self.R = int(link), [0.0, 0.0, 0.0], list(t), Rm.reshape(-1).tolist()
+
+
+class IKSolver:
+    """IKSolver (robotik.h:151-260) for one objective: solve() starts from
+    the robot's current configuration and leaves the result in it."""
+
+    def __init__(self, robot: "RobotModel"):
+        self.robot = robot
+        self.objectives: List[IKObjective] = []
+        self.maxIters = 100
+        self.tol = 1e-3
+        self._residual = None
+
+    def add(self, objective: IKObjective):
+        if self.objectives:
+            raise RuntimeError("one objective per solver on this path")
+        self.objectives.append(objective)
+
+    def setMaxIters(self, iters: int):
+        self.maxIters = int(iters)
+
+    def setTolerance(self, tol: float):
+        self.tol = float(tol)
+
+    def solve(self) -> bool:
+        obj = self.objectives[0]
+        r = self.robot
+        Rt = None if obj.R is None else np.asarray(obj.R, np.float32)[None]
+        q, ok, res, _ = r.world.engine.ik_solve(r._q[None], obj.link, np.asarray(obj.plocal, np.float32)[None],
+                                                np.asarray(obj.pworld, np.float32)[None], Rtarget=Rt,
+                                                max_iters=self.maxIters, tol=self.tol, robot=r.index)
+        r.setConfig(q.cpu().numpy()[0].astype(np.float64))
+        self._residual = float(res.cpu().numpy()[0])
+        return bool(ok.cpu().numpy()[0])
+
+    def getResidualMax(self) -> float:
+        return self._residual
 
 
 def RandomizedSelfCollisionPairs(robot: "RobotModel", numSamples: int, seed: int = 0) -> np.ndarray:

@@ -992,6 +992,137 @@ int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, i
   return 0;
 }
 
+/* Batched inverse kinematics, the same Levenberg-Marquardt iteration as the
+   engine's (klampt_gb300/csrc/kgpu_ik.cu) in FP64: residual e = [p(q) - p*]
+   or [p(q) - p*; 1/2 sum_k R*_k x R_k], steps -J^T (J J^T + mu I)^-1 e on the
+   link's ancestor DOFs, clamped to the limits, mu / 4 on an accepted step,
+   mu * 8 on a rejected one, converged at max |e_i| <= tol.  q: [B, L] in/out. */
+int orc_ik(void* robot, int B, double* q, const int* links, const double* plocal, const double* ptarget,
+           const double* Rtarget, int max_iters, double tol, unsigned char* ok, double* residual, int* iters)
+{
+  Robot* R = (Robot*)robot;
+  const int L = R->L;
+  const int m = Rtarget ? 6 : 3;
+  std::vector<double> T((size_t)L * 12), Tn((size_t)L * 12);
+  auto resid = [&](const std::vector<double>& TT, int b, int li, double* e) {
+    double p[3];
+    kx_xform_point(&TT[12 * (size_t)li], plocal + 3 * (size_t)b, p);
+    for (int k = 0; k < 3; ++k) e[k] = p[k] - ptarget[3 * (size_t)b + k];
+    if (m == 6) {
+      const double* Rt = Rtarget + 9 * (size_t)b;
+      const double* Rq = &TT[12 * (size_t)li];
+      double ex = 0, ey = 0, ez = 0;
+      for (int k = 0; k < 3; ++k) {
+        const double ax = Rt[k], ay = Rt[3 + k], az = Rt[6 + k], bx = Rq[k], by = Rq[3 + k], bz = Rq[6 + k];
+        ex += ay * bz - az * by;
+        ey += az * bx - ax * bz;
+        ez += ax * by - ay * bx;
+      }
+      e[3] = 0.5 * ex;
+      e[4] = 0.5 * ey;
+      e[5] = 0.5 * ez;
+    }
+  };
+  for (int b = 0; b < B; ++b) {
+    double* qb = q + (size_t)b * L;
+    const int li = links[b];
+    std::vector<char> active(L, 0);
+    for (int j = li; j >= 0; j = R->parents[j]) active[j] = R->jtypes[j] != KX_JOINT_WELD;
+    for (int i = 0; i < L; ++i) qb[i] = std::min(std::max(qb[i], R->qmin[i]), R->qmax[i]);
+    orc_fk(R, qb, T.data());
+    double e[6], en[6];
+    resid(T, b, li, e);
+    double E = 0, emax = 0;
+    for (int a = 0; a < m; ++a) { E += e[a] * e[a]; emax = std::max(emax, fabs(e[a])); }
+    double mu = 1e-4;
+    int it = 0;
+    std::vector<double> J((size_t)6 * L), qn(L);
+    for (; it < max_iters && emax > tol; ++it) {
+      double p[3];
+      kx_xform_point(&T[12 * (size_t)li], plocal + 3 * (size_t)b, p);
+      std::fill(J.begin(), J.end(), 0.0);
+      for (int j = 0; j < L; ++j) {
+        if (!active[j]) continue;
+        const double* Tj = &T[12 * (size_t)j];
+        const double* ax = &R->axes[3 * (size_t)j];
+        double w[3];
+        for (int r = 0; r < 3; ++r) w[r] = Tj[3 * r] * ax[0] + Tj[3 * r + 1] * ax[1] + Tj[3 * r + 2] * ax[2];
+        if (R->jtypes[j] == KX_JOINT_REVOLUTE) {
+          const double rx = p[0] - Tj[9], ry = p[1] - Tj[10], rz = p[2] - Tj[11];
+          J[0 * L + j] = w[1] * rz - w[2] * ry;
+          J[1 * L + j] = w[2] * rx - w[0] * rz;
+          J[2 * L + j] = w[0] * ry - w[1] * rx;
+          J[3 * L + j] = w[0];
+          J[4 * L + j] = w[1];
+          J[5 * L + j] = w[2];
+        } else {
+          J[0 * L + j] = w[0];
+          J[1 * L + j] = w[1];
+          J[2 * L + j] = w[2];
+        }
+      }
+      double A[6][6], Lc[6][6], y[6], z[6];
+      bool spd = true;
+      for (int r = 0; r < m; ++r)
+        for (int s = 0; s <= r; ++s) {
+          double v = 0;
+          for (int j = 0; j < L; ++j) v += J[r * L + j] * J[s * L + j];
+          A[r][s] = v + (r == s ? mu : 0.0);
+        }
+      for (int r = 0; r < m; ++r)
+        for (int s = 0; s <= r; ++s) {
+          double v = A[r][s];
+          for (int t = 0; t < s; ++t) v -= Lc[r][t] * Lc[s][t];
+          if (s == r) {
+            spd = spd && v > 0;
+            Lc[r][r] = sqrt(std::max(v, 1e-300));
+          } else {
+            Lc[r][s] = v / Lc[s][s];
+          }
+        }
+      if (!spd) {
+        mu *= 8;
+        if (mu > 1e6) break;
+        continue;
+      }
+      for (int r = 0; r < m; ++r) {
+        double v = e[r];
+        for (int t = 0; t < r; ++t) v -= Lc[r][t] * z[t];
+        z[r] = v / Lc[r][r];
+      }
+      for (int r = m - 1; r >= 0; --r) {
+        double v = z[r];
+        for (int t = r + 1; t < m; ++t) v -= Lc[t][r] * y[t];
+        y[r] = v / Lc[r][r];
+      }
+      for (int j = 0; j < L; ++j) {
+        double dq = 0;
+        for (int r = 0; r < m; ++r) dq -= J[r * L + j] * y[r];
+        qn[j] = std::min(std::max(qb[j] + dq, R->qmin[j]), R->qmax[j]);
+      }
+      orc_fk(R, qn.data(), Tn.data());
+      resid(Tn, b, li, en);
+      double En = 0, enmax = 0;
+      for (int a = 0; a < m; ++a) { En += en[a] * en[a]; enmax = std::max(enmax, fabs(en[a])); }
+      if (En < E) {
+        for (int j = 0; j < L; ++j) qb[j] = qn[j];
+        T.swap(Tn);
+        for (int a = 0; a < m; ++a) e[a] = en[a];
+        E = En;
+        emax = enmax;
+        mu = std::max(mu * 0.25, 1e-10);
+      } else {
+        mu *= 8;
+        if (mu > 1e6) break;
+      }
+    }
+    ok[b] = emax <= tol;
+    residual[b] = emax;
+    if (iters) iters[b] = it;
+  }
+  return 0;
+}
+
 /* Self-collision pairs occurring over B configurations (the sampling loop of
    RandomizedSelfCollisionPairs, Cpp/Modeling/RandomizedSelfCollisions.cpp:
    19-38): bit j of mask[i] (i < j) is set when enabled pair (i, j) collides

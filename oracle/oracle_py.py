@@ -40,7 +40,7 @@ def lib():
         L.orc_robot_create.restype = P
         L.orc_env_create.restype = P
         for name in ("orc_check_configs", "orc_check_edges", "orc_is_feasible", "orc_pair_distance",
-                     "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian", "orc_self_pairs"):
+                     "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian", "orc_self_pairs", "orc_ik"):
             getattr(L, name).restype = ctypes.c_int
         L.orc_robot_destroy.argtypes = [P]
         L.orc_env_destroy.argtypes = [P]
@@ -186,6 +186,23 @@ class Oracle:
                           _p(q), ctypes.c_int(T), ctypes.c_int(W), ctypes.c_double(tau),
                           _p(Lout), _p(grad), ctypes.c_int(nthreads))
         return Lout, grad
+
+
+def ik_solve(oracle: "Oracle", q0, links, plocal, ptarget, Rtarget=None, max_iters=100, tol=1e-3):
+    """FP64 restatement of the engine's IK iteration: (q, ok, residual, iters)."""
+    L = oracle.nl
+    q = np.ascontiguousarray(q0, dtype=np.float64).reshape(-1, L).copy()
+    B = q.shape[0]
+    links = np.ascontiguousarray(links, np.int32).reshape(B)
+    pl = np.ascontiguousarray(plocal, np.float64).reshape(B, 3)
+    pt = np.ascontiguousarray(ptarget, np.float64).reshape(B, 3)
+    Rt = None if Rtarget is None else np.ascontiguousarray(Rtarget, np.float64).reshape(B, 9)
+    ok = np.zeros(B, np.uint8)
+    res = np.zeros(B, np.float64)
+    its = np.zeros(B, np.int32)
+    lib().orc_ik(ctypes.c_void_p(oracle.robot), ctypes.c_int(B), _p(q), _p(links), _p(pl), _p(pt), _p(Rt),
+                 ctypes.c_int(max_iters), ctypes.c_double(tol), _p(ok), _p(res), _p(its))
+    return q, ok, res, its
 
 
 def self_pairs(oracle: "Oracle", q, nthreads: int = 1, mask=None) -> np.ndarray:

@@ -279,3 +279,25 @@ def test_oracle_jacobian_matches_finite_differences():
             dR = (Tp[li, :9] - Tm[li, :9]).reshape(3, 3) / (2 * h)
             Om = dR @ o.fk(q[b].astype(np.float64))[li, :9].reshape(3, 3).T
             assert np.allclose([Om[2, 1], Om[0, 2], Om[1, 0]], J[b, :3, j], atol=1e-6)
+
+
+def test_oracle_ik_reaches_reachable_targets():
+    """The FP64 IK restatement: targets made by FK of random configurations
+    are reached from perturbed starts (position, and position + rotation)."""
+    from oracle.oracle_py import Oracle, ik_solve
+    robot = sc.arm(7, rings=4, segments=8)
+    o = Oracle(robot, sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))]))
+    rng = np.random.default_rng(11)
+    B = 64
+    qt = rng.uniform(-2.5, 2.5, (B, 7))
+    pl = np.tile([0.0, 0.0, 0.3], (B, 1))
+    T = np.stack([o.fk(x)[6] for x in qt])
+    pt = np.einsum("bij,bj->bi", T[:, :9].reshape(B, 3, 3), pl) + T[:, 9:]
+    q0 = np.clip(qt + rng.normal(0, 0.3, qt.shape), -math.pi, math.pi)
+    q, ok, res, its = ik_solve(o, q0, np.full(B, 6), pl, pt, tol=1e-6)
+    assert ok.mean() > 0.9 and (res[ok == 1] <= 1e-6).all()
+    for b in np.nonzero(ok)[0][:8]:
+        Tb = o.fk(q[b])[6]
+        assert np.abs(Tb[:9].reshape(3, 3) @ pl[b] + Tb[9:] - pt[b]).max() <= 1e-6
+    q, ok, res, its = ik_solve(o, q0, np.full(B, 6), pl, pt, Rtarget=T[:, :9], tol=1e-6)
+    assert ok.mean() > 0.8
