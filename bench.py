@@ -224,6 +224,27 @@ def secondary_metrics(reps: int = 2) -> dict:
     out["hetero_configs"] = {"value": len(ids) / (ms / 1e3), "unit": "configs/s",
                              "sample": "65,536 configs of 6/7/12/30-DOF robots (40/30/20/10%), 1.0M-tri environment, one launch"}
     w3.close()
+    # environment creation (tree build + upload), host median split vs GPU
+    # linear BVH, and the same hetero batch through the GPU-built trees
+    from klampt_gb300.engine import Environment
+    Environment(sc.env_from_objects("warm", sc.random_boxes(4, np.random.default_rng(0))), gpu_build=True).close()
+    build_ms = {}
+    for name, e in (("env_1M_objects", env3), ("env_terrain_1M", env4)):
+        row = {"tris": e.num_tris}
+        for key, flag in (("host_ms", False), ("gpu_ms", True)):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            h = Environment(e, gpu_build=flag)
+            torch.cuda.synchronize()
+            row[key] = (time.perf_counter() - t0) * 1e3
+            h.close()
+        build_ms[name] = row
+    w3g = World(env3, robots, gpu_build=True)
+    ms_g = _event_ms(lambda: w3g.check_configs_multi(ids_d, q3d, sync=False), reps)
+    w3g.sync()
+    w3g.close()
+    out["env_build"] = {"unit": "ms (wall clock, kgpu_env_create_ex)", "scenes": build_ms,
+                        "hetero_configs_gpu_built": {"value": len(ids) / (ms_g / 1e3), "unit": "configs/s"}}
     # ray casting: four 640x480 pinhole cameras into the icosphere field
     robot1, env1, _ = sc.scene_cfg1(n_edges=2)
     w1 = World(env1, [robot1])

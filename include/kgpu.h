@@ -129,6 +129,17 @@ kgpu_status kgpu_robot_destroy(kgpu_robot robot);
  * for distance queries) and uploads them.  Replaces WorldModel geometry
  * initialisation (Cpp/Modeling/World.cpp:266-284). */
 kgpu_status kgpu_env_create(const kgpu_env_desc* desc, kgpu_env* out);
+
+/* kgpu_env_create with build flags.  KGPU_ENV_BUILD_GPU builds the
+ * environment trees on the current GPU (linear BVH: Morton-code radix sort
+ * and radix tree, boxes bottom up) instead of the host median-split builder;
+ * the layout, the results of every query and the FP32 conservativeness are
+ * the same, the tree shape (and so the traversal cost) differs.  The host
+ * builder stands in for the PQP precompute InitCollisions runs
+ * (Cpp/Modeling/World.cpp:266-274); the GPU build is for scenes whose
+ * precompute dominates. */
+#define KGPU_ENV_BUILD_GPU 1
+kgpu_status kgpu_env_create_ex(const kgpu_env_desc* desc, int32_t flags, kgpu_env* out);
 kgpu_status kgpu_env_destroy(kgpu_env env);
 
 /* Joins an environment and robots.  Collision masks start at Klamp't's

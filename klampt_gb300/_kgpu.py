@@ -66,6 +66,7 @@ _SIGS = {
     "kgpu_robot_create": [_c_p, _c_p],
     "kgpu_robot_destroy": [_c_p],
     "kgpu_env_create": [_c_p, _c_p],
+    "kgpu_env_create_ex": [_c_p, _i32, _c_p],
     "kgpu_env_destroy": [_c_p],
     "kgpu_world_create": [_c_p, _c_p, _i32, _c_p],
     "kgpu_world_destroy": [_c_p],

@@ -22,7 +22,8 @@ OUT_DIR = os.path.join(PKG, "_lib")
 OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libkgpu.so")
 
-CU_SOURCES = ["kgpu_api.cu", "kgpu_collide.cu", "kgpu_plain.cu", "kgpu_dist.cu", "kgpu_noalloc.cu", "kgpu_ray.cu", "kgpu_ik.cu"]
+CU_SOURCES = ["kgpu_api.cu", "kgpu_collide.cu", "kgpu_plain.cu", "kgpu_dist.cu", "kgpu_noalloc.cu", "kgpu_ray.cu", "kgpu_ik.cu",
+              "kgpu_lbvh.cu"]
 CPP_SOURCES = ["bvh.cpp"]
 HEADERS = ["kgpu_internal.h", "kgpu_device.cuh"]
 INCLUDE_HEADERS = ["kgpu.h", "kgpu_exact.h"]

@@ -371,9 +371,12 @@ kgpu_status kgpu_robot_destroy(kgpu_robot r)
   return KGPU_OK;
 }
 
-kgpu_status kgpu_env_create(const kgpu_env_desc* d, kgpu_env* out)
+kgpu_status kgpu_env_create(const kgpu_env_desc* d, kgpu_env* out) { return kgpu_env_create_ex(d, 0, out); }
+
+kgpu_status kgpu_env_create_ex(const kgpu_env_desc* d, int32_t flags, kgpu_env* out)
 {
   if (!d || !out) return fail(KGPU_ERR_INVALID, "null argument");
+  if (flags & ~KGPU_ENV_BUILD_GPU) return fail(KGPU_ERR_INVALID, "unknown environment build flag");
   *out = nullptr;
   int N = d->num_objects;
   if (N < 0 || (N > 0 && (!d->vert_offset || !d->tri_offset)))
@@ -434,7 +437,15 @@ kgpu_status kgpu_env_create(const kgpu_env_desc* d, kgpu_env* out)
       }
     if (ids.empty()) continue;
     HostBvh& b = E->gbvh[g];
-    build_bvh(E->tri64, ids, &E->tri_obj, b);
+    if (flags & KGPU_ENV_BUILD_GPU) {
+      cudaError_t be = lbvh_build(E->tri64, ids, E->tri_obj, b);
+      if (be != cudaSuccess) {
+        delete E;
+        return cuda_fail(be, "environment tree build on the GPU");
+      }
+    } else {
+      build_bvh(E->tri64, ids, &E->tri_obj, b);
+    }
     int node_base = (int)nodes.size(), tri_base = (int)leaf_tris.size();
     append_bvh(b, node_base, tri_base, nodes, node64);
     for (size_t k = 0; k < b.nodes.size(); ++k) {

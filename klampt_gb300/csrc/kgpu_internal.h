@@ -54,6 +54,11 @@ struct HostBvh {
 void build_bvh(const std::vector<double>& tri, const std::vector<int>& ids,
                const std::vector<int>* tri_obj, HostBvh& out);
 
+// The same object-aware layout built on the current GPU (linear BVH over
+// Morton codes; kgpu_lbvh.cu).  tri_obj maps every triangle id to its object.
+cudaError_t lbvh_build(const std::vector<double>& tri, const std::vector<int>& ids, const std::vector<int>& tri_obj,
+                       HostBvh& out);
+
 // Device tables of one robot (read through the read-only cache).
 struct KRobotDev {
   int nlinks;

@@ -63,9 +63,12 @@ class Robot:
 
 
 class Environment:
-    """Static environment handle from a scenes.EnvSpec-like object."""
+    """Static environment handle from a scenes.EnvSpec-like object.
 
-    def __init__(self, spec):
+    ``gpu_build`` builds the environment trees on the GPU (linear BVH) instead
+    of the host builder; every query gives the same results with either."""
+
+    def __init__(self, spec, gpu_build: bool = False):
         self.spec = spec
         p = spec.packed()
         self._arrays = p
@@ -73,7 +76,7 @@ class Environment:
                           verts=_ptr(p["verts"]), tri_offset=_ptr(p["tri_offset"]), tris=_ptr(p["tris"]),
                           groups=_ptr(p["groups"]), convex=_ptr(p["convex"]), margins=_ptr(p["margins"]))
         h = ctypes.c_void_p()
-        check(lib().kgpu_env_create(ctypes.byref(d), ctypes.byref(h)))
+        check(lib().kgpu_env_create_ex(ctypes.byref(d), 1 if gpu_build else 0, ctypes.byref(h)))
         self.handle = h
 
     def close(self):
@@ -112,8 +115,8 @@ class EdgePlan:
 class World:
     """An environment plus robots on the current CUDA device."""
 
-    def __init__(self, env_spec, robot_specs: Sequence):
-        self.env = Environment(env_spec) if env_spec is not None else None
+    def __init__(self, env_spec, robot_specs: Sequence, gpu_build: bool = False):
+        self.env = Environment(env_spec, gpu_build=gpu_build) if env_spec is not None else None
         self.robots: List[Robot] = [Robot(s) for s in robot_specs]
         arr = (ctypes.c_void_p * len(self.robots))(*[r.handle.value for r in self.robots])
         h = ctypes.c_void_p()
