@@ -166,14 +166,16 @@ kgpu_status kgpu_world_enable_self_pair(kgpu_world world, int32_t robot, int32_t
  * top of the computed error bounds, default 0), "blocks_per_sm" (2, 3 or 4
  * resident engine blocks per SM), "grab" (work items per queue atomic, 1..16),
  * "job_flush" (triangle-pair jobs batched before testing, 8..64),
- * "edge_chunk" (consecutive steps of an edge checked in order by one work
- * item, 1..64, default 4), "fp64_inline" (1: triangle pairs the FP32 tests
+ * "edge_chunk" (consecutive steps of an edge per work item, 1..64, default
+ * 16; the item checks them in groups of 32 / L steps, L the robot's link
+ * count rounded up to 8, 16 or 32, earliest step first), "fp64_inline" (1: triangle pairs the FP32 tests
  * leave undecided get the FP64 test inside the traversal kernel; 0: they are
  * listed and decided by a second kernel, keeping FP64 code out of the
  * traversal kernel; -1, the default: 0 for edge batches, 1 for configuration
  * batches), read-only
  * "eps_env", "warps_per_block", "num_sms".  The autotuner
- * (klampt_gb300/autotune.py) sets blocks_per_sm, grab and job_flush.
+ * (klampt_gb300/autotune.py) sets blocks_per_sm, grab, job_flush and
+ * edge_chunk or fp64_inline.
  * Unknown names are KGPU_ERR_INVALID. */
 kgpu_status kgpu_world_set_option(kgpu_world world, const char* name, double value);
 kgpu_status kgpu_world_get_option(kgpu_world world, const char* name, double* value);

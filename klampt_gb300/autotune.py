@@ -9,7 +9,7 @@ and, for configuration batches,
   fp64_inline    0, 1      (FP64 triangle tests deferred to a second kernel,
                             or inline in the traversal)
 or, for edge batches (FP64 tests always deferred there),
-  edge_chunk     2, 4, 8   (consecutive steps of an edge per work item)
+  edge_chunk     8, 16, 32 (consecutive steps of an edge per work item)
 times each with CUDA events (median of `reps` after one warm-up) and leaves
 the fastest setting in the world.  Results are identical for every setting; only
 the time changes.
@@ -26,7 +26,7 @@ from .engine import World
 
 _BASE = {"blocks_per_sm": (2, 3, 4), "grab": (1, 2, 4), "job_flush": (32, 64)}
 GRID = dict(_BASE, fp64_inline=(0, 1))
-GRID_EDGES = dict(_BASE, fp64_inline=(0,), edge_chunk=(2, 4, 8))
+GRID_EDGES = dict(_BASE, fp64_inline=(0,), edge_chunk=(8, 16, 32))
 
 
 def _time(fn: Callable[[], None], reps: int) -> float:

@@ -48,7 +48,7 @@ constexpr int kJobCap = 96;
 constexpr int kGrab = 2;  // items taken from the queue per atomic
 constexpr int kWarps = 8; // warps per block
 constexpr int kMaxChunk = 64;  // most consecutive edge steps per work item
-constexpr int kDefaultChunk = 4;
+constexpr int kDefaultChunk = 16;
 constexpr int kTailItemsPerWarp = 16;  // single-step rounds once fewer items than this per warp remain
 
 enum Mode { MODE_CONFIGS = 0, MODE_FEASIBLE = 1, MODE_EDGES = 2 };
@@ -63,6 +63,7 @@ struct __align__(16) WarpSmem {
   float T[kMaxLinks][12];
   float delta[kMaxLinks];     // per-link bound on |FP32 - exact| world coordinates
   float gerr[kMaxLinks];      // per-link max |R^T R - I| of the FP32 rotation (+ rounding)
+  float tol64[64];            // box-test tolerance parts: rows 0-31 per link row, 32-63 per group
   double q64[kMaxLinks];      // canonical FP64 joint values (filled with T64)
   const float* item_qa;       // the item's joint values: configuration, or edge
   const float* item_qb;       //   endpoints qa/qb (item_qb null for configurations)
@@ -70,6 +71,7 @@ struct __align__(16) WarpSmem {
   int item_id;                // configuration index b, or edge index e
   int item_rid;               // robot of the item
   int don_top;                // stack entries handed over by a sibling warp
+  int don_glim;               // steps of the handed-over group still to decide
 };
 
 // Work sharing inside a block once the queue is drained (edge batches, whose
@@ -148,28 +150,33 @@ struct Cnt {
   unsigned long long node_pairs = 0, tri_pairs = 0, band = 0, spills = 0, cert = 0, hit64 = 0;
 };
 
-// Result of one query set.
-enum { TR_FREE = 0, TR_HIT = 1, TR_OVERFLOW = 2 };
+// A traversal returns the number of leading steps of its group found free
+// (the first step with a contact; the group size when none), or TR_OVERFLOW.
+enum { TR_OVERFLOW = -1 };
 
 __device__ __forceinline__ uint2 make_entry(int nodeA, int la, int tgt, int nodeB)
 {
   return make_uint2((uint32_t)nodeB, (uint32_t)nodeA | ((uint32_t)la << 20) | ((uint32_t)tgt << 25));
 }
 
-// Tests the triangle-pair jobs of the warp, one triangle pair per lane;
-// returns true on a confirmed contact.  Per pair: FP32 separating-axis filter
+// Tests the triangle-pair jobs of the warp, one triangle pair per lane.
+// Triangle-pair jobs of a step group: steps g < glim are live (a job's step
+// is its link row >> lgL).  Per pair: FP32 separating-axis filter
 // (separated beyond the band: done), FP32 intersection certificate (crossing
 // beyond the band: contact), otherwise the pair is undecided in FP32.  The
 // main pass (FP64 = false) appends such a pair to A.pend and goes on (k_band
-// decides it afterwards); the fallback pass (FP64 = true) decides it here
-// with the FP64 test on transforms computed once per configuration (fk64
-// tracks whether T64 is valid).  Keeping the FP64 code out of the main
-// pass's kernel keeps that kernel's hot loop in the instruction cache.
+// decides it afterwards); the fallback pass (FP64 = true, groups of one step)
+// decides it here with the FP64 test on transforms computed once per
+// configuration (fk64 tracks whether T64 is valid).  Keeping the FP64 code
+// out of the main pass's kernel keeps that kernel's hot loop in the
+// instruction cache.  A contact at step g lowers glim to g: later steps of
+// the group need no decision, earlier ones still do.  Returns the new glim.
 template <bool FP64>
-__device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
-                                      int njobs, int lane, double (*T64)[12], int& fk64, const EngineArgs& A,
-                                      Cnt& cnt)
+__device__ __noinline__ int run_jobs(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                     int njobs, int lane, double (*T64)[12], int& fk64, const EngineArgs& A,
+                                     Cnt& cnt, int glim, int lgL)
 {
+  const int lmask = (1 << lgL) - 1;
   // exclusive prefix over job sizes
   uint32_t carry = 0;
 #pragma unroll 1
@@ -199,7 +206,7 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
   for (uint32_t base = 0; base < total; base += 32) {
     uint32_t p = base + lane;
     bool band = false, certain = false;
-    int la = 0, tgt = 0, tA = 0, tB = 0;
+    int la = 0, tgt = 0, tA = 0, tB = 0, step = 32;
     if (p < total) {
       // job holding p: largest j with jobOff[j] <= p
       int lo = 0, hi = njobs - 1;
@@ -208,46 +215,55 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
         if (S.jobOff[mid] <= p) lo = mid; else hi = mid - 1;
       }
       const int j = lo;
-      const uint32_t r = p - S.jobOff[j];
       const uint32_t jm = S.jobM[j];
-      const uint32_t cb = ((jm >> 16) & 3u) + 1;
       la = jm & 0xff;
       tgt = (jm >> 8) & 0xff;
-      tA = (int)(S.jobA[j] & 0x0fffffffu) + (int)(r / cb);
-      tB = (int)S.jobB[j] + (int)(r % cb);
-      float3 P[3], Q[3];
-      const float* TA = S.T[la];
-      const bool self = tgt < 32;
-      const float* TB = S.T[self ? tgt : 0];
-      const float4* qsrc = self ? ltri : etri;
+      step = la >> lgL;
+      if (step < glim) {
+        const uint32_t r = p - S.jobOff[j];
+        const uint32_t cb = ((jm >> 16) & 3u) + 1;
+        tA = (int)(S.jobA[j] & 0x0fffffffu) + (int)(r / cb);
+        tB = (int)S.jobB[j] + (int)(r % cb);
+        float3 P[3], Q[3];
+        const float* TA = S.T[la];
+        const bool self = tgt < 32;
+        const float* TB = S.T[self ? tgt : 0];
+        const float4* qsrc = self ? ltri : etri;
 #pragma unroll
-      for (int v = 0; v < 3; ++v) {
-        float4 x = __ldg(ltri + 3 * (size_t)tA + v);
-        P[v] = xform32(TA, make_float3(x.x, x.y, x.z));
-        float4 y = __ldg(qsrc + 3 * (size_t)tB + v);
-        Q[v] = self ? xform32(TB, make_float3(y.x, y.y, y.z)) : make_float3(y.x, y.y, y.z);
+        for (int v = 0; v < 3; ++v) {
+          float4 x = __ldg(ltri + 3 * (size_t)tA + v);
+          P[v] = xform32(TA, make_float3(x.x, x.y, x.z));
+          float4 y = __ldg(qsrc + 3 * (size_t)tB + v);
+          Q[v] = self ? xform32(TB, make_float3(y.x, y.y, y.z)) : make_float3(y.x, y.y, y.z);
+        }
+        const float margin =
+            R.link_margin[la & lmask] + (self ? R.link_margin[tgt & lmask] : W->group_margin[tgt - 32]);
+        const float dA = S.delta[la] + W->eps_extra;
+        const float dB = (self ? S.delta[tgt] : W->eps_env) + W->eps_extra;
+        band = !tri_separated32(P, Q, dA + dB, margin);
+        if (band && margin == 0.f) certain = tri_certain_hit32(P[0], P[1], P[2], Q[0], Q[1], Q[2], fmaxf(dA, dB));
+        cnt.tri_pairs++;
       }
-      const float margin = R.link_margin[la] + (self ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
-      const float dA = S.delta[la] + W->eps_extra;
-      const float dB = (self ? S.delta[tgt] : W->eps_env) + W->eps_extra;
-      band = !tri_separated32(P, Q, dA + dB, margin);
-      if (band && margin == 0.f) certain = tri_certain_hit32(P[0], P[1], P[2], Q[0], Q[1], Q[2], fmaxf(dA, dB));
     }
-    cnt.tri_pairs += (p < total) ? 1 : 0;
     if (__any_sync(0xffffffffu, certain)) {
       cnt.cert++;
-      return true;
+      glim = min(glim, (int)__reduce_min_sync(0xffffffffu, certain ? (unsigned)step : 32u));
+      if (glim == 0) return 0;
     }
-    const bool need64 = band && !certain;
+    const bool need64 = band && !certain && step < glim;
     if (__any_sync(0xffffffffu, need64)) {
       if (!FP64) {
         const unsigned m = __ballot_sync(0xffffffffu, need64);
         unsigned at = 0;
         if (lane == 0) at = atomicAdd(A.pend_count, (unsigned)__popc(m));
         at = __shfl_sync(0xffffffffu, at, 0) + __popc(m & lanemask_lt());
-        if (need64 && at < (unsigned)A.pend_cap)
-          A.pend[at] = make_uint4((unsigned)S.item_id, (unsigned)S.item_k | ((unsigned)la << 16) | ((unsigned)tgt << 21),
+        if (need64 && at < (unsigned)A.pend_cap) {
+          // the record names the step and link indices (not link rows)
+          const unsigned tl = tgt < 32 ? (unsigned)(tgt & lmask) : (unsigned)tgt;
+          A.pend[at] = make_uint4((unsigned)S.item_id,
+                                  (unsigned)(S.item_k + step) | ((unsigned)(la & lmask) << 16) | (tl << 21),
                                   (unsigned)tA, (unsigned)tB);
+        }
       } else {
         ensure_fk64(S, R, T64, lane, fk64);
         int hit = 0;
@@ -257,12 +273,13 @@ __device__ __noinline__ bool run_jobs(WarpSmem& S, const KWorldDev* __restrict__
         }
         if (__any_sync(0xffffffffu, hit)) {
           cnt.hit64++;
-          return true;
+          glim = min(glim, (int)__reduce_min_sync(0xffffffffu, hit ? (unsigned)step : 32u));
+          if (glim == 0) return 0;
         }
       }
     }
   }
-  return false;
+  return glim;
 }
 
 // Separation of two link boxes along their six face axes (the columns of the
@@ -301,14 +318,13 @@ __device__ __noinline__ bool obb_separated(const float* TA, const float* TB, flo
 
 // Node-pair test for one stack entry; returns 0 (culled), 1 (children in c0,
 // c1) or 2 (leaf job in jA, jB, jM).
-// box-test tolerance of a (link la, target tgt) pair: error bounds of both
-// sides, the optional extra inflation and the summed margins
-__device__ __forceinline__ float pair_tol(const WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
-                                          int la, int tgt)
+// box-test tolerance of a (link row la, target tgt) pair: error bounds of
+// both sides, the optional extra inflation and the summed margins, from the
+// per-row and per-group parts in S.tol64; the factor covers the rounding of
+// the sums (all terms are non-negative)
+__device__ __forceinline__ float pair_tol(const WarpSmem& S, int la, int tgt)
 {
-  const bool self = tgt < 32;
-  return S.delta[la] + (self ? S.delta[tgt] : W->eps_env) + 2.f * W->eps_extra + R.link_margin[la] +
-         (self ? R.link_margin[tgt] : W->group_margin[tgt - 32]);
+  return (S.tol64[la] + S.tol64[tgt]) * (1.f + 16.f * kU);
 }
 
 __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __restrict__ W,
@@ -330,7 +346,7 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
     Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z);
     Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z);
   }
-  const float tol = pair_tol(S, W, R, la, tgt);
+  const float tol = pair_tol(S, la, tgt);
   if (!boxes_overlap(A, Bx, tol)) return 0;
   if (self && obb_separated(S.T[la], S.T[tgt], na.b, nb.b, A.c, Bx.c, tol, fmaxf(S.gerr[la], S.gerr[tgt])))
     return 0;
@@ -355,7 +371,7 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
 
 // Gives the bottom half of this warp's stack (and the item context) to a
 // waiting sibling, if one can be claimed; returns the entries given.
-__device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, int lane, int top, int nl)
+__device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, int lane, int top, int glim)
 {
   int t = -1;
   if (lane == 0) {
@@ -368,11 +384,9 @@ __device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, in
   WarpSmem& D = all[t];
   const int h = top / 2;
   for (int k = lane; k < h; k += 32) D.stack[k] = S.stack[k];
-  for (int i = lane; i < nl * 12; i += 32) D.T[i / 12][i % 12] = S.T[i / 12][i % 12];
-  if (lane < nl) {
-    D.delta[lane] = S.delta[lane];
-    D.gerr[lane] = S.gerr[lane];
-  }
+  for (int i = lane; i < kMaxLinks * 12; i += 32) D.T[i / 12][i % 12] = S.T[i / 12][i % 12];
+  D.delta[lane] = S.delta[lane];
+  D.gerr[lane] = S.gerr[lane];
   if (lane == 0) {
     D.item_qa = S.item_qa;
     D.item_qb = S.item_qb;
@@ -381,9 +395,26 @@ __device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, in
     D.item_id = S.item_id;
     D.item_rid = S.item_rid;
     D.don_top = h;
+    D.don_glim = glim;
   }
   __syncwarp();
-  for (int k = lane; k < top - h; k += 32) S.stack[k] = S.stack[h + k];
+  {
+    // the kept entries move down in two phases (all loads, then all stores):
+    // the ranges overlap, and lanes of a warp are not guaranteed to run the
+    // iterations of an in-place copy in lockstep
+    uint2 keep[kStackCap / 64 + 1];
+#pragma unroll
+    for (int i = 0; i < kStackCap / 64 + 1; ++i) {
+      const int k = lane + 32 * i;
+      if (k < top - h) keep[i] = S.stack[h + k];
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < kStackCap / 64 + 1; ++i) {
+      const int k = lane + 32 * i;
+      if (k < top - h) S.stack[k] = keep[i];
+    }
+  }
   __syncwarp();
   if (lane == 0) {
     __threadfence_block();
@@ -392,28 +423,40 @@ __device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, in
   return h;
 }
 
-// Traverses queries [qbase, qbase+qcount) of robot R for the configuration
-// whose FP32 link transforms are in S.T, or (preset > 0) the preset entries
-// S.stack[0, preset) handed over by a sibling.  Warp-uniform control flow.
+// Traverses queries [qbase, qbase+qcount) of robot R for steps g < glim of a
+// step group (link row g * 2^lgL + link of S.T holds link `link` at step g),
+// or (preset > 0) the preset entries S.stack[0, preset) handed over by a
+// sibling.  All steps share one stack; an entry's step is its link row >> lgL,
+// and a contact at step g drops the entries of steps >= g.  Returns the first
+// step with a contact (glim when none) or TR_OVERFLOW.  Warp-uniform control
+// flow.
 template <bool FP64>
 __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
                                      int qbase, int qcount, int lane, uint2* spill, int spill_cap,
                                      double (*T64)[12], int& fk64, const EngineArgs& A, int job_flush,
-                                     Cnt& cnt, WarpSmem* all, int me, BlockShare& B, int preset)
+                                     Cnt& cnt, WarpSmem* all, int me, BlockShare& B, int preset, int glim, int lgL)
 {
   const unsigned lt = lanemask_lt();
+  const int lmask = (1 << lgL) - 1;
   int top = preset, njobs = 0, spill_top = 0;
-  if (preset > 0) qcount = 0;
+  S.tol64[lane] = S.delta[lane] + W->eps_extra + R.link_margin[lane & lmask];
+  S.tol64[32 + lane] = W->eps_env + W->eps_extra + W->group_margin[lane];
+  __syncwarp();
+  const int nroot = preset > 0 ? 0 : qcount * glim;
 
-  // root pairs of every query, tested in parallel
+  // root pairs of every query and step, tested in parallel; pushed so that
+  // step 0 ends on top (batches from the last, lane 0 highest), and children
+  // below keep that order: the earliest steps are traversed first, later
+  // steps fill the lanes they leave idle, and a contact at step g drops the
+  // work of the steps after it
 #pragma unroll 1
-  for (int qb = 0; qb < qcount; qb += 32) {
+  for (int qb = (nroot - 1) & ~31; qb >= 0; qb -= 32) {
     if (top > kStackCap - 32) {
       const int H = kStackCap / 2;
       if (spill_top + H > spill_cap) return TR_OVERFLOW;
       for (int k = lane; k < H; k += 32) spill[spill_top + k] = S.stack[k];
       __syncwarp();
-      for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];
+      for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];  // disjoint: top <= 2 H
       __syncwarp();
       spill_top += H;
       top -= H;
@@ -422,26 +465,29 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
     const int qi = qb + lane;
     bool push = false;
     uint2 ent = make_uint2(0, 0);
-    if (qi < qcount) {
-      const uint32_t qw = __ldg(W->queries + qbase + qi);
+    if (qi < nroot) {
+      const int g = qi / qcount;
+      const uint32_t qw = __ldg(W->queries + qbase + (qi - g * qcount));
       const int a = qw & 0xff, tgt = (qw >> 8) & 0xff;
       const int ra = R.link_root[a];
       const int rb = tgt < 32 ? R.link_root[tgt] : W->group_root[tgt - 32];
       if (ra >= 0 && rb >= 0) {
-        ent = make_entry(ra, a, tgt, rb);
+        const int row = (g << lgL) | a;
+        const int trow = tgt < 32 ? ((g << lgL) | tgt) : tgt;
+        ent = make_entry(ra, row, trow, rb);
         // box cull of the root pair; survivors are pushed and expanded below
         const KNode na = W->lnodes[ra];
         const KNode nb = (tgt < 32 ? W->lnodes : W->enodes)[rb];
-        const Box32 A = xform_box(S.T[a], na.a, na.b);
+        const Box32 A = xform_box(S.T[row], na.a, na.b);
         Box32 Bx;
-        if (tgt < 32) Bx = xform_box(S.T[tgt], nb.a, nb.b);
+        if (tgt < 32) Bx = xform_box(S.T[trow], nb.a, nb.b);
         else { Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z); Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z); }
-        push = boxes_overlap(A, Bx, pair_tol(S, W, R, a, tgt));
+        push = boxes_overlap(A, Bx, pair_tol(S, row, trow));
         cnt.node_pairs++;
       }
     }
     const unsigned mp = __ballot_sync(0xffffffffu, push);
-    if (push) S.stack[top + __popc(mp & lt)] = ent;
+    if (push) S.stack[top + __popc(mp) - 1 - __popc(mp & lt)] = ent;
     top += __popc(mp);
     __syncwarp();
   }
@@ -456,14 +502,14 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
         spill_top -= n;
         top = n;
       } else if (njobs == 0) {
-        return TR_FREE;
+        return glim;
       }
     }
     if (njobs >= job_flush || (top == 0 && njobs > 0)) {
-      const bool hit = run_jobs<FP64>(S, W, R, njobs, lane, T64, fk64, A, cnt);
+      glim = run_jobs<FP64>(S, W, R, njobs, lane, T64, fk64, A, cnt, glim, lgL);
       __syncwarp();
       njobs = 0;
-      if (hit) return TR_HIT;
+      if (glim == 0) return 0;
       continue;
     }
     if (top > kStackCap - 32) {
@@ -471,7 +517,7 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
       if (spill_top + H > spill_cap) return TR_OVERFLOW;
       for (int k = lane; k < H; k += 32) spill[spill_top + k] = S.stack[k];
       __syncwarp();
-      for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];
+      for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];  // disjoint: top <= 2 H
       __syncwarp();
       spill_top += H;
       top -= H;
@@ -480,12 +526,15 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
     if (A.mode == MODE_EDGES && top >= kDonateMin) {
       int idle = 0;
       if (lane == 0) idle = *((volatile int*)&B.idle);
-      if (__shfl_sync(0xffffffffu, idle, 0) > 0) top -= share_stack(all, me, B, lane, top, R.nlinks);
+      if (__shfl_sync(0xffffffffu, idle, 0) > 0) top -= share_stack(all, me, B, lane, top, glim);
     }
     const int n = min(top, 32);
-    const bool have = lane < n;
+    bool have = lane < n;
     uint2 e = make_uint2(0, 0);
-    if (have) e = S.stack[top - 1 - lane];
+    if (have) {
+      e = S.stack[top - 1 - lane];
+      have = (int)(((e.y >> 20) & 31u) >> lgL) < glim;  // entries of steps past a contact are dropped
+    }
     __syncwarp();
     top -= n;
     int outcome = 0;  // 1: two children, 2: leaf job
@@ -496,7 +545,7 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
     const unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
     const unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
     if (outcome == 1) {
-      const int r = top + 2 * __popc(m1 & lt);
+      const int r = top + 2 * (__popc(m1) - 1 - __popc(m1 & lt));
       S.stack[r] = c1;
       S.stack[r + 1] = c0;
     } else if (outcome == 2) {
@@ -582,22 +631,26 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
       } else if (rid < 0) {
         rid = __ldg(A.robot_ids + b);
       }
-      // FK of up to G consecutive steps at once (G = 32 / L groups of L lanes,
-      // L the link count rounded up to 8, 16 or 32): rows [g L, g L + nl) of
-      // S.T hold step fk_base + g; a later step's rows are moved to 0..nl-1
-      int fk_base = -1, fk_cnt = 0;
+      // Steps in groups of up to G = 32 / L (edge items of the main pass;
+      // L = the link count rounded up to 8, 16 or 32): lanes g L + link
+      // compute FK of link `link` at step kb + g, link row g L + link of
+      // S.T holds it, and one traversal per query set decides the group's
+      // steps together.  Configurations and the FP64 pass use groups of one.
+      const KRobotDev& R = W->robots[rid];
+      const int nl = R.nlinks;
+      const int lgL = nl <= 8 ? 3 : (nl <= 16 ? 4 : 5);
+      const int L = 1 << lgL;
+      const int Gmax = (FP64 || A.mode != MODE_EDGES) ? 1 : 32 / L;
 #pragma unroll 1
-      for (int k = k0; k <= k1; ++k) {
+      for (int kb = k0; kb <= k1; kb += Gmax) {
+        int glim = min(Gmax, k1 - kb + 1);
         if (A.mode == MODE_EDGES) {
           int fh = 0;
           if (lane == 0) fh = *((volatile int*)(A.first_hit + e));
           fh = __shfl_sync(0xffffffffu, fh, 0);
-          if (fh < k) break;  // this or an earlier step of the edge already hit
+          if (fh <= kb) break;  // this or an earlier step of the edge already hit
+          glim = min(glim, fh - kb);
         }
-        const KRobotDev& R = W->robots[rid];
-        const int nl = R.nlinks;
-        // joint values in FP32 with an error bound e_q against the canonical
-        // FP64 values (exact for configurations; FMA interpolation for edges)
         if (lane == 0) {
           if (A.mode == MODE_EDGES) {
             S.item_qa = A.qa + (size_t)e * nl;
@@ -606,115 +659,103 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
             S.item_qa = A.q + (size_t)b * A.q_stride;
             S.item_qb = nullptr;
           }
-          S.item_k = k;
+          S.item_k = kb;
           S.item_n = n;
           S.item_id = A.mode == MODE_EDGES ? e : b;
           S.item_rid = rid;
         }
+        // joint values in FP32 with an error bound e_q against the canonical
+        // FP64 values (exact for configurations; FMA interpolation for edges)
+        const int g = lane >> lgL, link = lane & (L - 1);
+        const bool valid = g < glim && link < nl;
         float q = 0.f, e_q = 0.f;
-        if (lane < nl) {
+        if (valid) {
           if (A.mode == MODE_EDGES) {
-            const float a = __ldg(A.qa + (size_t)e * nl + lane), bq = __ldg(A.qb + (size_t)e * nl + lane);
+            const float a = __ldg(A.qa + (size_t)e * nl + link), bq = __ldg(A.qb + (size_t)e * nl + link);
             const float d = bq - a;
-            q = fmaf((float)k / (float)n, d, a);
+            q = fmaf((float)(kb + g) / (float)n, d, a);
             e_q = kU * (fabsf(d) + fabsf(q) + fabsf(a)) * 1.01f + 1e-30f;
           } else {
-            q = __ldg(A.q + (size_t)b * A.q_stride + lane);
+            q = __ldg(A.q + (size_t)b * A.q_stride + link);
           }
         }
         __syncwarp();
-        if (!FP64) items++;
-        const bool nonfinite = __any_sync(0xffffffffu, lane < nl && !(fabsf(q) < 1.0e6f));
-        if (nonfinite) {
+        if (!FP64) items += (unsigned long long)glim;
+        if (__any_sync(0xffffffffu, valid && !(fabsf(q) < 1.0e6f))) {
           if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
           continue;
         }
         if (A.mode != MODE_CONFIGS) {
           // joint limits: certain in FP32 away from the bounds, canonical FP64
-          // comparison (RobotCSpace.cpp:610-630) within rounding of them
+          // comparison (RobotCSpace.cpp:610-630) within rounding of them; the
+          // first violating step ends the group there
           bool unsure = false;
-          if (lane < nl) {
-            const float lo = R.qmin[lane], hi = R.qmax[lane];
+          if (valid) {
+            const float lo = R.qmin[link], hi = R.qmax[link];
             const float tolq = e_q + 4.f * kU * (fabsf(q) + fmaxf(fabsf(lo), fabsf(hi))) + 1e-30f;
             unsure = !((q - lo) > tolq && (hi - q) > tolq);
           }
           bool viol = false;
           if (unsure) {
-            const double q64 = item_q64(S, lane);
-            viol = q64 < R.qmin64[lane] || q64 > R.qmax64[lane];
+            const double q64 = A.mode == MODE_EDGES
+                                   ? kx_interp((double)S.item_qa[link], (double)S.item_qb[link], kb + g, n)
+                                   : (double)S.item_qa[link];
+            viol = q64 < R.qmin64[link] || q64 > R.qmax64[link];
           }
-          if (__any_sync(0xffffffffu, viol)) {
+          const int gv = (int)__reduce_min_sync(0xffffffffu, viol ? (unsigned)g : 32u);
+          if (gv < glim) {
             if (lane == 0) {
-              if (A.mode == MODE_EDGES) atomicMin(A.first_hit + e, k);
+              if (A.mode == MODE_EDGES) atomicMin(A.first_hit + e, kb + gv);
               else A.feasible[b] = 0;
             }
-            continue;
+            glim = gv;
           }
+          if (glim == 0) break;
         }
-        const int L = nl <= 8 ? 8 : (nl <= 16 ? 16 : 32);
-        if (k < fk_base || k >= fk_base + fk_cnt) {
-          fk_base = k;
-          fk_cnt = A.mode == MODE_EDGES ? min(32 / L, k1 - k + 1) : 1;
-          const int g = lane / L, link = lane & (L - 1);
-          const bool valid = g < fk_cnt && link < nl;
-          float qg = 0.f, eg = 0.f;
-          if (valid) {
-            if (A.mode == MODE_EDGES) {
-              const float a = __ldg(A.qa + (size_t)e * nl + link), bq = __ldg(A.qb + (size_t)e * nl + link);
-              const float d = bq - a;
-              qg = fmaf((float)(k + g) / (float)n, d, a);
-              eg = kU * (fabsf(d) + fabsf(qg) + fabsf(a)) * 1.01f + 1e-30f;
-            } else {
-              qg = q;
-              eg = e_q;
-            }
-          }
-          float P[12], delta;
-          warp_fk32_group(R, lane, L, valid, qg, eg, P, &delta);
-          if (valid) {
+        float P[12], delta;
+        warp_fk32_group(R, lane, L, valid, q, e_q, P, &delta);
+        if (valid) {
 #pragma unroll
-            for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
-            S.delta[lane] = delta;
-            S.gerr[lane] = rot_gram_err32(P);
-          }
-        } else if (lane < nl) {
-          const int row = (k - fk_base) * L + lane;
-#pragma unroll
-          for (int i = 0; i < 12; ++i) S.T[lane][i] = S.T[row][i];
-          S.delta[lane] = S.delta[row];
-          S.gerr[lane] = S.gerr[row];
+          for (int i = 0; i < 12; ++i) S.T[lane][i] = P[i];
+          S.delta[lane] = delta;
+          S.gerr[lane] = rot_gram_err32(P);
         }
         __syncwarp();
-        int env_res = TR_FREE, self_res = TR_FREE;
+        int env_lim = glim, self_lim = glim;
         int fk64 = 0;
         const bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
         const bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
         if (want_env && R.nqueries_env > 0)
-          env_res = traverse<FP64>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, A,
-                                   job_flush, cnt, all, warp, B, 0);
-        const bool stop = A.mode != MODE_CONFIGS && env_res != TR_FREE;
-        if (!stop && want_self && R.nqueries_self > 0)
-          self_res = traverse<FP64>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill,
-                                    spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0);
-        if (env_res == TR_OVERFLOW || self_res == TR_OVERFLOW) {
+          env_lim = traverse<FP64>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, A,
+                                   job_flush, cnt, all, warp, B, 0, glim, lgL);
+        // edges and feasibility need the self pairs only before the first
+        // environment contact; configurations report both
+        const int glim2 = A.mode == MODE_CONFIGS ? glim : env_lim;
+        if (env_lim >= 0) self_lim = glim2;
+        if (glim2 > 0 && want_self && R.nqueries_self > 0)
+          self_lim = traverse<FP64>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill,
+                                    spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0, glim2, lgL);
+        if (env_lim < 0 || self_lim < 0) {
           if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
           continue;
         }
+        const int ghit = min(env_lim, self_lim);
         if (lane == 0) {
           // verdicts only ever turn into contacts (the outputs start as
           // "free"), so shared traversals and the FP64 pass can add theirs
           // in any order
           if (A.mode == MODE_CONFIGS) {
-            if (A.env_hit && env_res == TR_HIT) A.env_hit[b] = 1;
-            if (A.self_hit && self_res == TR_HIT) A.self_hit[b] = 1;
+            if (A.env_hit && env_lim < glim) A.env_hit[b] = 1;
+            if (A.self_hit && self_lim < glim) A.self_hit[b] = 1;
           } else if (A.mode == MODE_FEASIBLE) {
-            if (env_res == TR_HIT || self_res == TR_HIT) A.feasible[b] = 0;
-          } else if (env_res == TR_HIT || self_res == TR_HIT) {
-            atomicMin(A.first_hit + e, k);
+            if (ghit < glim) A.feasible[b] = 0;
+          } else if (ghit < glim) {
+            atomicMin(A.first_hit + e, kb + ghit);
           }
         }
         __syncwarp();
-      }  // steps of the item
+        if (A.mode == MODE_EDGES && ghit < glim) break;
+      }  // step groups of the item
     }
   }
 
@@ -734,19 +775,25 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
       if (lane == 0) atomicSub(&B.idle, 1);
       __syncwarp();
       const KRobotDev& R = W->robots[S.item_rid];
-      int fh = INT_MAX;
-      if (A.mode == MODE_EDGES && lane == 0) fh = *((volatile int*)(A.first_hit + S.item_id));
-      fh = __shfl_sync(0xffffffffu, fh, 0);
-      if (fh > S.item_k) {  // not decided yet
+      const int nl = R.nlinks;
+      const int lgL = nl <= 8 ? 3 : (nl <= 16 ? 4 : 5);
+      int glim = S.don_glim;
+      if (A.mode == MODE_EDGES) {
+        int fh = 0;
+        if (lane == 0) fh = *((volatile int*)(A.first_hit + S.item_id));
+        fh = __shfl_sync(0xffffffffu, fh, 0);
+        glim = fh <= S.item_k ? 0 : min(glim, fh - S.item_k);  // steps not decided yet
+      }
+      if (glim > 0) {
         int fk64 = 0;
         const bool self = ((S.stack[0].y >> 25) & 63u) < 32u;
         const int res = traverse<FP64>(S, W, R, 0, 0, lane, spill, spill_cap, T64, fk64, A, job_flush, cnt, all,
-                                       warp, B, S.don_top);
+                                       warp, B, S.don_top, glim, lgL);
         if (lane == 0) {
           if (res == TR_OVERFLOW) {
             set_status(W->status, KGPU_ERR_OVERFLOW);
-          } else if (res == TR_HIT) {
-            if (A.mode == MODE_EDGES) atomicMin(A.first_hit + S.item_id, S.item_k);
+          } else if (res < glim) {
+            if (A.mode == MODE_EDGES) atomicMin(A.first_hit + S.item_id, S.item_k + res);
             else if (A.mode == MODE_FEASIBLE) A.feasible[S.item_id] = 0;
             else if (self && A.self_hit) A.self_hit[S.item_id] = 1;
             else if (!self && A.env_hit) A.env_hit[S.item_id] = 1;
@@ -859,10 +906,10 @@ __global__ void __launch_bounds__(kWarps * 32, 2) k_self_pairs(const KWorldDev* 
       if (lane == 0) known = *((volatile unsigned int*)(pair_mask + a));
       if ((__shfl_sync(0xffffffffu, known, 0) >> tgt) & 1u) continue;
       const int res = traverse<true>(S, W, R, qidx, 1, lane, spill, spill_cap, T64, fk64, A, job_flush, cnt, all,
-                                     warp, B, 0);
+                                     warp, B, 0, 1, 5);
       if (lane == 0) {
         if (res == TR_OVERFLOW) set_status(W->status, KGPU_ERR_OVERFLOW);
-        else if (res == TR_HIT) atomicOr(pair_mask + a, 1u << tgt);
+        else if (res == 0) atomicOr(pair_mask + a, 1u << tgt);
       }
       __syncwarp();
     }
