@@ -55,12 +55,12 @@ enum Mode { MODE_CONFIGS = 0, MODE_FEASIBLE = 1, MODE_EDGES = 2 };
 
 // per-warp shared memory (~6.4 KB, so that up to 32 warps fit on an SM)
 struct __align__(16) WarpSmem {
+  float T[kMaxLinks][12];     // first: every row starts on a 16-byte boundary
   uint2 stack[kStackCap];
   uint32_t jobA[kJobCap];
   uint32_t jobB[kJobCap];
   uint32_t jobM[kJobCap];
   uint32_t jobOff[kJobCap + 1];
-  float T[kMaxLinks][12];
   float delta[kMaxLinks];     // per-link bound on |FP32 - exact| world coordinates
   float gerr[kMaxLinks];      // per-link max |R^T R - I| of the FP32 rotation (+ rounding)
   float tol64[64];            // box-test tolerance parts: rows 0-31 per link row, 32-63 per group
@@ -73,6 +73,7 @@ struct __align__(16) WarpSmem {
   int don_top;                // stack entries handed over by a sibling warp
   int don_glim;               // steps of the handed-over group still to decide
 };
+static_assert(sizeof(float) * 12 % 16 == 0, "link rows of WarpSmem::T stay 16-byte aligned");
 
 // Work sharing inside a block once the queue is drained (edge batches, whose
 // long items would otherwise end the launch on one warp; a contact found by
@@ -86,7 +87,7 @@ struct BlockShare {
   int idle;
   int flag[kWarps];
 };
-constexpr int kDonateMin = 64;     // stack entries a warp needs before it shares
+constexpr int kDonateMin = 32;     // stack entries a warp needs before it shares
 constexpr int kShareSpins = 1 << 20;  // bound on a waiting warp's polls (~0.3 s)
 
 // canonical FP64 joint values of the current item (lane < nl), as the oracle
@@ -149,6 +150,16 @@ struct EngineArgs {
 struct Cnt {
   unsigned long long node_pairs = 0, tri_pairs = 0, band = 0, spills = 0, cert = 0, hit64 = 0;
 };
+
+// a link row of S.T (16-byte aligned) into registers with three 16-byte loads
+__device__ __forceinline__ void load_row(const float* T, float* o)
+{
+  const float4* p = reinterpret_cast<const float4*>(T);
+  const float4 a = p[0], b = p[1], c = p[2];
+  o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = a.w;
+  o[4] = b.x; o[5] = b.y; o[6] = b.z; o[7] = b.w;
+  o[8] = c.x; o[9] = c.y; o[10] = c.z; o[11] = c.w;
+}
 
 // A traversal returns the number of leading steps of its group found free
 // (the first step with a contact; the group size when none), or TR_OVERFLOW.
@@ -225,9 +236,10 @@ __device__ __noinline__ int run_jobs(WarpSmem& S, const KWorldDev* __restrict__ 
         tA = (int)(S.jobA[j] & 0x0fffffffu) + (int)(r / cb);
         tB = (int)S.jobB[j] + (int)(r % cb);
         float3 P[3], Q[3];
-        const float* TA = S.T[la];
         const bool self = tgt < 32;
-        const float* TB = S.T[self ? tgt : 0];
+        float TA[12], TB[12];
+        load_row(S.T[la], TA);
+        load_row(S.T[self ? tgt : la], TB);
         const float4* qsrc = self ? ltri : etri;
 #pragma unroll
         for (int v = 0; v < 3; ++v) {
@@ -338,10 +350,14 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
   const bool self = tgt < 32;
   const KNode na = W->lnodes[nodeA];
   const KNode nb = (self ? W->lnodes : W->enodes)[nodeB];
-  const Box32 A = xform_box(S.T[la], na.a, na.b);
+  float TA[12];
+  load_row(S.T[la], TA);
+  const Box32 A = xform_box(TA, na.a, na.b);
   Box32 Bx;
   if (self) {
-    Bx = xform_box(S.T[tgt], nb.a, nb.b);
+    float TB[12];
+    load_row(S.T[tgt], TB);
+    Bx = xform_box(TB, nb.a, nb.b);
   } else {
     Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z);
     Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z);
