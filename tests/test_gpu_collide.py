@@ -171,6 +171,28 @@ def test_cfg1_edges_host_and_graph(cfg1):
     plan.close()
 
 
+def test_edges_full_batch_repeatable(built):
+    """The full 16,384-edge batch (deep traversals handed between warps at
+    the end of every launch) gives the oracle's first hits in each of 42
+    launches (14 for each of three edge chunk sizes): hand-over races show
+    up as rare, launch-dependent first hits one step late."""
+    import torch
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robot, env, (qa, qb, ns) = sc.scene_cfg1()
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    fh_o, _ = o.check_edges(qa, qb, ns, nthreads=NT)
+    a, b, n = (torch.as_tensor(x).cuda() for x in (qa, qb, ns))
+    for chunk in (8, 16, 32):
+        w.set_option("edge_chunk", chunk)
+        for _ in range(14):
+            fh = w.check_edges(a, b, n).cpu().numpy()
+            bad = np.flatnonzero(fh != fh_o)
+            assert bad.size == 0, (chunk, bad[:5], fh[bad[:5]], fh_o[bad[:5]])
+    w.close()
+
+
 def test_edges_single_step_and_limits(cfg1):
     """n = 1 edges (two configurations) and an edge leaving the limits."""
     robot, env, (qa, qb, ns), w, o = cfg1
