@@ -49,8 +49,8 @@ struct HostBvh {
 
 // Builds a BVH over triangles `ids` (tri: 9 doubles per triangle id).  When
 // tri_obj is given, the top levels split whole objects so that every object
-// owns one subtree.  Median split on the widest centroid axis, leaves of at
-// most kLeafSize triangles, children adjacent.
+// owns one subtree.  Binned surface-area splits of the triangles, leaves of
+// at most kLeafSize triangles, children adjacent.
 void build_bvh(const std::vector<double>& tri, const std::vector<int>& ids,
                const std::vector<int>* tri_obj, HostBvh& out);
 
