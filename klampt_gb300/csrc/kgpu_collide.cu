@@ -741,16 +741,24 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
         int fk64 = 0;
         const bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
         const bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
-        if (want_env && R.nqueries_env > 0)
-          env_lim = traverse<FP64>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, A,
-                                   job_flush, cnt, all, warp, B, 0, glim, lgL);
-        // edges and feasibility need the self pairs only before the first
-        // environment contact; configurations report both
-        const int glim2 = A.mode == MODE_CONFIGS ? glim : env_lim;
-        if (env_lim >= 0) self_lim = glim2;
-        if (glim2 > 0 && want_self && R.nqueries_self > 0)
-          self_lim = traverse<FP64>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill,
-                                    spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0, glim2, lgL);
+        if (A.mode != MODE_CONFIGS) {
+          // edges and feasibility: any contact decides a step, so the
+          // environment and self queries share one traversal (one stack
+          // drain per group instead of two)
+          const int nq = R.nqueries_env + R.nqueries_self;
+          if (nq > 0)
+            env_lim = traverse<FP64>(S, W, R, R.query_off, nq, lane, spill, spill_cap, T64, fk64, A, job_flush, cnt,
+                                     all, warp, B, 0, glim, lgL);
+          self_lim = env_lim >= 0 ? env_lim : glim;
+        } else {
+          // configurations report the environment and self verdicts apart
+          if (want_env && R.nqueries_env > 0)
+            env_lim = traverse<FP64>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, A,
+                                     job_flush, cnt, all, warp, B, 0, glim, lgL);
+          if (want_self && R.nqueries_self > 0)
+            self_lim = traverse<FP64>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill,
+                                      spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0, glim, lgL);
+        }
         if (env_lim < 0 || self_lim < 0) {
           if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
           continue;
