@@ -171,8 +171,8 @@ kgpu_status kgpu_world_enable_self_pair(kgpu_world world, int32_t robot, int32_t
  * count rounded up to 8, 16 or 32, earliest step first), "fp64_inline" (1: triangle pairs the FP32 tests
  * leave undecided get the FP64 test inside the traversal kernel; 0: they are
  * listed and decided by a second kernel, keeping FP64 code out of the
- * traversal kernel; -1, the default: 0 for edge batches, 1 for configuration
- * batches), read-only
+ * traversal kernel and letting configurations of one robot be checked in
+ * groups; -1, the default: 0), read-only
  * "eps_env", "warps_per_block", "num_sms".  The autotuner
  * (klampt_gb300/autotune.py) sets blocks_per_sm, grab, job_flush and
  * edge_chunk or fp64_inline.

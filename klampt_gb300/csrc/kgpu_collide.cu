@@ -71,7 +71,7 @@ struct __align__(16) WarpSmem {
   int item_id;                // configuration index b, or edge index e
   int item_rid;               // robot of the item
   int don_top;                // stack entries handed over by a sibling warp
-  int don_glim;               // steps of the handed-over group still to decide
+  unsigned don_live;          // steps of the handed-over group still to decide
 };
 static_assert(sizeof(float) * 12 % 16 == 0, "link rows of WarpSmem::T stay 16-byte aligned");
 
@@ -161,9 +161,8 @@ __device__ __forceinline__ void load_row(const float* T, float* o)
   o[8] = c.x; o[9] = c.y; o[10] = c.z; o[11] = c.w;
 }
 
-// A traversal returns the number of leading steps of its group found free
-// (the first step with a contact; the group size when none), or TR_OVERFLOW.
-enum { TR_OVERFLOW = -1 };
+// traversal result flag: the spill area ran out (step bits are 0..3)
+constexpr unsigned kTrOverflow = 1u << 31;
 
 __device__ __forceinline__ uint2 make_entry(int nodeA, int la, int tgt, int nodeB)
 {
@@ -171,23 +170,26 @@ __device__ __forceinline__ uint2 make_entry(int nodeA, int la, int tgt, int node
 }
 
 // Tests the triangle-pair jobs of the warp, one triangle pair per lane.
-// Triangle-pair jobs of a step group: steps g < glim are live (a job's step
-// is its link row >> lgL).  Per pair: FP32 separating-axis filter
-// (separated beyond the band: done), FP32 intersection certificate (crossing
-// beyond the band: contact), otherwise the pair is undecided in FP32.  The
-// main pass (FP64 = false) appends such a pair to A.pend and goes on (k_band
-// decides it afterwards); the fallback pass (FP64 = true, groups of one step)
-// decides it here with the FP64 test on transforms computed once per
-// configuration (fk64 tracks whether T64 is valid).  Keeping the FP64 code
-// out of the main pass's kernel keeps that kernel's hot loop in the
-// instruction cache.  A contact at step g lowers glim to g: later steps of
-// the group need no decision, earlier ones still do.  Returns the new glim.
-template <bool FP64>
-__device__ __noinline__ int run_jobs(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
-                                     int njobs, int lane, double (*T64)[12], int& fk64, const EngineArgs& A,
-                                     Cnt& cnt, int glim, int lgL)
+// Triangle-pair jobs of a step group: bit g of `live` marks step (or
+// configuration) g still undecided; a job's step is its link row >> lgL.
+// Per pair: FP32 separating-axis filter (separated beyond the band: done),
+// FP32 intersection certificate (crossing beyond the band: contact),
+// otherwise the pair is undecided in FP32.  The main pass (FP64 = false)
+// appends such a pair to A.pend and goes on (k_band decides it afterwards);
+// the fallback pass (FP64 = true, groups of one) decides it here with the
+// FP64 test on transforms computed once per configuration (fk64 tracks
+// whether T64 is valid).  Keeping the FP64 code out of the main pass's
+// kernel keeps that kernel's hot loop in the instruction cache.  A contact
+// at step g clears bit g of `live` (edge steps: bits g and above, later
+// steps need no decision).  Returns the steps found in contact.
+template <bool FP64, bool EDGES>
+__device__ __noinline__ unsigned run_jobs(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                          int njobs, int lane, double (*T64)[12], int& fk64, const EngineArgs& A,
+                                          Cnt& cnt, unsigned& live, int lgL)
 {
   const int lmask = (1 << lgL) - 1;
+  constexpr bool seq = EDGES;
+  unsigned hits = 0;
   // exclusive prefix over job sizes
   uint32_t carry = 0;
 #pragma unroll 1
@@ -216,8 +218,8 @@ __device__ __noinline__ int run_jobs(WarpSmem& S, const KWorldDev* __restrict__ 
 #pragma unroll 1
   for (uint32_t base = 0; base < total; base += 32) {
     uint32_t p = base + lane;
-    bool band = false, certain = false;
-    int la = 0, tgt = 0, tA = 0, tB = 0, step = 32;
+    bool band = false, certain = false, mine = false;
+    int la = 0, tgt = 0, tA = 0, tB = 0, step = 0;
     if (p < total) {
       // job holding p: largest j with jobOff[j] <= p
       int lo = 0, hi = njobs - 1;
@@ -230,7 +232,8 @@ __device__ __noinline__ int run_jobs(WarpSmem& S, const KWorldDev* __restrict__ 
       la = jm & 0xff;
       tgt = (jm >> 8) & 0xff;
       step = la >> lgL;
-      if (step < glim) {
+      mine = (live >> step) & 1u;
+      if (mine) {
         const uint32_t r = p - S.jobOff[j];
         const uint32_t cb = ((jm >> 16) & 3u) + 1;
         tA = (int)(S.jobA[j] & 0x0fffffffu) + (int)(r / cb);
@@ -259,10 +262,12 @@ __device__ __noinline__ int run_jobs(WarpSmem& S, const KWorldDev* __restrict__ 
     }
     if (__any_sync(0xffffffffu, certain)) {
       cnt.cert++;
-      glim = min(glim, (int)__reduce_min_sync(0xffffffffu, certain ? (unsigned)step : 32u));
-      if (glim == 0) return 0;
+      const unsigned hm = __reduce_or_sync(0xffffffffu, certain ? 1u << step : 0u);
+      hits |= hm;
+      live &= seq ? (1u << (__ffs(hm) - 1)) - 1u : ~hm;
+      if (live == 0) return hits;
     }
-    const bool need64 = band && !certain && step < glim;
+    const bool need64 = band && !certain && ((live >> step) & 1u);
     if (__any_sync(0xffffffffu, need64)) {
       if (!FP64) {
         const unsigned m = __ballot_sync(0xffffffffu, need64);
@@ -270,11 +275,12 @@ __device__ __noinline__ int run_jobs(WarpSmem& S, const KWorldDev* __restrict__ 
         if (lane == 0) at = atomicAdd(A.pend_count, (unsigned)__popc(m));
         at = __shfl_sync(0xffffffffu, at, 0) + __popc(m & lanemask_lt());
         if (need64 && at < (unsigned)A.pend_cap) {
-          // the record names the step and link indices (not link rows)
+          // the record names the edge step (or the configuration) and link
+          // indices, not link rows
           const unsigned tl = tgt < 32 ? (unsigned)(tgt & lmask) : (unsigned)tgt;
-          A.pend[at] = make_uint4((unsigned)S.item_id,
-                                  (unsigned)(S.item_k + step) | ((unsigned)(la & lmask) << 16) | (tl << 21),
-                                  (unsigned)tA, (unsigned)tB);
+          const unsigned item = seq ? (unsigned)S.item_id : (unsigned)(S.item_id + step);
+          const unsigned k = seq ? (unsigned)(S.item_k + step) : 0u;
+          A.pend[at] = make_uint4(item, k | ((unsigned)(la & lmask) << 16) | (tl << 21), (unsigned)tA, (unsigned)tB);
         }
       } else {
         ensure_fk64(S, R, T64, lane, fk64);
@@ -285,13 +291,15 @@ __device__ __noinline__ int run_jobs(WarpSmem& S, const KWorldDev* __restrict__ 
         }
         if (__any_sync(0xffffffffu, hit)) {
           cnt.hit64++;
-          glim = min(glim, (int)__reduce_min_sync(0xffffffffu, hit ? (unsigned)step : 32u));
-          if (glim == 0) return 0;
+          const unsigned hm = __reduce_or_sync(0xffffffffu, hit ? 1u << step : 0u);
+          hits |= hm;
+          live &= seq ? (1u << (__ffs(hm) - 1)) - 1u : ~hm;
+          if (live == 0) return hits;
         }
       }
     }
   }
-  return glim;
+  return hits;
 }
 
 // Separation of two link boxes along their six face axes (the columns of the
@@ -387,7 +395,7 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
 
 // Gives the bottom half of this warp's stack (and the item context) to a
 // waiting sibling, if one can be claimed; returns the entries given.
-__device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, int lane, int top, int glim)
+__device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, int lane, int top, unsigned live)
 {
   int t = -1;
   if (lane == 0) {
@@ -411,7 +419,7 @@ __device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, in
     D.item_id = S.item_id;
     D.item_rid = S.item_rid;
     D.don_top = h;
-    D.don_glim = glim;
+    D.don_live = live;
   }
   __syncwarp();
   {
@@ -439,26 +447,30 @@ __device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, in
   return h;
 }
 
-// Traverses queries [qbase, qbase+qcount) of robot R for steps g < glim of a
-// step group (link row g * 2^lgL + link of S.T holds link `link` at step g),
-// or (preset > 0) the preset entries S.stack[0, preset) handed over by a
-// sibling.  All steps share one stack; an entry's step is its link row >> lgL,
-// and a contact at step g drops the entries of steps >= g.  Returns the first
-// step with a contact (glim when none) or TR_OVERFLOW.  Warp-uniform control
-// flow.
-template <bool FP64>
-__device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
-                                     int qbase, int qcount, int lane, uint2* spill, int spill_cap,
-                                     double (*T64)[12], int& fk64, const EngineArgs& A, int job_flush,
-                                     Cnt& cnt, WarpSmem* all, int me, BlockShare& B, int preset, int glim, int lgL)
+// Traverses queries [qbase, qbase+qcount) of robot R for the steps (or
+// configurations) g of a group whose bit is set in `live` (link row
+// g * 2^lgL + link of S.T holds link `link` at step g), or (preset > 0) the
+// preset entries S.stack[0, preset) handed over by a sibling.  All steps
+// share one stack; an entry's step is its link row >> lgL, and the entries
+// of a step found in contact are dropped (of an edge step: also those of the
+// later steps).  Returns the steps found in contact (bits 0..3: a group has
+// at most 32 / 8 steps), plus kTrOverflow when the spill area ran out.
+// Warp-uniform control flow.
+template <bool FP64, bool EDGES>
+__device__ __noinline__ unsigned traverse(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                          int qbase, int qcount, int lane, uint2* spill, int spill_cap,
+                                          double (*T64)[12], int& fk64, const EngineArgs& A, int job_flush,
+                                          Cnt& cnt, WarpSmem* all, int me, BlockShare& B, int preset, unsigned live,
+                                          int lgL)
 {
   const unsigned lt = lanemask_lt();
   const int lmask = (1 << lgL) - 1;
   int top = preset, njobs = 0, spill_top = 0;
+  unsigned hits = 0;
   S.tol64[lane] = S.delta[lane] + W->eps_extra + R.link_margin[lane & lmask];
   S.tol64[32 + lane] = W->eps_env + W->eps_extra + W->group_margin[lane];
   __syncwarp();
-  const int nroot = preset > 0 ? 0 : qcount * glim;
+  const int nroot = preset > 0 || live == 0 ? 0 : qcount * (32 - __clz(live));
 
   // root pairs of every query and step, tested in parallel; pushed so that
   // step 0 ends on top (batches from the last, lane 0 highest), and children
@@ -469,7 +481,7 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
   for (int qb = (nroot - 1) & ~31; qb >= 0; qb -= 32) {
     if (top > kStackCap - 32) {
       const int H = kStackCap / 2;
-      if (spill_top + H > spill_cap) return TR_OVERFLOW;
+      if (spill_top + H > spill_cap) return hits | kTrOverflow;
       for (int k = lane; k < H; k += 32) spill[spill_top + k] = S.stack[k];
       __syncwarp();
       for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];  // disjoint: top <= 2 H
@@ -483,23 +495,25 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
     uint2 ent = make_uint2(0, 0);
     if (qi < nroot) {
       const int g = qi / qcount;
-      const uint32_t qw = __ldg(W->queries + qbase + (qi - g * qcount));
-      const int a = qw & 0xff, tgt = (qw >> 8) & 0xff;
-      const int ra = R.link_root[a];
-      const int rb = tgt < 32 ? R.link_root[tgt] : W->group_root[tgt - 32];
-      if (ra >= 0 && rb >= 0) {
-        const int row = (g << lgL) | a;
-        const int trow = tgt < 32 ? ((g << lgL) | tgt) : tgt;
-        ent = make_entry(ra, row, trow, rb);
-        // box cull of the root pair; survivors are pushed and expanded below
-        const KNode na = W->lnodes[ra];
-        const KNode nb = (tgt < 32 ? W->lnodes : W->enodes)[rb];
-        const Box32 A = xform_box(S.T[row], na.a, na.b);
-        Box32 Bx;
-        if (tgt < 32) Bx = xform_box(S.T[trow], nb.a, nb.b);
-        else { Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z); Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z); }
-        push = boxes_overlap(A, Bx, pair_tol(S, row, trow));
-        cnt.node_pairs++;
+      if ((live >> g) & 1u) {
+        const uint32_t qw = __ldg(W->queries + qbase + (qi - g * qcount));
+        const int a = qw & 0xff, tgt = (qw >> 8) & 0xff;
+        const int ra = R.link_root[a];
+        const int rb = tgt < 32 ? R.link_root[tgt] : W->group_root[tgt - 32];
+        if (ra >= 0 && rb >= 0) {
+          const int row = (g << lgL) | a;
+          const int trow = tgt < 32 ? ((g << lgL) | tgt) : tgt;
+          ent = make_entry(ra, row, trow, rb);
+          // box cull of the root pair; survivors are pushed and expanded below
+          const KNode na = W->lnodes[ra];
+          const KNode nb = (tgt < 32 ? W->lnodes : W->enodes)[rb];
+          const Box32 A = xform_box(S.T[row], na.a, na.b);
+          Box32 Bx;
+          if (tgt < 32) Bx = xform_box(S.T[trow], nb.a, nb.b);
+          else { Bx.c = make_float3(nb.a.x, nb.a.y, nb.a.z); Bx.h = make_float3(nb.b.x, nb.b.y, nb.b.z); }
+          push = boxes_overlap(A, Bx, pair_tol(S, row, trow));
+          cnt.node_pairs++;
+        }
       }
     }
     const unsigned mp = __ballot_sync(0xffffffffu, push);
@@ -518,19 +532,19 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
         spill_top -= n;
         top = n;
       } else if (njobs == 0) {
-        return glim;
+        return hits;
       }
     }
     if (njobs >= job_flush || (top == 0 && njobs > 0)) {
-      glim = run_jobs<FP64>(S, W, R, njobs, lane, T64, fk64, A, cnt, glim, lgL);
+      hits |= run_jobs<FP64, EDGES>(S, W, R, njobs, lane, T64, fk64, A, cnt, live, lgL);
       __syncwarp();
       njobs = 0;
-      if (glim == 0) return 0;
+      if (live == 0) return hits;
       continue;
     }
     if (top > kStackCap - 32) {
       const int H = kStackCap / 2;
-      if (spill_top + H > spill_cap) return TR_OVERFLOW;
+      if (spill_top + H > spill_cap) return hits | kTrOverflow;
       for (int k = lane; k < H; k += 32) spill[spill_top + k] = S.stack[k];
       __syncwarp();
       for (int k = lane; k < top - H; k += 32) S.stack[k] = S.stack[H + k];  // disjoint: top <= 2 H
@@ -539,17 +553,17 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
       top -= H;
       cnt.spills++;
     }
-    if (A.mode == MODE_EDGES && top >= kDonateMin) {
+    if (EDGES && top >= kDonateMin) {
       int idle = 0;
       if (lane == 0) idle = *((volatile int*)&B.idle);
-      if (__shfl_sync(0xffffffffu, idle, 0) > 0) top -= share_stack(all, me, B, lane, top, glim);
+      if (__shfl_sync(0xffffffffu, idle, 0) > 0) top -= share_stack(all, me, B, lane, top, live);
     }
     const int n = min(top, 32);
     bool have = lane < n;
     uint2 e = make_uint2(0, 0);
     if (have) {
       e = S.stack[top - 1 - lane];
-      have = (int)(((e.y >> 20) & 31u) >> lgL) < glim;  // entries of steps past a contact are dropped
+      have = (live >> (((e.y >> 20) & 31u) >> lgL)) & 1u;  // entries of decided steps are dropped
     }
     __syncwarp();
     top -= n;
@@ -584,7 +598,7 @@ __device__ __noinline__ int traverse(WarpSmem& S, const KWorldDev* __restrict__ 
 // pairs are common and an inline FP64 contact ends an item early) or as the
 // fallback after a main pass whose list overflowed (otherwise it returns at
 // once); its verdicts overwrite the main pass's.
-template <int MINB, bool FP64>
+template <int MINB, bool FP64, bool EDGES>
 __global__ void __launch_bounds__(kWarps * 32, MINB)
     k_engine(const KWorldDev* __restrict__ W, const EngineArgs A)
 {
@@ -607,13 +621,20 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
     for (int w = 0; w < kWarps; ++w) B.flag[w] = 2;
   }
   __syncthreads();
-  const int total = A.mode == MODE_EDGES ? A.meta[1] : A.B;
-  const int maxn = A.mode == MODE_EDGES ? A.meta[0] : 0;  // last round index
+  // configurations of one robot go in groups of G = 32 / L (L = its link
+  // count rounded up to 8, 16 or 32) per work item in the main pass; mixed
+  // robots and the FP64 pass take one configuration per item
+  const int lgC = EDGES || FP64 || A.robot < 0
+                      ? 5
+                      : (W->robots[A.robot].nlinks <= 8 ? 3 : (W->robots[A.robot].nlinks <= 16 ? 4 : 5));
+  const int Gcfg = 32 >> lgC;
+  const int total = EDGES ? A.meta[1] : (A.B + Gcfg - 1) / Gcfg;
+  const int maxn = EDGES ? A.meta[0] : 0;  // last round index
   const int grab = A.grab >= 1 && A.grab <= 16 ? A.grab : kGrab;
   const int job_flush = A.job_flush >= 8 && A.job_flush <= kJobCap - 32 ? A.job_flush : kJobCap - 32;
   const int chunk = A.chunk >= 1 && A.chunk <= kMaxChunk ? A.chunk : 1;
-  const int nchunked = A.mode == MODE_EDGES ? A.meta[2] : 0;
-  const int split = A.mode == MODE_EDGES ? A.meta[3] : 0;
+  const int nchunked = EDGES ? A.meta[2] : 0;
+  const int split = EDGES ? A.meta[3] : 0;
 
 #pragma unroll 1
   for (;;) {
@@ -625,8 +646,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
     for (unsigned it = base; it < base + grab && it < (unsigned)total; ++it) {
       // ---- decode the item
       int rid = A.robot;
-      int b = (int)it, e = 0, k0 = 0, k1 = 0, n = 0;
-      if (A.mode == MODE_EDGES) {
+      int b = 0, e = 0, k0 = 0, k1 = 0, n = 0;
+      if (EDGES) {
         // rounds r < J: steps [r*chunk, r*chunk + chunk) of every edge that
         // reaches r*chunk, checked in order; rounds r >= J: the single step
         // split + (r - J)
@@ -644,67 +665,70 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
         } else {
           k0 = k1 = split + (lo - nchunked);
         }
-      } else if (rid < 0) {
-        rid = __ldg(A.robot_ids + b);
+      } else {
+        // configurations b .. b + k1 of the item
+        b = (int)it * Gcfg;
+        k1 = min(Gcfg, A.B - b) - 1;
+        if (rid < 0) rid = __ldg(A.robot_ids + b);
       }
-      // Steps in groups of up to G = 32 / L (edge items of the main pass;
-      // L = the link count rounded up to 8, 16 or 32): lanes g L + link
-      // compute FK of link `link` at step kb + g, link row g L + link of
-      // S.T holds it, and one traversal per query set decides the group's
-      // steps together.  Configurations and the FP64 pass use groups of one.
+      // Steps (configurations) in groups of up to G = 32 / L: lanes g L +
+      // link compute FK of link `link` at step g of the group, link row
+      // g L + link of S.T holds it, and one traversal per query set decides
+      // the group's steps together.  The FP64 pass uses groups of one.
       const KRobotDev& R = W->robots[rid];
       const int nl = R.nlinks;
       const int lgL = nl <= 8 ? 3 : (nl <= 16 ? 4 : 5);
       const int L = 1 << lgL;
-      const int Gmax = (FP64 || A.mode != MODE_EDGES) ? 1 : 32 / L;
+      const int Gmax = FP64 ? 1 : 32 / L;
 #pragma unroll 1
       for (int kb = k0; kb <= k1; kb += Gmax) {
-        int glim = min(Gmax, k1 - kb + 1);
-        if (A.mode == MODE_EDGES) {
+        const int gn = min(Gmax, k1 - kb + 1);
+        unsigned live = gn >= 32 ? 0xffffffffu : (1u << gn) - 1u;
+        if (EDGES) {
           int fh = 0;
           if (lane == 0) fh = *((volatile int*)(A.first_hit + e));
           fh = __shfl_sync(0xffffffffu, fh, 0);
           if (fh <= kb) break;  // this or an earlier step of the edge already hit
-          glim = min(glim, fh - kb);
+          if (fh - kb < 32) live &= (1u << (fh - kb)) - 1u;
         }
+        const int cb = EDGES ? 0 : b + kb;  // first configuration of the group
         if (lane == 0) {
-          if (A.mode == MODE_EDGES) {
+          if (EDGES) {
             S.item_qa = A.qa + (size_t)e * nl;
             S.item_qb = A.qb + (size_t)e * nl;
           } else {
-            S.item_qa = A.q + (size_t)b * A.q_stride;
+            S.item_qa = A.q + (size_t)cb * A.q_stride;
             S.item_qb = nullptr;
           }
-          S.item_k = kb;
+          S.item_k = EDGES ? kb : 0;
           S.item_n = n;
-          S.item_id = A.mode == MODE_EDGES ? e : b;
+          S.item_id = EDGES ? e : cb;
           S.item_rid = rid;
         }
         // joint values in FP32 with an error bound e_q against the canonical
         // FP64 values (exact for configurations; FMA interpolation for edges)
         const int g = lane >> lgL, link = lane & (L - 1);
-        const bool valid = g < glim && link < nl;
+        const bool valid = ((live >> g) & 1u) && link < nl;
         float q = 0.f, e_q = 0.f;
         if (valid) {
-          if (A.mode == MODE_EDGES) {
+          if (EDGES) {
             const float a = __ldg(A.qa + (size_t)e * nl + link), bq = __ldg(A.qb + (size_t)e * nl + link);
             const float d = bq - a;
             q = fmaf((float)(kb + g) / (float)n, d, a);
             e_q = kU * (fabsf(d) + fabsf(q) + fabsf(a)) * 1.01f + 1e-30f;
           } else {
-            q = __ldg(A.q + (size_t)b * A.q_stride + link);
+            q = __ldg(A.q + (size_t)(cb + g) * A.q_stride + link);
           }
         }
         __syncwarp();
-        if (!FP64) items += (unsigned long long)glim;
+        if (!FP64) items += (unsigned long long)__popc(live);
         if (__any_sync(0xffffffffu, valid && !(fabsf(q) < 1.0e6f))) {
           if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
           continue;
         }
         if (A.mode != MODE_CONFIGS) {
           // joint limits: certain in FP32 away from the bounds, canonical FP64
-          // comparison (RobotCSpace.cpp:610-630) within rounding of them; the
-          // first violating step ends the group there
+          // comparison (RobotCSpace.cpp:610-630) within rounding of them
           bool unsure = false;
           if (valid) {
             const float lo = R.qmin[link], hi = R.qmax[link];
@@ -713,20 +737,27 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           }
           bool viol = false;
           if (unsure) {
-            const double q64 = A.mode == MODE_EDGES
+            const double q64 = EDGES
                                    ? kx_interp((double)S.item_qa[link], (double)S.item_qb[link], kb + g, n)
-                                   : (double)S.item_qa[link];
+                                   : (double)S.item_qa[(size_t)g * A.q_stride + link];
             viol = q64 < R.qmin64[link] || q64 > R.qmax64[link];
           }
-          const int gv = (int)__reduce_min_sync(0xffffffffu, viol ? (unsigned)g : 32u);
-          if (gv < glim) {
-            if (lane == 0) {
-              if (A.mode == MODE_EDGES) atomicMin(A.first_hit + e, kb + gv);
-              else A.feasible[b] = 0;
+          const unsigned vm = __reduce_or_sync(0xffffffffu, viol ? 1u << g : 0u);
+          if (vm) {
+            if (EDGES) {
+              // the first violating step ends the edge there
+              const int gv = __ffs(vm) - 1;
+              if (lane == 0) atomicMin(A.first_hit + e, kb + gv);
+              live &= (1u << gv) - 1u;
+            } else {
+              if (lane < 32 && ((vm >> lane) & 1u)) A.feasible[cb + lane] = 0;
+              live &= ~vm;
             }
-            glim = gv;
           }
-          if (glim == 0) break;
+          if (live == 0) {
+            if (EDGES) break;
+            continue;
+          }
         }
         float P[12], delta;
         warp_fk32_group(R, lane, L, valid, q, e_q, P, &delta);
@@ -737,119 +768,126 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           S.gerr[lane] = rot_gram_err32(P);
         }
         __syncwarp();
-        int env_lim = glim, self_lim = glim;
+        unsigned env_hits = 0, self_hits = 0;
         int fk64 = 0;
-        const bool want_env = A.mode != MODE_CONFIGS || A.env_hit != nullptr;
-        const bool want_self = A.mode != MODE_CONFIGS || A.self_hit != nullptr;
         if (A.mode != MODE_CONFIGS) {
           // edges and feasibility: any contact decides a step, so the
           // environment and self queries share one traversal (one stack
           // drain per group instead of two)
           const int nq = R.nqueries_env + R.nqueries_self;
           if (nq > 0)
-            env_lim = traverse<FP64>(S, W, R, R.query_off, nq, lane, spill, spill_cap, T64, fk64, A, job_flush, cnt,
-                                     all, warp, B, 0, glim, lgL);
-          self_lim = env_lim >= 0 ? env_lim : glim;
+            env_hits = traverse<FP64, EDGES>(S, W, R, R.query_off, nq, lane, spill, spill_cap, T64, fk64, A,
+                                             job_flush, cnt, all, warp, B, 0, live, lgL);
         } else {
           // configurations report the environment and self verdicts apart
-          if (want_env && R.nqueries_env > 0)
-            env_lim = traverse<FP64>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64, fk64, A,
-                                     job_flush, cnt, all, warp, B, 0, glim, lgL);
-          if (want_self && R.nqueries_self > 0)
-            self_lim = traverse<FP64>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane, spill,
-                                      spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0, glim, lgL);
+          if (A.env_hit != nullptr && R.nqueries_env > 0)
+            env_hits = traverse<FP64, EDGES>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64,
+                                             fk64, A, job_flush, cnt, all, warp, B, 0, live, lgL);
+          if (A.self_hit != nullptr && R.nqueries_self > 0)
+            self_hits = traverse<FP64, EDGES>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane,
+                                              spill, spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0, live,
+                                              lgL);
         }
-        if (env_lim < 0 || self_lim < 0) {
+        if ((env_hits | self_hits) & kTrOverflow) {
           if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
           continue;
         }
-        const int ghit = min(env_lim, self_lim);
-        if (lane == 0) {
-          // verdicts only ever turn into contacts (the outputs start as
-          // "free"), so shared traversals and the FP64 pass can add theirs
-          // in any order
+        // verdicts only ever turn into contacts (the outputs start as
+        // "free"), so shared traversals and the FP64 pass can add theirs in
+        // any order
+        const unsigned any_hits = env_hits | self_hits;
+        if (EDGES) {
+          if (any_hits) {
+            if (lane == 0) atomicMin(A.first_hit + e, kb + __ffs(any_hits) - 1);
+            __syncwarp();
+            break;
+          }
+        } else if (lane < 32) {
           if (A.mode == MODE_CONFIGS) {
-            if (A.env_hit && env_lim < glim) A.env_hit[b] = 1;
-            if (A.self_hit && self_lim < glim) A.self_hit[b] = 1;
-          } else if (A.mode == MODE_FEASIBLE) {
-            if (ghit < glim) A.feasible[b] = 0;
-          } else if (ghit < glim) {
-            atomicMin(A.first_hit + e, kb + ghit);
+            if ((env_hits >> lane) & 1u) A.env_hit[cb + lane] = 1;
+            if ((self_hits >> lane) & 1u) A.self_hit[cb + lane] = 1;
+          } else if ((any_hits >> lane) & 1u) {
+            A.feasible[cb + lane] = 0;
           }
         }
         __syncwarp();
-        if (A.mode == MODE_EDGES && ghit < glim) break;
       }  // step groups of the item
     }
   }
 
   // ---- queue drained: take over halves of the block's deep traversals
-  if (lane == 0) {
-    atomicExch(&B.flag[warp], 0);
-    atomicAdd(&B.idle, 1);
-  }
-  __syncwarp();
+  // (edge batches; configuration items are short and their warps just end)
+  if (EDGES) {
+    if (lane == 0) {
+      atomicExch(&B.flag[warp], 0);
+      atomicAdd(&B.idle, 1);
+    }
+    __syncwarp();
 #pragma unroll 1
-  for (int spins = 0, waits = 0;;) {
-    int f = 0;
-    if (lane == 0) f = *((volatile int*)&B.flag[warp]);
-    f = __shfl_sync(0xffffffffu, f, 0);
-    if (f == 1) {
-      __threadfence_block();
-      if (lane == 0) atomicSub(&B.idle, 1);
-      __syncwarp();
-      const KRobotDev& R = W->robots[S.item_rid];
-      const int nl = R.nlinks;
-      const int lgL = nl <= 8 ? 3 : (nl <= 16 ? 4 : 5);
-      int glim = S.don_glim;
-      if (A.mode == MODE_EDGES) {
-        int fh = 0;
-        if (lane == 0) fh = *((volatile int*)(A.first_hit + S.item_id));
-        fh = __shfl_sync(0xffffffffu, fh, 0);
-        glim = fh <= S.item_k ? 0 : min(glim, fh - S.item_k);  // steps not decided yet
-      }
-      if (glim > 0) {
-        int fk64 = 0;
-        const bool self = ((S.stack[0].y >> 25) & 63u) < 32u;
-        const int res = traverse<FP64>(S, W, R, 0, 0, lane, spill, spill_cap, T64, fk64, A, job_flush, cnt, all,
-                                       warp, B, S.don_top, glim, lgL);
-        if (lane == 0) {
-          if (res == TR_OVERFLOW) {
-            set_status(W->status, KGPU_ERR_OVERFLOW);
-          } else if (res < glim) {
-            if (A.mode == MODE_EDGES) atomicMin(A.first_hit + S.item_id, S.item_k + res);
-            else if (A.mode == MODE_FEASIBLE) A.feasible[S.item_id] = 0;
-            else if (self && A.self_hit) A.self_hit[S.item_id] = 1;
-            else if (!self && A.env_hit) A.env_hit[S.item_id] = 1;
+    for (int spins = 0, waits = 0;;) {
+      int f = 0;
+      if (lane == 0) f = *((volatile int*)&B.flag[warp]);
+      f = __shfl_sync(0xffffffffu, f, 0);
+      if (f == 1) {
+        __threadfence_block();
+        if (lane == 0) atomicSub(&B.idle, 1);
+        __syncwarp();
+        const KRobotDev& R = W->robots[S.item_rid];
+        const int nl = R.nlinks;
+        const int lgL = nl <= 8 ? 3 : (nl <= 16 ? 4 : 5);
+        unsigned live = S.don_live;
+        if (EDGES) {
+          int fh = 0;
+          if (lane == 0) fh = *((volatile int*)(A.first_hit + S.item_id));
+          fh = __shfl_sync(0xffffffffu, fh, 0);
+          // steps not decided yet
+          if (fh <= S.item_k) live = 0;
+          else if (fh - S.item_k < 32) live &= (1u << (fh - S.item_k)) - 1u;
+        }
+        if (live != 0) {
+          int fk64 = 0;
+          const bool self = ((S.stack[0].y >> 25) & 63u) < 32u;
+          const unsigned hits = traverse<FP64, EDGES>(S, W, R, 0, 0, lane, spill, spill_cap, T64, fk64, A, job_flush,
+                                                      cnt, all, warp, B, S.don_top, live, lgL);
+          if (lane == 0) {
+            if (hits & kTrOverflow) {
+              set_status(W->status, KGPU_ERR_OVERFLOW);
+            } else if (hits) {
+              const int g = __ffs(hits) - 1;
+              if (EDGES) atomicMin(A.first_hit + S.item_id, S.item_k + g);
+              else if (A.mode == MODE_FEASIBLE) A.feasible[S.item_id + g] = 0;
+              else if (self && A.self_hit) A.self_hit[S.item_id + g] = 1;
+              else if (!self && A.env_hit) A.env_hit[S.item_id + g] = 1;
+            }
           }
         }
+        if (lane == 0) {
+          atomicExch(&B.flag[warp], 0);
+          atomicAdd(&B.idle, 1);
+        }
+        __syncwarp();
+        spins = 0;
+        waits = 0;
+        continue;
       }
-      if (lane == 0) {
-        atomicExch(&B.flag[warp], 0);
-        atomicAdd(&B.idle, 1);
+      if (f == 0) {
+        int idle = 0;
+        if (lane == 0) idle = *((volatile int*)&B.idle);
+        idle = __shfl_sync(0xffffffffu, idle, 0);
+        if (idle >= kWarps || spins >= kShareSpins) {
+          int old = 0;
+          if (lane == 0) old = atomicCAS(&B.flag[warp], 0, 4);
+          if (__shfl_sync(0xffffffffu, old, 0) == 0) break;  // left: no longer claimable
+          continue;  // claimed meanwhile: the hand-over is in progress
+        }
+      } else if (++waits > kShareSpins) {
+        // a hand-over that does not complete: report it and stop
+        if (lane == 0) set_status(W->status, KGPU_ERR_TIMEOUT);
+        break;
       }
-      __syncwarp();
-      spins = 0;
-      waits = 0;
-      continue;
+      ++spins;
+      __nanosleep(256);
     }
-    if (f == 0) {
-      int idle = 0;
-      if (lane == 0) idle = *((volatile int*)&B.idle);
-      idle = __shfl_sync(0xffffffffu, idle, 0);
-      if (idle >= kWarps || spins >= kShareSpins) {
-        int old = 0;
-        if (lane == 0) old = atomicCAS(&B.flag[warp], 0, 4);
-        if (__shfl_sync(0xffffffffu, old, 0) == 0) break;  // left: no longer claimable
-        continue;  // claimed meanwhile: the hand-over is in progress
-      }
-    } else if (++waits > kShareSpins) {
-      // a hand-over that does not complete: report it and stop
-      if (lane == 0) set_status(W->status, KGPU_ERR_TIMEOUT);
-      break;
-    }
-    ++spins;
-    __nanosleep(256);
   }
   unsigned long long np = cnt.node_pairs, tp = cnt.tri_pairs, bd = cnt.band;
 #pragma unroll
@@ -929,11 +967,11 @@ __global__ void __launch_bounds__(kWarps * 32, 2) k_self_pairs(const KWorldDev* 
       unsigned int known = 0;
       if (lane == 0) known = *((volatile unsigned int*)(pair_mask + a));
       if ((__shfl_sync(0xffffffffu, known, 0) >> tgt) & 1u) continue;
-      const int res = traverse<true>(S, W, R, qidx, 1, lane, spill, spill_cap, T64, fk64, A, job_flush, cnt, all,
-                                     warp, B, 0, 1, 5);
+      const unsigned hits = traverse<true, false>(S, W, R, qidx, 1, lane, spill, spill_cap, T64, fk64, A, job_flush,
+                                                  cnt, all, warp, B, 0, 1u, 5);
       if (lane == 0) {
-        if (res == TR_OVERFLOW) set_status(W->status, KGPU_ERR_OVERFLOW);
-        else if (res == 0) atomicOr(pair_mask + a, 1u << tgt);
+        if (hits & kTrOverflow) set_status(W->status, KGPU_ERR_OVERFLOW);
+        else if (hits) atomicOr(pair_mask + a, 1u << tgt);
       }
       __syncwarp();
     }
@@ -1235,10 +1273,10 @@ __global__ void k_jacobian(const KWorldDev* __restrict__ W, int robot, const flo
   }
 }
 
-template <int MINB, bool FP64>
+template <int MINB, bool FP64, bool EDGES>
 cudaError_t init_engine()
 {
-  return cudaFuncSetAttribute(k_engine<MINB, FP64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(k_engine<MINB, FP64, EDGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)(sizeof(WarpSmem) * kWarps + sizeof(BlockShare)));
 }
 
@@ -1248,7 +1286,10 @@ template <int MINB, bool FP64>
 cudaError_t launch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, cudaStream_t s)
 {
   size_t smem = sizeof(WarpSmem) * kWarps + sizeof(BlockShare);
-  k_engine<MINB, FP64><<<blocks, kWarps * 32, smem, s>>>(W, A);
+  if (A.mode == MODE_EDGES)
+    k_engine<MINB, FP64, true><<<blocks, kWarps * 32, smem, s>>>(W, A);
+  else
+    k_engine<MINB, FP64, false><<<blocks, kWarps * 32, smem, s>>>(W, A);
   return cudaGetLastError();
 }
 
@@ -1289,11 +1330,16 @@ int engine_scratch_doubles() { return kT64Doubles; }
 
 cudaError_t engine_init()
 {
-  cudaError_t e = init_engine<2, false>();
-  if (e == cudaSuccess) e = init_engine<3, false>();
-  if (e == cudaSuccess) e = init_engine<4, false>();
-  if (e == cudaSuccess) e = init_engine<2, true>();
-  if (e == cudaSuccess) e = init_engine<3, true>();
+  cudaError_t e = init_engine<2, false, true>();
+  if (e == cudaSuccess) e = init_engine<3, false, true>();
+  if (e == cudaSuccess) e = init_engine<4, false, true>();
+  if (e == cudaSuccess) e = init_engine<2, true, true>();
+  if (e == cudaSuccess) e = init_engine<3, true, true>();
+  if (e == cudaSuccess) e = init_engine<2, false, false>();
+  if (e == cudaSuccess) e = init_engine<3, false, false>();
+  if (e == cudaSuccess) e = init_engine<4, false, false>();
+  if (e == cudaSuccess) e = init_engine<2, true, false>();
+  if (e == cudaSuccess) e = init_engine<3, true, false>();
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_self_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(sizeof(WarpSmem) * kWarps + sizeof(BlockShare)));
@@ -1366,7 +1412,7 @@ cudaError_t launch_check_configs(const KWorldDev* W, const Scratch& S, int robot
   A.env_hit = env_hit;
   A.self_hit = self_hit;
   A.feasible = feasible;
-  A.inline64 = fp64_inline != 0;  // default (-1): inline for configuration batches
+  A.inline64 = fp64_inline == 1;  // default (-1): deferred, as for edge batches
   A.spill = S.spill;
   A.spill_per_warp = (int)S.spill_per_warp;
   return dispatch_engine(W, A, S, blocks, per_sm, s);

@@ -223,7 +223,7 @@ struct kgpu_world_s {
   int grab = 2;            // work items per queue atomic (1..16)
   int job_flush = 64;      // triangle-pair jobs collected before testing them (8..64)
   int edge_chunk = 16;     // consecutive steps of an edge per work item (1..64)
-  int fp64_inline = -1;    // FP64 triangle tests inline (1) or deferred to k_band (0); -1: by batch kind
+  int fp64_inline = -1;    // FP64 triangle tests inline (1) or deferred to k_band (0); -1: deferred
   int num_sms = 0;
   bool tables_dirty = true;
   // pinned staging for the host-buffer entry points
