@@ -248,6 +248,16 @@ def secondary_metrics(reps: int = 2) -> dict:
     # ray casting: four 640x480 pinhole cameras into the icosphere field
     robot1, env1, _ = sc.scene_cfg1(n_edges=2)
     w1 = World(env1, [robot1])
+    # configuration batches of one robot (environment and self verdicts, and
+    # feasibility) on the same scene
+    q1 = torch.as_tensor(sc.uniform_configs(robot1, 262144, np.random.default_rng(2003))).cuda()
+    ms_c = _event_ms(lambda: w1.check_configs(q1, sync=False), reps)
+    ms_f = _event_ms(lambda: w1.is_feasible(q1, sync=False), reps)
+    w1.sync()
+    out["configs"] = {"value": q1.shape[0] / (ms_c / 1e3), "unit": "configs/s",
+                      "sample": "262,144 uniform configurations of the 7-DOF arm among 2,000 icospheres; "
+                                "environment and self verdicts apart",
+                      "feasibility": {"value": q1.shape[0] / (ms_f / 1e3), "unit": "configs/s"}}
     rays = [sc.camera_rays(eye, sc.SPHERE_FIELD_CENTER, 640, 480) for eye in sc.CAMERA_EYES]
     Sd = torch.as_tensor(np.concatenate([r[0] for r in rays])).cuda()
     Dd = torch.as_tensor(np.concatenate([r[1] for r in rays])).cuda()
