@@ -126,6 +126,36 @@ def test_feasibility_matches_oracle(cfg0):
     assert f[::7].sum() == 0
 
 
+@pytest.mark.parametrize("which", ["dual_arm", "humanoid"])
+def test_config_groups_other_link_counts(built, which):
+    """Configuration batches are checked in groups of 32 / L configurations
+    (L = link count rounded up to 8, 16 or 32): the 12-link dual arm runs in
+    pairs, the 31-link humanoid alone.  A batch size that is not a multiple
+    of the group, joint-limit violations at every position of a group, and
+    environment, self and feasibility verdicts against the oracle."""
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robot = sc.dual_arm() if which == "dual_arm" else sc.humanoid()
+    env = sc.sphere_field(np.random.default_rng(1001), n=400)
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    q = sc.uniform_configs(robot, 1001, np.random.default_rng(31))
+    eh_o, sh_o, _ = o.check_configs(q, nthreads=NT)
+    eh, sh = (x.cpu().numpy() for x in w.check_configs(q))
+    assert np.array_equal(eh, eh_o) and np.array_equal(sh, sh_o)
+    assert 0.02 < eh.mean() < 0.98
+    qq = q.copy()
+    span = robot.qmax - robot.qmin
+    for k in range(0, len(qq), 5):
+        j = (k // 5) % robot.num_links
+        if span[j] > 0:
+            qq[k, j] = robot.qmax[j] + 0.25
+    f_o = o.is_feasible(qq, nthreads=NT)
+    f = w.is_feasible(qq).cpu().numpy()
+    assert np.array_equal(f, f_o)
+    w.close()
+
+
 def test_cfg1_configs_bit_exact(cfg1):
     robot, env, (qa, qb, ns), w, o = cfg1
     q = sc.uniform_configs(robot, 2048, np.random.default_rng(7))
