@@ -448,6 +448,11 @@ def main():
     c_dt = time.perf_counter() - c0
     mismatches = int((fh_o != fh).sum()) + int((fh_plain.cpu().numpy() != fh_o[:sub]).sum())
     cpu_rate = checked_configs(fh_o, ns) / c_dt
+    # the reference's serial path: one thread over a prefix of the edges
+    n1 = min(len(ns), 2048)
+    c0 = time.perf_counter()
+    fh_1, _ = o.check_edges(qa[:n1], qb[:n1], ns[:n1], nthreads=1)
+    cpu_rate_1 = checked_configs(fh_1, ns[:n1]) / (time.perf_counter() - c0)
     items = int(cnt[2])
     alg_bytes = int(cnt[0]) * NODE_BYTES + int(cnt[1]) * TRI_PAIR_BYTES + items * (4 * robot.num_links) + 4 * len(ns)
     achieved = alg_bytes / (t_dev / args.steps) / 1e9
@@ -467,14 +472,16 @@ def main():
                    "launch": "CUDA-graph edge plan", "autotuned": tuned},
         "secondary": secondary,
         "e2e": e2e,
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": 7 * args.steps,  # per edge plan: 3 prep kernels, main pass, k_band, fallback, finalize
         "plain_fp64": {"value": plain_rate, "unit": "configs/s", "edges": sub, "speedup": value / plain_rate},
         "mismatches": mismatches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_step": alg_bytes},
         "cpu_baseline": {"value": cpu_rate, "unit": "configs/s", "cores": cores, "kind": "port",
-                         "sample": f"all {len(ns)} edges, FP64 oracle, std::thread over all cores"},
+                         "sample": f"all {len(ns)} edges, FP64 oracle, std::thread over all cores",
+                         "single_thread": {"value": cpu_rate_1, "unit": "configs/s", "cores": 1,
+                                           "sample": f"first {n1} edges, FP64 oracle, one thread"}},
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
