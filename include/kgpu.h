@@ -221,6 +221,16 @@ kgpu_status kgpu_ik_solve(kgpu_world world, int32_t robot, int32_t B, float* q, 
 kgpu_status kgpu_self_collision_pairs(kgpu_world world, int32_t robot, const float* q, int32_t B,
                                       uint32_t* pair_mask, kgpu_stream stream);
 
+/* Independent self-collision pairs (RandomizedIndependentSelfCollisionPairs'
+ * second pass, TestIndependentCollisions,
+ * Cpp/Modeling/RandomizedSelfCollisions.cpp:42-66): for each of B
+ * configurations the enabled pairs set in candidates (num_links words, as
+ * kgpu_self_collision_pairs fills them) are tested; when exactly one of them
+ * collides, its bit is set in pair_mask (OR-accumulated). */
+kgpu_status kgpu_independent_self_collision_pairs(kgpu_world world, int32_t robot, const float* q, int32_t B,
+                                                  const uint32_t* candidates, uint32_t* pair_mask,
+                                                  kgpu_stream stream);
+
 /* Full Jacobians of points on links at B configurations: J[b] is 6 x
  * num_links (row-major), rows 0-2 the angular part, rows 3-5 the linear
  * part of the world velocity of the point plocal[b] (link frame) on link

@@ -89,6 +89,7 @@ _SIGS = {
     "kgpu_ik_solve": [_c_p, _i32, _i32, _c_p, _c_p, _i32, _c_p, _c_p, _c_p, _i32, ctypes.c_float, _c_p, _c_p, _c_p,
                       _c_p],
     "kgpu_self_collision_pairs": [_c_p, _i32, _c_p, _i32, _c_p, _c_p],
+    "kgpu_independent_self_collision_pairs": [_c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
     "kgpu_jacobian": [_c_p, _i32, _c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
     "kgpu_raycast": [_c_p, _c_p, _c_p, _i32, _c_p, _c_p, _c_p, _c_p, _c_p],
     "kgpu_check_configs_host": [_c_p, _i32, _c_p, _i32, _c_p, _c_p],

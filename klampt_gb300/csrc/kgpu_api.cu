@@ -962,8 +962,20 @@ kgpu_status kgpu_self_collision_pairs(kgpu_world w, int32_t robot, const float* 
   kgpu_status st = check_world(w, robot);
   if (st) return st;
   if (B < 0 || (B > 0 && (!q || !pair_mask))) return fail(KGPU_ERR_INVALID, "bad buffers");
-  return launch_status(launch_self_pairs(w->d_dev, w->scratch, robot, q, B, pair_mask, w->num_sms, (cudaStream_t)s),
-                       "kgpu_self_collision_pairs");
+  return launch_status(
+      launch_self_pairs(w->d_dev, w->scratch, robot, q, B, nullptr, pair_mask, w->num_sms, (cudaStream_t)s),
+      "kgpu_self_collision_pairs");
+}
+
+kgpu_status kgpu_independent_self_collision_pairs(kgpu_world w, int32_t robot, const float* q, int32_t B,
+                                                  const uint32_t* candidates, uint32_t* pair_mask, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && (!q || !candidates || !pair_mask))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  return launch_status(
+      launch_self_pairs(w->d_dev, w->scratch, robot, q, B, candidates, pair_mask, w->num_sms, (cudaStream_t)s),
+      "kgpu_independent_self_collision_pairs");
 }
 
 kgpu_status kgpu_jacobian(kgpu_world w, int32_t robot, const float* q, int32_t B, const int32_t* links,

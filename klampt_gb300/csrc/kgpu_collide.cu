@@ -912,8 +912,11 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
 // 19-38, batched): per configuration, FK then every enabled link pair on its
 // own, FP64 decisions inline; a pair found colliding sets bit tgt of
 // pair_mask[a] (OR-accumulated across calls), and pairs already set are not
-// tested again.
+// tested again.  With `cand` (TestIndependentCollisions,
+// RandomizedSelfCollisions.cpp:42-66): only the candidate pairs are tested,
+// and a configuration in which exactly one of them collides sets that pair.
 __global__ void __launch_bounds__(kWarps * 32, 2) k_self_pairs(const KWorldDev* __restrict__ W, const EngineArgs A,
+                                                                 const unsigned int* __restrict__ cand,
                                                                  unsigned int* pair_mask)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -959,22 +962,41 @@ __global__ void __launch_bounds__(kWarps * 32, 2) k_self_pairs(const KWorldDev* 
     }
     __syncwarp();
     int fk64 = 0;
+    int found = 0, fa = 0, ft = 0;
 #pragma unroll 1
     for (int qi = 0; qi < R.nqueries_self; ++qi) {
       const int qidx = R.query_off + R.nqueries_env + qi;
       const uint32_t qw = __ldg(W->queries + qidx);
       const int a = qw & 0xff, tgt = (qw >> 8) & 0xff;
-      unsigned int known = 0;
-      if (lane == 0) known = *((volatile unsigned int*)(pair_mask + a));
-      if ((__shfl_sync(0xffffffffu, known, 0) >> tgt) & 1u) continue;
+      if (cand) {
+        if (!((__ldg(cand + a) >> tgt) & 1u)) continue;  // not a candidate pair
+      } else {
+        unsigned int known = 0;
+        if (lane == 0) known = *((volatile unsigned int*)(pair_mask + a));
+        if ((__shfl_sync(0xffffffffu, known, 0) >> tgt) & 1u) continue;
+      }
       const unsigned hits = traverse<true, false>(S, W, R, qidx, 1, lane, spill, spill_cap, T64, fk64, A, job_flush,
                                                   cnt, all, warp, B, 0, 1u, 5);
-      if (lane == 0) {
-        if (hits & kTrOverflow) set_status(W->status, KGPU_ERR_OVERFLOW);
-        else if (hits) atomicOr(pair_mask + a, 1u << tgt);
+      if (hits & kTrOverflow) {
+        if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
+        found = 2;  // no verdict for this configuration
+        break;
+      }
+      if (hits) {
+        if (!cand) {
+          if (lane == 0) atomicOr(pair_mask + a, 1u << tgt);
+        } else if (++found > 1) {
+          break;  // more than one candidate pair collides
+        } else {
+          fa = a;
+          ft = tgt;
+        }
       }
       __syncwarp();
     }
+    // independent pairs: the configuration's only colliding candidate pair
+    if (cand && found == 1 && lane == 0) atomicOr(pair_mask + fa, 1u << ft);
+    __syncwarp();
   }
 }
 
@@ -1358,7 +1380,7 @@ cudaError_t launch_fk(const KWorldDev* W, int robot, const float* q, int B, floa
 }
 
 cudaError_t launch_self_pairs(const KWorldDev* W, const Scratch& S, int robot, const float* q, int B,
-                              unsigned int* pair_mask, int num_sms, cudaStream_t s)
+                              const unsigned int* cand, unsigned int* pair_mask, int num_sms, cudaStream_t s)
 {
   if (B <= 0) return cudaSuccess;
   cudaError_t err = cudaMemsetAsync(S.counters, 0, sizeof(unsigned int), s);
@@ -1374,7 +1396,7 @@ cudaError_t launch_self_pairs(const KWorldDev* W, const Scratch& S, int robot, c
   A.spill_per_warp = (int)S.spill_per_warp;
   A.inline64 = 1;
   const size_t smem = sizeof(WarpSmem) * kWarps + sizeof(BlockShare);
-  k_self_pairs<<<2 * num_sms, kWarps * 32, smem, s>>>(W, A, pair_mask);
+  k_self_pairs<<<2 * num_sms, kWarps * 32, smem, s>>>(W, A, cand, pair_mask);
   return cudaGetLastError();
 }
 

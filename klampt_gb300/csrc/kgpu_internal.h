@@ -266,7 +266,7 @@ cudaError_t launch_ik(const KWorldDev* W, int robot, int B, float* q, const int*
                       const float* plocal, const float* ptarget, const float* Rtarget, int max_iters, float tol,
                       uint8_t* ok, float* residual, int* iters, cudaStream_t s);
 cudaError_t launch_self_pairs(const KWorldDev* W, const Scratch& S, int robot, const float* q, int B,
-                              unsigned int* pair_mask, int num_sms, cudaStream_t s);
+                              const unsigned int* cand, unsigned int* pair_mask, int num_sms, cudaStream_t s);
 cudaError_t launch_jacobian(const KWorldDev* W, int robot, const float* q, const int* links, int link_all,
                             const float* plocal, int B, float* J, cudaStream_t s);
 cudaError_t launch_raycast(const KWorldDev* Wd, const float* s, const float* d, int R, int* obj, int* tri,

@@ -318,6 +318,23 @@ class World:
             self.sync()
         return m
 
+    def independent_self_collision_pairs(self, q, candidates, robot: int = 0, mask=None, sync: bool = True):
+        """Candidate self pairs (uint32 words [L], as self_collision_pairs
+        returns them) that collide alone in some configuration of q [B, L]:
+        uint32 words [L], OR-accumulated into `mask` when given."""
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L).contiguous()
+        if isinstance(candidates, torch.Tensor):
+            c = candidates.to(device="cuda", dtype=torch.int32).reshape(L).contiguous()
+        else:  # uint32 words: reinterpret, bit 31 included
+            c = torch.as_tensor(np.ascontiguousarray(candidates, dtype=np.uint32).view(np.int32)).cuda().reshape(L)
+        m = torch.zeros(L, dtype=torch.int32, device="cuda") if mask is None else mask
+        check(lib().kgpu_independent_self_collision_pairs(self.handle, robot, _dptr(qd), qd.shape[0], _dptr(c),
+                                                          _dptr(m), _stream()))
+        if sync:
+            self.sync()
+        return m
+
     def jacobian(self, q, links, plocal, robot: int = 0, sync: bool = True):
         """Full Jacobians [B, 6, L] (angular rows, then linear) of points
         plocal [B, 3] (link frame) on links [B] (or one int for all)."""

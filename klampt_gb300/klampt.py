@@ -20,6 +20,7 @@ Mirrors (paths relative to the Klamp't tree):
   IKObjective / IKSolver (one objective)
                                    Python/klampt/src/robotik.h:21-260
   RandomizedSelfCollisionPairs     Cpp/Modeling/RandomizedSelfCollisions.h:24
+  RandomizedIndependentSelfCollisionPairs  Cpp/Modeling/RandomizedSelfCollisions.h:33
 Batched overloads: RobotModel.setConfigs / getJacobians, WorldCollider.check_configs /
 distance_batch / rayCastBatch, RobotCSpace.isFeasibleBatch / isVisibleBatch.
 
@@ -335,19 +336,41 @@ class IKSolver:
         return self._residual
 
 
-def RandomizedSelfCollisionPairs(robot: "RobotModel", numSamples: int, seed: int = 0) -> np.ndarray:
-    """collision[i, j] = True iff enabled pair (i, j) collided in one of
-    numSamples configurations drawn uniformly within the finite joint limits
-    (Cpp/Modeling/RandomizedSelfCollisions.cpp:9-38; DOFs with an infinite
-    limit keep their current value)."""
+def _sample_configs(robot: "RobotModel", numSamples: int, rng: np.random.Generator) -> np.ndarray:
+    """Configurations uniform within the finite joint limits; DOFs with an
+    infinite limit keep their current value (SampleRobot,
+    Cpp/Modeling/RandomizedSelfCollisions.cpp:9-17)."""
     spec = robot.spec
-    rng = np.random.default_rng(seed)
-    L = spec.num_links
     Q = np.tile(robot._q, (numSamples, 1)).astype(np.float32)
     fin = np.isfinite(spec.qmin) & np.isfinite(spec.qmax)
     Q[:, fin] = rng.uniform(spec.qmin[fin], spec.qmax[fin], (numSamples, int(fin.sum())))
+    return Q
+
+
+def _words_to_matrix(words: np.ndarray, L: int) -> np.ndarray:
+    return np.array([[bool((int(words[i]) >> j) & 1) for j in range(L)] for i in range(L)])
+
+
+def RandomizedSelfCollisionPairs(robot: "RobotModel", numSamples: int, seed: int = 0) -> np.ndarray:
+    """collision[i, j] = True iff enabled pair (i, j) collided in one of
+    numSamples configurations drawn uniformly within the finite joint limits
+    (Cpp/Modeling/RandomizedSelfCollisions.cpp:9-38)."""
+    Q = _sample_configs(robot, numSamples, np.random.default_rng(seed))
     words = robot.world.engine.self_collision_pairs(Q, robot=robot.index).cpu().numpy().astype(np.uint32)
-    return np.array([[bool((words[i] >> j) & 1) for j in range(L)] for i in range(L)])
+    return _words_to_matrix(words, robot.spec.num_links)
+
+
+def RandomizedIndependentSelfCollisionPairs(robot: "RobotModel", numSamples: int, seed: int = 0) -> np.ndarray:
+    """collision[i, j] = True iff enabled pair (i, j) was, in one of numSamples
+    further samples, the only colliding pair among those found colliding in
+    a first numSamples samples (Cpp/Modeling/RandomizedSelfCollisions.cpp:
+    42-66 and 114-140: TestCollisions, then TestIndependentCollisions)."""
+    rng = np.random.default_rng(seed)
+    eng = robot.world.engine
+    cand = eng.self_collision_pairs(_sample_configs(robot, numSamples, rng), robot=robot.index)
+    words = eng.independent_self_collision_pairs(_sample_configs(robot, numSamples, rng), cand,
+                                                 robot=robot.index).cpu().numpy().astype(np.uint32)
+    return _words_to_matrix(words, robot.spec.num_links)
 
 
 class RobotCSpace:

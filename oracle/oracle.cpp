@@ -240,10 +240,11 @@ bool bvtt_collide(Ctx& c, int la, int lb, int grp)
   const Robot& R = *c.R;
   const Env& E = *c.E;
   const Bvh& A = R.bvh[la];
-  const Bvh& B = lb >= 0 ? R.bvh[lb] : E.group_bvh[grp];
+  const int g = grp < 0 ? 0 : grp;  // a group only when lb < 0
+  const Bvh& B = lb >= 0 ? R.bvh[lb] : E.group_bvh[g];
   if (A.empty() || B.empty()) return false;
   double mA = R.margins[la];
-  double mB = lb >= 0 ? R.margins[lb] : E.group_margin[grp];
+  double mB = lb >= 0 ? R.margins[lb] : E.group_margin[g];
   double tol = 1e-9 + mA + mB;
   std::vector<std::pair<int, int>> st;
   st.reserve(256);
@@ -1147,6 +1148,45 @@ int orc_self_pairs(void* robot, void* env, const float* q, int B, unsigned* mask
           if (R->self_mask[i * L + j] && !((m[i] >> j) & 1u) && !R->tloc[i].empty() && !R->tloc[j].empty() &&
               bvtt_collide(c, i, j, -1))
             m[i] |= 1u << j;
+    }
+  });
+  for (auto& m : part)
+    for (int i = 0; i < L; ++i) mask[i] |= m[i];
+  return 0;
+}
+
+/* Independent self-collision pairs: the second pass of
+   RandomizedIndependentSelfCollisionPairs (TestIndependentCollisions,
+   Cpp/Modeling/RandomizedSelfCollisions.cpp:42-66).  Per configuration the
+   enabled candidate pairs (bit j of cand[i]) are tested; when exactly one
+   collides, its bit is set in mask.  The reference stops counting at the
+   second collision; the result is the same. */
+int orc_indep_pairs(void* robot, void* env, const float* q, int B, const unsigned* cand, unsigned* mask,
+                    int nthreads)
+{
+  Robot* R = (Robot*)robot;
+  Env* E = (Env*)env;
+  const int L = R->L;
+  std::vector<std::vector<unsigned>> part((size_t)std::max(1, nthreads), std::vector<unsigned>(L, 0u));
+  parallel_for(B, nthreads, [&](int t, int b0, int b1) {
+    Ctx c;
+    std::vector<uint32_t> masks(L, 0u);
+    c.init(R, E, masks.data());
+    std::vector<double> qd(L);
+    std::vector<unsigned>& m = part[t];
+    for (int b = b0; b < b1; ++b) {
+      for (int i = 0; i < L; ++i) qd[i] = (double)q[(size_t)b * L + i];
+      c.set_config(qd.data());
+      int found = 0, fi = 0, fj = 0;
+      for (int i = 0; i < L && found < 2; ++i)
+        for (int j = i + 1; j < L && found < 2; ++j)
+          if (R->self_mask[i * L + j] && ((cand[i] >> j) & 1u) && !R->tloc[i].empty() && !R->tloc[j].empty() &&
+              bvtt_collide(c, i, j, -1)) {
+            ++found;
+            fi = i;
+            fj = j;
+          }
+      if (found == 1) m[fi] |= 1u << fj;
     }
   });
   for (auto& m : part)

@@ -40,7 +40,8 @@ def lib():
         L.orc_robot_create.restype = P
         L.orc_env_create.restype = P
         for name in ("orc_check_configs", "orc_check_edges", "orc_is_feasible", "orc_pair_distance",
-                     "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian", "orc_self_pairs", "orc_ik"):
+                     "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian", "orc_self_pairs", "orc_ik",
+                     "orc_indep_pairs"):
             getattr(L, name).restype = ctypes.c_int
         L.orc_robot_destroy.argtypes = [P]
         L.orc_env_destroy.argtypes = [P]
@@ -213,6 +214,17 @@ def self_pairs(oracle: "Oracle", q, nthreads: int = 1, mask=None) -> np.ndarray:
     m = np.zeros(L, np.uint32) if mask is None else np.ascontiguousarray(mask, np.uint32).copy()
     lib().orc_self_pairs(ctypes.c_void_p(oracle.robot), ctypes.c_void_p(oracle.env), _p(q), ctypes.c_int(q.shape[0]),
                          _p(m), ctypes.c_int(nthreads))
+    return m
+
+
+def indep_pairs(oracle: "Oracle", q, cand, nthreads: int = 1, mask=None) -> np.ndarray:
+    """Candidate pairs (uint32 words) that collide alone in some configuration."""
+    L = oracle.nl
+    q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, L)
+    c = np.ascontiguousarray(cand, np.uint32).reshape(L)
+    m = np.zeros(L, np.uint32) if mask is None else np.ascontiguousarray(mask, np.uint32).copy()
+    lib().orc_indep_pairs(ctypes.c_void_p(oracle.robot), ctypes.c_void_p(oracle.env), _p(q), ctypes.c_int(q.shape[0]),
+                          _p(c), _p(m), ctypes.c_int(nthreads))
     return m
 
 

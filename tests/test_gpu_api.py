@@ -230,6 +230,34 @@ def test_self_collision_pair_sampling():
     W.close()
 
 
+def test_independent_self_collision_pairs():
+    """Candidate pairs that collide alone in a sample: engine against the FP64
+    oracle (humanoid: many candidate pairs, most samples with several
+    collisions), plus the Klamp't-facing two-pass function."""
+    from klampt_gb300.engine import World
+    from klampt_gb300.klampt import (RandomizedIndependentSelfCollisionPairs, RandomizedSelfCollisionPairs,
+                                     WorldModel)
+    from oracle.oracle_py import Oracle, indep_pairs, self_pairs
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    rng = np.random.default_rng(19)
+    for robot in (sc.arm(7, rings=8, segments=8), sc.humanoid()):
+        w = World(env, [robot])
+        o = Oracle(robot, env)
+        cand = self_pairs(o, sc.uniform_configs(robot, 2000, rng), nthreads=NT)
+        q = sc.uniform_configs(robot, 3000, rng)
+        m = w.independent_self_collision_pairs(q, cand).cpu().numpy().astype(np.uint32)
+        mo = indep_pairs(o, q, cand, nthreads=NT)
+        assert np.array_equal(m, mo) and mo.any()
+        assert not (mo & ~cand).any()  # independent pairs are candidates
+        w.close()
+    W = WorldModel([sc.humanoid()], env)
+    col = RandomizedSelfCollisionPairs(W.robot(0), 400, seed=5)
+    ind = RandomizedIndependentSelfCollisionPairs(W.robot(0), 400, seed=5)
+    # the two-pass function draws its candidate samples as the one-pass call does
+    assert ind.any() and not (ind & ~col).any()
+    W.close()
+
+
 def test_batched_ik_matches_oracle_iteration():
     """Batched IK (FP32, one warp per problem) against the FP64 restatement of
     the same iteration: same convergence verdicts on almost every problem,
