@@ -344,7 +344,10 @@ kgpu_status kgpu_check_edges_noalloc(kgpu_world world, int32_t robot, const floa
 
 /* ---- captured edge-check plans (CUDA-graph replay) ------------------------ */
 /* Records the whole edge-check pipeline for fixed device buffers into a CUDA
- * graph; each launch replays it on `stream`. */
+ * graph; each launch replays it on `stream`.  The plan keeps using the
+ * world's scratch buffers it was recorded with (buffers that later calls
+ * grow are kept until the world is destroyed); destroy plans before their
+ * world. */
 kgpu_status kgpu_edge_plan_create(kgpu_world world, int32_t robot, const float* qa,
                                   const float* qb, const int32_t* nsteps, int32_t E,
                                   int32_t* first_hit, kgpu_edge_plan* out);

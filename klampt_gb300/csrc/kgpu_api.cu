@@ -127,6 +127,8 @@ void append_bvh(const HostBvh& b, int node_base, int tri_base, std::vector<KNode
 
 void free_world_device(kgpu_world w)
 {
+  for (void* p : w->retired) cudaFree(p);
+  w->retired.clear();
   dfree(w->d_robots);
   dfree(w->d_queries);
   dfree(w->d_dev);
@@ -233,7 +235,12 @@ int grid_blocks(kgpu_world w) { return w->num_sms * w->blocks_per_sm; }
 kgpu_status ensure_edge_scratch(kgpu_world w, int E)
 {
   if ((size_t)E <= w->scratch.edge_cap) return KGPU_OK;
-  dfree(w->scratch.edge_perm);
+  if (w->live_plans > 0) {
+    w->retired.push_back(w->scratch.edge_perm);  // a captured plan still uses it
+    w->scratch.edge_perm = nullptr;
+  } else {
+    dfree(w->scratch.edge_perm);
+  }
   size_t cap = (size_t)E < 1024 ? 1024 : (size_t)E;
   CK(cudaMalloc((void**)&w->scratch.edge_perm, cap * sizeof(int)));
   w->scratch.edge_cap = cap;
@@ -856,9 +863,12 @@ kgpu_status kgpu_check_configs_multi(kgpu_world w, const int32_t* robot_ids, con
   if (B < 0 || (B > 0 && (!q || !robot_ids)) || q_stride < maxl)
     return fail(KGPU_ERR_INVALID, "bad buffers or q_stride %d < max links %d", q_stride, maxl);
   if (!env_hit && !self_hit) return KGPU_OK;
+  // the edge permutation buffer holds the robot-sorted order (grown on demand)
+  st = ensure_edge_scratch(w, B);
+  if (st) return st;
   return launch_status(launch_check_configs(w->d_dev, w->scratch, -1, robot_ids, q, q_stride, B, env_hit, self_hit,
                                             nullptr, grid_blocks(w), w->blocks_per_sm, (cudaStream_t)s, w->grab,
-                                            w->job_flush, w->fp64_inline),
+                                            w->job_flush, w->fp64_inline, (int)w->robots.size(), w->d_status),
                        "kgpu_check_configs_multi");
 }
 
@@ -1098,6 +1108,7 @@ kgpu_status kgpu_edge_plan_create(kgpu_world w, int32_t robot, const float* qa, 
     kgpu_edge_plan_destroy(p);
     return cuda_fail(e, "edge plan capture");
   }
+  w->live_plans++;
   *out = p;
   return KGPU_OK;
 }
@@ -1112,7 +1123,10 @@ kgpu_status kgpu_edge_plan_launch(kgpu_edge_plan p, kgpu_stream s)
 kgpu_status kgpu_edge_plan_destroy(kgpu_edge_plan p)
 {
   if (!p) return KGPU_OK;
-  if (p->exec) cudaGraphExecDestroy(p->exec);
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->world->live_plans--;
+  }
   if (p->graph) cudaGraphDestroy(p->graph);
   delete p;
   return KGPU_OK;

@@ -69,6 +69,7 @@ struct __align__(16) WarpSmem {
   const float* item_qb;       //   endpoints qa/qb (item_qb null for configurations)
   int item_k, item_n;         // edge step k of n
   int item_id;                // configuration index b, or edge index e
+  int item_cfg[4];            // configuration index of each step of a configuration group
   int item_rid;               // robot of the item
   int don_top;                // stack entries handed over by a sibling warp
   unsigned don_live;          // steps of the handed-over group still to decide
@@ -278,7 +279,7 @@ __device__ __noinline__ unsigned run_jobs(WarpSmem& S, const KWorldDev* __restri
           // the record names the edge step (or the configuration) and link
           // indices, not link rows
           const unsigned tl = tgt < 32 ? (unsigned)(tgt & lmask) : (unsigned)tgt;
-          const unsigned item = seq ? (unsigned)S.item_id : (unsigned)(S.item_id + step);
+          const unsigned item = seq ? (unsigned)S.item_id : (unsigned)S.item_cfg[step];
           const unsigned k = seq ? (unsigned)(S.item_k + step) : 0u;
           A.pend[at] = make_uint4(item, k | ((unsigned)(la & lmask) << 16) | (tl << 21), (unsigned)tA, (unsigned)tB);
         }
@@ -628,7 +629,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
                       ? 5
                       : (W->robots[A.robot].nlinks <= 8 ? 3 : (W->robots[A.robot].nlinks <= 16 ? 4 : 5));
   const int Gcfg = 32 >> lgC;
-  const int total = EDGES ? A.meta[1] : (A.B + Gcfg - 1) / Gcfg;
+  // mixed robots sorted by robot (A.perm set): per-robot groups, see k_cfg_offsets
+  const int total = EDGES ? A.meta[1] : (A.perm ? A.meta[0] : (A.B + Gcfg - 1) / Gcfg);
   const int maxn = EDGES ? A.meta[0] : 0;  // last round index
   const int grab = A.grab >= 1 && A.grab <= 16 ? A.grab : kGrab;
   const int job_flush = A.job_flush >= 8 && A.job_flush <= kJobCap - 32 ? A.job_flush : kJobCap - 32;
@@ -665,11 +667,21 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
         } else {
           k0 = k1 = split + (lo - nchunked);
         }
-      } else {
+      } else if (!A.perm) {
         // configurations b .. b + k1 of the item
         b = (int)it * Gcfg;
         k1 = min(Gcfg, A.B - b) - 1;
         if (rid < 0) rid = __ldg(A.robot_ids + b);
+      } else {
+        // slot sl's configurations perm[cfg_off[sl], cfg_off[sl + 1]) in
+        // groups of G: item it is group it - item_off[sl]; b is a position in perm
+        const int nrob = A.meta[1];
+        int sl = 0;
+        while (sl + 1 < nrob && __ldg(A.meta + 3 + sl) <= (int)it) ++sl;
+        rid = __ldg(A.meta + 4 + 3 * nrob + sl);
+        const int Gr = __ldg(A.meta + 4 + 2 * nrob + sl);
+        b = __ldg(A.meta + 3 + nrob + sl) + ((int)it - __ldg(A.meta + 2 + sl)) * Gr;
+        k1 = min(Gr, __ldg(A.meta + 4 + nrob + sl) - b) - 1;
       }
       // Steps (configurations) in groups of up to G = 32 / L: lanes g L +
       // link compute FK of link `link` at step g of the group, link row
@@ -691,24 +703,30 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           if (fh <= kb) break;  // this or an earlier step of the edge already hit
           if (fh - kb < 32) live &= (1u << (fh - kb)) - 1u;
         }
-        const int cb = EDGES ? 0 : b + kb;  // first configuration of the group
+        // configuration groups: position cb + i holds configuration
+        // perm[cb + i] (mixed robots) or cb + i
+        const int cb = EDGES ? 0 : b + kb;
+        const int lane_cfg = EDGES || lane >= gn ? 0 : (A.perm ? __ldg(A.perm + cb + lane) : cb + lane);
+        const int cfg0 = __shfl_sync(0xffffffffu, lane_cfg, 0);
+        if (!EDGES && lane < gn) S.item_cfg[lane] = lane_cfg;
         if (lane == 0) {
           if (EDGES) {
             S.item_qa = A.qa + (size_t)e * nl;
             S.item_qb = A.qb + (size_t)e * nl;
           } else {
-            S.item_qa = A.q + (size_t)cb * A.q_stride;
+            S.item_qa = A.q + (size_t)cfg0 * A.q_stride;
             S.item_qb = nullptr;
           }
           S.item_k = EDGES ? kb : 0;
           S.item_n = n;
-          S.item_id = EDGES ? e : cb;
+          S.item_id = EDGES ? e : cfg0;
           S.item_rid = rid;
         }
         // joint values in FP32 with an error bound e_q against the canonical
         // FP64 values (exact for configurations; FMA interpolation for edges)
         const int g = lane >> lgL, link = lane & (L - 1);
         const bool valid = ((live >> g) & 1u) && link < nl;
+        const int my_cfg = __shfl_sync(0xffffffffu, lane_cfg, g < 32 ? g : 0);  // configuration of step g
         float q = 0.f, e_q = 0.f;
         if (valid) {
           if (EDGES) {
@@ -717,7 +735,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
             q = fmaf((float)(kb + g) / (float)n, d, a);
             e_q = kU * (fabsf(d) + fabsf(q) + fabsf(a)) * 1.01f + 1e-30f;
           } else {
-            q = __ldg(A.q + (size_t)(cb + g) * A.q_stride + link);
+            q = __ldg(A.q + (size_t)my_cfg * A.q_stride + link);
           }
         }
         __syncwarp();
@@ -737,9 +755,8 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           }
           bool viol = false;
           if (unsure) {
-            const double q64 = EDGES
-                                   ? kx_interp((double)S.item_qa[link], (double)S.item_qb[link], kb + g, n)
-                                   : (double)S.item_qa[(size_t)g * A.q_stride + link];
+            const double q64 = EDGES ? kx_interp((double)S.item_qa[link], (double)S.item_qb[link], kb + g, n)
+                                     : (double)q;  // configurations are exact in FP32
             viol = q64 < R.qmin64[link] || q64 > R.qmax64[link];
           }
           const unsigned vm = __reduce_or_sync(0xffffffffu, viol ? 1u << g : 0u);
@@ -750,7 +767,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
               if (lane == 0) atomicMin(A.first_hit + e, kb + gv);
               live &= (1u << gv) - 1u;
             } else {
-              if (lane < 32 && ((vm >> lane) & 1u)) A.feasible[cb + lane] = 0;
+              if ((vm >> lane) & 1u) A.feasible[lane_cfg] = 0;
               live &= ~vm;
             }
           }
@@ -804,10 +821,10 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           }
         } else if (lane < 32) {
           if (A.mode == MODE_CONFIGS) {
-            if ((env_hits >> lane) & 1u) A.env_hit[cb + lane] = 1;
-            if ((self_hits >> lane) & 1u) A.self_hit[cb + lane] = 1;
+            if ((env_hits >> lane) & 1u) A.env_hit[lane_cfg] = 1;
+            if ((self_hits >> lane) & 1u) A.self_hit[lane_cfg] = 1;
           } else if ((any_hits >> lane) & 1u) {
-            A.feasible[cb + lane] = 0;
+            A.feasible[lane_cfg] = 0;
           }
         }
         __syncwarp();
@@ -1091,6 +1108,61 @@ __global__ void __launch_bounds__(kWarps * 32) k_band(const KWorldDev* __restric
     atomicAdd(W->stats + 3, band);
     atomicAdd(W->stats + 6, hits);
   }
+}
+
+// ---- mixed-robot configuration batches ------------------------------------
+// Configurations are counted and scattered by robot so that one robot's
+// configurations form groups of G_r = 32 / L_r (1 with the FP64 test
+// inline).  Robots with more links (costlier items) come first, so that the
+// queue ends on cheap items.  meta, per slot s (s = 0..nrob; robot of slot s
+// = rob[s]): [0] work items, [1] robots, [2 + s] first item of slot s,
+// [3 + nrob + s] first position of slot s in perm, [4 + 2 nrob + s] its G,
+// [4 + 3 nrob + s] rob[s], [4 + 4 nrob + r] slot of robot r.  The order
+// inside a robot's range depends on atomics; verdicts do not.
+__global__ void k_cfg_count(const int* robot_ids, int B, int nrob, int* counts, int* status)
+{
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int r = robot_ids[b];
+  if (r < 0 || r >= nrob) atomicCAS(status, 0, KGPU_ERR_INVALID);
+  else atomicAdd(counts + r, 1);
+}
+
+__global__ void k_cfg_offsets(const KWorldDev* __restrict__ W, const int* counts, int nrob, int single, int* fill,
+                              int* meta)
+{
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int io = 0, co = 0;
+  unsigned placed = 0;
+  for (int sl = 0; sl < nrob; ++sl) {
+    int r = -1;  // the unplaced robot with the most links (lowest index on ties)
+    for (int c = 0; c < nrob; ++c)
+      if (!((placed >> c) & 1u) && (r < 0 || W->robots[c].nlinks > W->robots[r].nlinks)) r = c;
+    placed |= 1u << r;
+    const int nl = W->robots[r].nlinks;
+    const int G = single ? 1 : (nl <= 8 ? 4 : (nl <= 16 ? 2 : 1));
+    meta[2 + sl] = io;
+    meta[3 + nrob + sl] = co;
+    meta[4 + 2 * nrob + sl] = G;
+    meta[4 + 3 * nrob + sl] = r;
+    meta[4 + 4 * nrob + r] = sl;
+    io += (counts[r] + G - 1) / G;
+    co += counts[r];
+    fill[r] = 0;
+  }
+  meta[2 + nrob] = io;
+  meta[3 + 2 * nrob] = co;
+  meta[0] = io;
+  meta[1] = nrob;
+}
+
+__global__ void k_cfg_scatter(const int* robot_ids, int B, int nrob, const int* meta, int* fill, int* perm)
+{
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= B) return;
+  const int r = robot_ids[b];
+  if (r < 0 || r >= nrob) return;
+  perm[meta[3 + nrob + meta[4 + 4 * nrob + r]] + atomicAdd(fill + r, 1)] = b;
 }
 
 // ---- edge preparation ------------------------------------------------------
@@ -1413,7 +1485,7 @@ cudaError_t launch_jacobian(const KWorldDev* W, int robot, const float* q, const
 cudaError_t launch_check_configs(const KWorldDev* W, const Scratch& S, int robot, const int* robot_ids,
                                  const float* q, int q_stride, int B, uint8_t* env_hit, uint8_t* self_hit,
                                  uint8_t* feasible, int blocks, int per_sm, cudaStream_t s, int grab,
-                                 int job_flush, int fp64_inline)
+                                 int job_flush, int fp64_inline, int nrobots, int* status)
 {
   if (B <= 0) return cudaSuccess;
   // the kernels only ever record contacts: start from "free"
@@ -1437,6 +1509,19 @@ cudaError_t launch_check_configs(const KWorldDev* W, const Scratch& S, int robot
   A.inline64 = fp64_inline == 1;  // default (-1): deferred, as for edge batches
   A.spill = S.spill;
   A.spill_per_warp = (int)S.spill_per_warp;
+  if (robot < 0 && nrobots > 0 && nrobots <= 32 && status && S.edge_perm && (size_t)B <= S.edge_cap) {
+    // mixed robots: sort by robot so that each robot's configurations go in groups
+    int* counts = S.edge_hist;
+    int* fill = S.edge_hist + 32;
+    if ((err = cudaMemsetAsync(counts, 0, 32 * sizeof(int), s)) != cudaSuccess) return err;
+    const int tb = 256, gb = (B + tb - 1) / tb;
+    k_cfg_count<<<gb, tb, 0, s>>>(robot_ids, B, nrobots, counts, status);
+    k_cfg_offsets<<<1, 32, 0, s>>>(W, counts, nrobots, A.inline64, fill, S.edge_meta);
+    k_cfg_scatter<<<gb, tb, 0, s>>>(robot_ids, B, nrobots, S.edge_meta, fill, S.edge_perm);
+    if ((err = cudaGetLastError()) != cudaSuccess) return err;
+    A.perm = S.edge_perm;
+    A.meta = S.edge_meta;
+  }
   return dispatch_engine(W, A, S, blocks, per_sm, s);
 }
 

@@ -232,6 +232,10 @@ struct kgpu_world_s {
   void* dstage = nullptr;
   size_t dstage_bytes = 0;
   cudaStream_t host_stream = nullptr;
+  // edge plans record scratch pointers: while any is alive, buffers that
+  // grow are kept (freed with the world) instead of freed
+  int live_plans = 0;
+  std::vector<void*> retired;
 };
 
 struct kgpu_edge_plan_s {
@@ -252,7 +256,8 @@ cudaError_t launch_check_configs(const KWorldDev* Wd, const Scratch& S, int robo
                                  const int* robot_ids, const float* q, int q_stride, int B,
                                  uint8_t* env_hit, uint8_t* self_hit, uint8_t* feasible,
                                  int blocks, int per_sm, cudaStream_t s, int grab = 0,
-                                 int job_flush = 0, int fp64_inline = -1);
+                                 int job_flush = 0, int fp64_inline = -1,
+                                 int nrobots = 0, int* status = nullptr);
 cudaError_t launch_check_edges(const KWorldDev* Wd, int* status, const Scratch& S, int robot,
                                const float* qa, const float* qb, const int* nsteps, int E,
                                int* first_hit, int blocks, int per_sm, cudaStream_t s,
