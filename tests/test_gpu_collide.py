@@ -201,6 +201,29 @@ def test_cfg1_edges_host_and_graph(cfg1):
     plan.close()
 
 
+def test_edge_plan_survives_scratch_growth(cfg1):
+    """An edge plan recorded for a small batch keeps working after a larger
+    edge batch and a mixed-robot batch have grown the world's scratch."""
+    import torch
+    robot, env, (qa, qb, ns), w, o = cfg1
+    small = slice(0, 100)
+    ref = w.check_edges(qa[small], qb[small], ns[small]).cpu().numpy()
+    a, b, n = (torch.as_tensor(x[small]).cuda() for x in (qa, qb, ns))
+    out = torch.empty(100, dtype=torch.int32, device="cuda")
+    plan = w.edge_plan(a, b, n, out)
+    plan.launch()
+    w.sync()
+    assert np.array_equal(out.cpu().numpy(), ref)
+    big = np.concatenate([qa] * 3), np.concatenate([qb] * 3), np.concatenate([ns] * 3)
+    fh_big = w.check_edges(*big).cpu().numpy()
+    assert np.array_equal(fh_big[:len(ns)], w.check_edges(qa, qb, ns).cpu().numpy())
+    out.fill_(-7)
+    plan.launch()
+    w.sync()
+    assert np.array_equal(out.cpu().numpy(), ref)
+    plan.close()
+
+
 def test_edges_full_batch_repeatable(built):
     """The full 16,384-edge batch (deep traversals handed between warps at
     the end of every launch) gives the oracle's first hits in each of 42
