@@ -161,17 +161,23 @@ def test_heterogeneous_batch_matches_oracle():
     launch, every configuration checked against its own robot's oracle."""
     from klampt_gb300.engine import World
     from oracle.oracle_py import Oracle
-    robots, env, (ids, q) = sc.scene_cfg3(total=1024, n_spheres=70, n_boxes=870)
+    robots, env, (ids, q) = sc.scene_cfg3(total=1023, n_spheres=70, n_boxes=870)
     w = World(env, robots)
-    eh, sh = w.check_configs_multi(ids, q)
-    eh, sh = eh.cpu().numpy(), sh.cpu().numpy()
+    ref = []
     for r, spec in enumerate(robots):
         sel = np.flatnonzero(ids == r)
-        o = Oracle(spec, env)
-        eo, so, _ = o.check_configs(q[sel, :spec.num_links], nthreads=NT)
-        assert np.array_equal(eh[sel], eo), r
-        assert np.array_equal(sh[sel], so), r
-    assert 0 < eh.mean() < 1 and 0 < sh.mean() < 1
+        eo, so, _ = Oracle(spec, env).check_configs(q[sel, :spec.num_links], nthreads=NT)
+        ref.append((sel, eo, so))
+    # configurations sorted by robot into per-robot groups (FP64 deferred)
+    # and one configuration per item (FP64 inline)
+    for fp64_inline in (0, 1):
+        w.set_option("fp64_inline", fp64_inline)
+        eh, sh = w.check_configs_multi(ids, q)
+        eh, sh = eh.cpu().numpy(), sh.cpu().numpy()
+        for r, (sel, eo, so) in enumerate(ref):
+            assert np.array_equal(eh[sel], eo), (fp64_inline, r)
+            assert np.array_equal(sh[sel], so), (fp64_inline, r)
+        assert 0 < eh.mean() < 1 and 0 < sh.mean() < 1
     w.close()
 
 
