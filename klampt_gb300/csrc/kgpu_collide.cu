@@ -624,12 +624,13 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
   __syncthreads();
   // configurations of one robot go in groups of G = 32 / L (L = its link
   // count rounded up to 8, 16 or 32) per work item in the main pass; mixed
-  // robots and the FP64 pass take one configuration per item
+  // robots sorted by robot (A.perm set) in groups of their robot's G, mixed
+  // robots otherwise and the FP64 pass one configuration per item
   const int lgC = EDGES || FP64 || A.robot < 0
                       ? 5
                       : (W->robots[A.robot].nlinks <= 8 ? 3 : (W->robots[A.robot].nlinks <= 16 ? 4 : 5));
   const int Gcfg = 32 >> lgC;
-  // mixed robots sorted by robot (A.perm set): per-robot groups, see k_cfg_offsets
+  // (k_cfg_offsets counts the items of the sorted order)
   const int total = EDGES ? A.meta[1] : (A.perm ? A.meta[0] : (A.B + Gcfg - 1) / Gcfg);
   const int maxn = EDGES ? A.meta[0] : 0;  // last round index
   const int grab = A.grab >= 1 && A.grab <= 16 ? A.grab : kGrab;
