@@ -359,15 +359,16 @@ def main():
     b = torch.as_tensor(qb).cuda()
     n = torch.as_tensor(ns).cuda()
     tuned = None
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     if not args.engine_only:
         from klampt_gb300 import autotune
         # tuned on a separately seeded batch of the same size and distribution
-        # (the timed edges are not used for tuning)
+        # (the timed edges are not used for tuning), with the same L2 flush
+        # before each repetition as before each timed step
         ta, tb, tn = sc.random_edges(robot, args.edges, np.random.default_rng(2001))
-        tuned, _ = autotune.tune_edges(w, ta, tb, tn, reps=3)
+        tuned, _ = autotune.tune_edges(w, ta, tb, tn, reps=3, prep=flush.zero_)
     out = torch.empty(args.edges, dtype=torch.int32, device="cuda")
     plan = w.edge_plan(a, b, n, out)
-    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     stream = torch.cuda.current_stream()
 
     for _ in range(args.warmup if args.engine_only else max(3, args.warmup)):

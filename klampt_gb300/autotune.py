@@ -10,15 +10,16 @@ and, for configuration batches,
                             or inline in the traversal)
 or, for edge batches (FP64 tests always deferred there),
   edge_chunk     8, 16, 32 (consecutive steps of an edge per work item)
-times each with CUDA events (median of `reps` after one warm-up) and leaves
-the fastest setting in the world.  Results are identical for every setting; only
+times each with CUDA events (median of `reps` after one warm-up), re-times
+the few fastest with more repetitions and leaves the fastest setting in the
+world.  Results are identical for every setting; only
 the time changes.
 """
 
 from __future__ import annotations
 
 import itertools
-from typing import Callable, Dict, List, Tuple
+from typing import Callable, Dict, List, Optional, Tuple
 
 import torch
 
@@ -29,11 +30,13 @@ GRID = dict(_BASE, fp64_inline=(0, 1))
 GRID_EDGES = dict(_BASE, fp64_inline=(0,), edge_chunk=(8, 16, 32))
 
 
-def _time(fn: Callable[[], None], reps: int) -> float:
+def _time(fn: Callable[[], None], reps: int, prep: Optional[Callable[[], None]] = None) -> float:
     fn()
     torch.cuda.synchronize()
     times = []
     for _ in range(reps):
+        if prep is not None:
+            prep()  # outside the timed region (e.g. an L2 flush)
         s = torch.cuda.Event(enable_timing=True)
         e = torch.cuda.Event(enable_timing=True)
         s.record()
@@ -45,28 +48,39 @@ def _time(fn: Callable[[], None], reps: int) -> float:
 
 
 def tune(world: World, run: Callable[[], None], reps: int = 3,
-         grid: Dict[str, tuple] = GRID) -> Tuple[Dict[str, int], List[Tuple[Dict[str, int], float]]]:
+         grid: Dict[str, tuple] = GRID, prep: Optional[Callable[[], None]] = None,
+         finalists: int = 4, final_reps: int = 9) -> Tuple[Dict[str, int], List[Tuple[Dict[str, int], float]]]:
     """Times `run` (a closure launching the workload on `world`) under every
-    setting of `grid`; applies and returns the best plus the full table (ms)."""
-    table = []
-    keys = list(grid)
-    for values in itertools.product(*(grid[k] for k in keys)):
-        cfg = dict(zip(keys, values))
+    setting of `grid` (median of `reps`; `prep` runs before each repetition,
+    untimed), re-times the `finalists` fastest with `final_reps` repetitions
+    so that one noisy sample does not decide, applies and returns the best
+    plus the full table (ms)."""
+    def timed(cfg):
         for k, v in cfg.items():
             world.set_option(k, v)
-        table.append((cfg, _time(run, reps)))
-    best = min(table, key=lambda x: x[1])[0]
+        return _time(run, reps, prep)
+
+    keys = list(grid)
+    table = [(cfg, timed(cfg)) for cfg in (dict(zip(keys, values))
+                                           for values in itertools.product(*(grid[k] for k in keys)))]
+    final = []
+    for cfg, _ in sorted(table, key=lambda x: x[1])[:max(1, finalists)]:
+        for k, v in cfg.items():
+            world.set_option(k, v)
+        final.append((cfg, _time(run, final_reps, prep)))
+    best = min(final, key=lambda x: x[1])[0]
     for k, v in best.items():
         world.set_option(k, v)
     world.sync()
     return best, table
 
 
-def tune_edges(world: World, qa, qb, nsteps, robot: int = 0, reps: int = 3):
+def tune_edges(world: World, qa, qb, nsteps, robot: int = 0, reps: int = 3,
+               prep: Optional[Callable[[], None]] = None):
     a = torch.as_tensor(qa).cuda()
     b = torch.as_tensor(qb).cuda()
     n = torch.as_tensor(nsteps).cuda()
-    return tune(world, lambda: world.check_edges(a, b, n, robot=robot, sync=False), reps, GRID_EDGES)
+    return tune(world, lambda: world.check_edges(a, b, n, robot=robot, sync=False), reps, GRID_EDGES, prep)
 
 
 def tune_configs(world: World, q, robot: int = 0, reps: int = 3):
