@@ -49,7 +49,7 @@ constexpr int kGrab = 2;  // items taken from the queue per atomic
 constexpr int kWarps = 8; // warps per block
 constexpr int kMaxChunk = 64;  // most consecutive edge steps per work item
 constexpr int kDefaultChunk = 16;
-constexpr int kTailItemsPerWarp = 16;  // single-step rounds once fewer items than this per warp remain
+constexpr int kTailItemsPerWarp = 2;  // single-step rounds once fewer items than this per warp remain
 
 enum Mode { MODE_CONFIGS = 0, MODE_FEASIBLE = 1, MODE_EDGES = 2 };
 
