@@ -294,6 +294,18 @@ kgpu_status kgpu_distance(kgpu_world world, int32_t robot, const float* q, int32
                           double cutoff, double* d, int32_t* pair, double* cp, float* grad,
                           kgpu_stream stream);
 
+/* Minimum distance between the robot's own links over its enabled self pairs,
+ * clamped at `cutoff`, with its gradient d/dq: the link-link part of
+ * WorldPlannerSettings::DistanceLowerBound when a robot is checked against
+ * itself (PlannerSettings.cpp:385-395) and of geometry_ad.MinDistance over
+ * link geometries.  d(i, j) = exact minimum triangle distance (0 when the
+ * surfaces meet); d: [B] = min over enabled pairs i < j, ties to the smallest
+ * (i, j) (cutoff when nothing is closer); pair: [B*2] (i, j) or (-1,-1); cp:
+ * [B*6] closest points in world frame (link i side, link j side; 0 when
+ * d = 0); grad: [B*num_links] (may be NULL; 0 when d = 0). */
+kgpu_status kgpu_self_distance(kgpu_world world, int32_t robot, const float* q, int32_t B, double cutoff,
+                               double* d, int32_t* pair, double* cp, float* grad, kgpu_stream stream);
+
 /* Soft-min over all (waypoint, link, object) pairs of a trajectory of the
  * signed distance, L = -tau * log sum exp(-d/tau), and dL/dq by the adjoint
  * kernel.  Replaces geometry_ad.MinDistance + pytorch.ADModule backward

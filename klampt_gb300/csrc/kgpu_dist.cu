@@ -969,6 +969,374 @@ __global__ void k_softmin_final(const double* wsum, const double* m, int T, int 
   }
 }
 
+// ---- self distance ----------------------------------------------------------
+// Minimum distance between the robot's own links over its enabled self pairs
+// (the link-link part of WorldPlannerSettings::DistanceLowerBound when a
+// robot is checked against itself, Cpp/Planning/PlannerSettings.cpp:385-395,
+// and of geometry_ad.MinDistance over link geometries).  Definition (the FP64
+// oracle's, bit for bit on the value and the closest points):
+//   d(i, j) = sqrt of the minimum canonical triangle distance (kx_tri_tri_dist2)
+//             over the pair's triangles, ties to the smallest (triangle of i,
+//             triangle of j) in mesh order; 0 when the surfaces meet;
+//   d      = min over enabled pairs i < j with d(i, j) < cutoff; pairs are
+//            visited in (i, j) order and a pair replaces the best so far
+//            only if its squared minimum is below the square of the best
+//            distance and its distance is strictly smaller (equal distances
+//            keep the earlier pair, even when the squares differ in the last
+//            bit); none: d = cutoff and pair (-1, -1).
+// Gradient: dd/dq_k = u . (dcp/dq_k - dcq/dq_k), u = (cp - cq) / d at the
+// closest points cp on link i and cq on link j (0 when d = 0), from FP64
+// transforms.  One warp per configuration: FP32 traversal of each pair with
+// conservative pruning against the running upper bound of the minimum,
+// triangle pairs within the error band finalised in canonical FP64.
+constexpr int kSDStack = 512;
+constexpr int kSDJobs = 64;
+constexpr int kSDCand = 128;
+
+struct __align__(16) SelfDistSmem {
+  float T[kMaxLinks][12];
+  float delta[kMaxLinks];
+  double T64[kMaxLinks][12];
+  double q64[kMaxLinks];
+  uint2 stack[kSDStack];
+  uint32_t jobA[kSDJobs], jobB[kSDJobs], jobOff[kSDJobs + 1];
+  uint32_t candA[kSDCand], candB[kSDCand];
+  float candD[kSDCand];
+  double b2, bcp[3], bcq[3];  // best over the pairs so far: squared distance, closest points
+  double bd;                   // its distance (the cutoff before any pair is found)
+  int bi, bj;
+  double pb2, pcp[3], pcq[3];  // best of the current pair (pb2 starts at the acceptance bound)
+  int pA, pB, phave;
+};
+
+struct SelfDistArgs {
+  int robot;
+  const float* q;
+  int B;
+  double cutoff;
+  double* d;       // [B]
+  int* pair;       // [B, 2]
+  double* cp;      // [B, 6] (point on link i, point on link j)
+  float* grad;     // [B, L] or null
+};
+
+// FP64 finalisation of candidates of pair (i, j), merged into the pair's
+// best: the lexicographic minimum (squared distance, triangle of i, triangle
+// of j) over the triangle pairs whose squared distance is below the pair's
+// acceptance bound (the square of the best distance of the earlier pairs)
+__device__ __noinline__ void sd_flush(SelfDistSmem& S, const KWorldDev* __restrict__ W, int lane, int i, int j,
+                                      int ncand, float lim)
+{
+  for (int base = 0; base < ncand; base += 32) {
+    const int k = base + lane;
+    double d2 = DBL_MAX;
+    int oa = INT_MAX, ob = INT_MAX;
+    double cp[3] = {0, 0, 0}, cq[3] = {0, 0, 0};
+    if (k < ncand && S.candD[k] <= lim) {
+      const int tA = (int)S.candA[k], tB = (int)S.candB[k];
+      double P[9], Q[9];
+      const double* pa = W->ltri64 + 9 * (size_t)tA;
+      const double* pb = W->ltri64 + 9 * (size_t)tB;
+      for (int v = 0; v < 3; ++v) {
+        kx_xform_point(S.T64[i], pa + 3 * v, P + 3 * v);
+        kx_xform_point(S.T64[j], pb + 3 * v, Q + 3 * v);
+      }
+      d2 = kx_tri_tri_dist2(P, Q, cp, cq);
+      oa = W->ltri_orig[tA];
+      ob = W->ltri_orig[tB];
+    }
+    int src;
+    double m2 = d2;
+    int ma = oa, mb = ob;
+    warp_lexmin(m2, ma, mb, src, lane);
+    // below the acceptance bound, or equal to the pair's best with smaller
+    // triangles
+    const bool better = S.phave ? (m2 < S.pb2 || (m2 == S.pb2 && (ma < S.pA || (ma == S.pA && mb < S.pB))))
+                                : m2 < S.pb2;
+    __syncwarp();
+    if (m2 < DBL_MAX && better && lane == src) {
+      S.pb2 = d2;
+      S.pA = oa;
+      S.pB = ob;
+      S.phave = 1;
+      for (int c = 0; c < 3; ++c) { S.pcp[c] = cp[c]; S.pcq[c] = cq[c]; }
+    }
+    __syncwarp();
+  }
+}
+
+__global__ void __launch_bounds__(kDW * 32, 1) k_self_dist(const KWorldDev* __restrict__ W, const SelfDistArgs A)
+{
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  SelfDistSmem& S = reinterpret_cast<SelfDistSmem*>(smem_raw)[warp];
+  const unsigned lt = lanemask_lt();
+  const KRobotDev& R = W->robots[A.robot];
+  const int nl = R.nlinks;
+  const float fcut = A.cutoff < 1e30 ? (float)A.cutoff * 1.000001f + 1e-7f : FLT_MAX;
+  const int nwarps = gridDim.x * kDW;
+#pragma unroll 1
+  for (int b = blockIdx.x * kDW + warp; b < A.B; b += nwarps) {
+    const float qv = lane < nl ? __ldg(A.q + (size_t)b * nl + lane) : 0.f;
+    if (__any_sync(0xffffffffu, lane < nl && !(fabsf(qv) < 1.0e6f))) {
+      if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
+      continue;
+    }
+    float P32[12], delta;
+    warp_fk32(R, lane, qv, 0.f, P32, &delta);
+    if (lane < nl) {
+#pragma unroll
+      for (int k = 0; k < 12; ++k) S.T[lane][k] = P32[k];
+      S.delta[lane] = delta + W->eps_extra;
+      S.q64[lane] = (double)qv;
+    }
+    if (lane == 0) {
+      S.b2 = DBL_MAX;
+      S.bd = A.cutoff;
+      S.bi = S.bj = -1;
+    }
+    __syncwarp();
+    warp_fk64(R, S.q64, S.T64, lane);
+    float m32 = fcut;  // upper bound on the minimum so far (warp-uniform)
+    bool contact = false;
+#pragma unroll 1
+    for (int qi = 0; qi < R.nqueries_self && !contact; ++qi) {
+      const uint32_t qw = __ldg(W->queries + R.query_off + R.nqueries_env + qi);
+      const int i = qw & 0xff, j = (qw >> 8) & 0xff;
+      if (R.link_root[i] < 0 || R.link_root[j] < 0) continue;
+      const float* TA = S.T[i];
+      const float* TB = S.T[j];
+      const float dd = S.delta[i] + S.delta[j];
+      int top = 1, njobs = 0, ncand = 0;
+      if (lane == 0) {
+        S.stack[0] = make_uint2((uint32_t)R.link_root[i], (uint32_t)R.link_root[j]);
+        const double bb = kx_mul(S.bd, S.bd);
+        S.pb2 = bb > 1e-300 ? bb : 1e-300;
+        S.pA = S.pB = INT_MAX;
+        S.phave = 0;
+      }
+      __syncwarp();
+#pragma unroll 1
+      while ((top > 0 || njobs > 0) && !contact) {
+        if (njobs >= 16 || (top == 0 && njobs > 0)) {
+          // ---- triangle pairs, one per lane
+          uint32_t carry = 0;
+          for (int bb = 0; bb < njobs; bb += 32) {
+            const int jj = bb + lane;
+            uint32_t c = 0;
+            if (jj < njobs) c = ((S.jobA[jj] >> 28) + 1) * ((S.jobB[jj] >> 28) + 1);
+            uint32_t incl = c;
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+              const uint32_t v = __shfl_up_sync(0xffffffffu, incl, off);
+              if (lane >= off) incl += v;
+            }
+            if (jj < njobs) S.jobOff[jj] = carry + incl - c;
+            carry += __shfl_sync(0xffffffffu, incl, 31);
+          }
+          __syncwarp();
+          const uint32_t total = carry;
+#pragma unroll 1
+          for (uint32_t base = 0; base < total; base += 32) {
+            const uint32_t p = base + lane;
+            float d32 = FLT_MAX, e = 0.f;
+            int tA = 0, tB = 0;
+            bool certain = false;
+            if (p < total) {
+              int lo = 0, hi = njobs - 1;
+              while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (S.jobOff[mid] <= p) lo = mid; else hi = mid - 1;
+              }
+              const uint32_t r = p - S.jobOff[lo];
+              const uint32_t cb = (S.jobB[lo] >> 28) + 1;
+              tA = (int)(S.jobA[lo] & 0x0fffffffu) + (int)(r / cb);
+              tB = (int)(S.jobB[lo] & 0x0fffffffu) + (int)(r % cb);
+              float3 P[3], Q[3];
+#pragma unroll
+              for (int v = 0; v < 3; ++v) {
+                const float4 x = __ldg(W->ltri32 + 3 * (size_t)tA + v);
+                P[v] = xform32(TA, make_float3(x.x, x.y, x.z));
+                const float4 y = __ldg(W->ltri32 + 3 * (size_t)tB + v);
+                Q[v] = xform32(TB, make_float3(y.x, y.y, y.z));
+              }
+              float3 lo3 = P[0], hi3 = P[0];
+#pragma unroll
+              for (int k = 1; k < 6; ++k) {
+                const float3 v = k < 3 ? P[k] : Q[k - 3];
+                lo3 = make_float3(fminf(lo3.x, v.x), fminf(lo3.y, v.y), fminf(lo3.z, v.z));
+                hi3 = make_float3(fmaxf(hi3.x, v.x), fmaxf(hi3.y, v.y), fmaxf(hi3.z, v.z));
+              }
+              const float span = fmaxf(fmaxf(hi3.x - lo3.x, hi3.y - lo3.y), hi3.z - lo3.z);
+              e = dd + 128.f * kU * span + 1e-8f;
+              if (tri_axis_lb32(P, Q, span) - e > m32 * (1.f + 2e-5f) + 2.f * e) {
+                d32 = FLT_MAX;  // cannot be a candidate
+              } else if (!tri_separated32(P, Q, dd, 0.f)) {
+                d32 = 0.f;
+                certain = tri_certain_hit32(P[0], P[1], P[2], Q[0], Q[1], Q[2], dd);
+              } else {
+                d32 = sqrtf(tri_dist2_32(P, Q));
+              }
+            }
+            if (__any_sync(0xffffffffu, certain)) {
+              contact = true;  // distance 0: no later pair can be smaller
+              if (lane == 0) {
+                S.b2 = 0.0;
+                S.bd = 0.0;
+                S.bi = i;
+                S.bj = j;
+              }
+              __syncwarp();
+              break;
+            }
+            m32 = fminf(m32, warp_min(d32 < FLT_MAX ? d32 + e : FLT_MAX));
+            const bool cand = d32 < FLT_MAX && d32 - e <= m32 * (1.f + 2e-5f);
+            const unsigned mc = __ballot_sync(0xffffffffu, cand);
+            if (ncand + __popc(mc) > kSDCand) {
+              sd_flush(S, W, lane, i, j, ncand, m32 * (1.f + 2e-5f) + 1e-6f);
+              ncand = 0;
+              if (S.phave) m32 = fminf(m32, (float)sqrt(S.pb2) * (1.f + 1e-6f));
+            }
+            if (cand) {
+              const int rr = ncand + __popc(mc & lt);
+              S.candA[rr] = (uint32_t)tA;
+              S.candB[rr] = (uint32_t)tB;
+              S.candD[rr] = d32 - e;
+            }
+            ncand += __popc(mc);
+            __syncwarp();
+          }
+          njobs = 0;
+          continue;
+        }
+        // ---- node pairs; near the stack capacity the batch narrows to
+        // depth-first order, whose growth is bounded by the trees' depth
+        const int n = min(min(top, 32), max(1, kSDStack - 64 - top));
+        const bool have = lane < n;
+        uint2 en = make_uint2(0, 0);
+        if (have) en = S.stack[top - 1 - lane];
+        __syncwarp();
+        top -= n;
+        int outcome = 0;
+        uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
+        uint32_t jA = 0, jB = 0;
+        if (have) {
+          const int nodeA = (int)en.x, nodeB = (int)en.y;
+          const KNode na = W->lnodes[nodeA];
+          const KNode nb = W->lnodes[nodeB];
+          const Box32 BA = xform_box(TA, na.a, na.b);
+          const Box32 BB = xform_box(TB, nb.a, nb.b);
+          const float slack = 4.f * kU * (fabsf(BA.c.x) + fabsf(BA.c.y) + fabsf(BA.c.z) + fabsf(BB.c.x) +
+                                          fabsf(BB.c.y) + fabsf(BB.c.z) + 1.f);
+          const float lb_box = box_dist32(BA, BB.c, BB.h) - dd * 1.7321f - slack;
+          const float cx = BA.c.x - BB.c.x, cy = BA.c.y - BB.c.y, cz = BA.c.z - BB.c.z;
+          const float lb_sph = sqrtf(cx * cx + cy * cy + cz * cz) * (1.f - 4.f * kU) - __ldg(W->lnode_r + nodeA) -
+                               __ldg(W->lnode_r + nodeB) - dd * 1.7321f - slack;
+          const float lb = fmaxf(lb_box, lb_sph);
+          if (lb <= m32 * (1.f + 2e-5f) + 3.f * dd + 1e-5f) {
+            const int cntA = f2i(na.b.w), cntB = f2i(nb.b.w);
+            const int ia = f2i(na.a.w), ib = f2i(nb.a.w);
+            if (cntA > 0 && cntB > 0) {
+              outcome = 2;
+              jA = (uint32_t)ia | ((uint32_t)(cntA - 1) << 28);
+              jB = (uint32_t)ib | ((uint32_t)(cntB - 1) << 28);
+            } else {
+              outcome = 1;
+              const bool splitB = cntA > 0 || (cntB == 0 && (nb.b.x + nb.b.y + nb.b.z) > (na.b.x + na.b.y + na.b.z));
+              if (splitB) { c0 = make_uint2((uint32_t)nodeA, (uint32_t)ib); c1 = make_uint2((uint32_t)nodeA, (uint32_t)ib + 1); }
+              else { c0 = make_uint2((uint32_t)ia, (uint32_t)nodeB); c1 = make_uint2((uint32_t)ia + 1, (uint32_t)nodeB); }
+            }
+          }
+        }
+        const unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
+        const unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
+        if (top + 2 * __popc(m1) > kSDStack) {
+          // cannot happen with the narrowing above (growth bounded by the
+          // trees' depth); checked so that an error is reported, not hidden
+          if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
+          top = 0;
+          njobs = 0;
+          ncand = 0;
+          break;
+        }
+        if (outcome == 1) {
+          const int rr = top + 2 * __popc(m1 & lt);
+          S.stack[rr] = c1;
+          S.stack[rr + 1] = c0;
+        } else if (outcome == 2) {
+          const int rr = njobs + __popc(m2 & lt);
+          S.jobA[rr] = jA;
+          S.jobB[rr] = jB;
+        }
+        top += 2 * __popc(m1);
+        njobs += __popc(m2);
+        __syncwarp();
+      }
+      if (!contact && ncand > 0) {
+        sd_flush(S, W, lane, i, j, ncand, m32 * (1.f + 2e-5f) + 1e-6f);
+        if (S.phave) m32 = fminf(m32, (float)sqrt(S.pb2) * (1.f + 1e-6f));
+      }
+      // the pair replaces the best only with a strictly smaller distance
+      if (!contact && S.phave) {
+        const double dp = kx_sqrt(S.pb2);
+        if (dp < S.bd) {
+          __syncwarp();
+          if (lane == 0) {
+            S.b2 = S.pb2;
+            S.bd = dp;
+            S.bi = i;
+            S.bj = j;
+            for (int c = 0; c < 3; ++c) { S.bcp[c] = S.pcp[c]; S.bcq[c] = S.pcq[c]; }
+          }
+        }
+      }
+      __syncwarp();
+      if (S.b2 == 0.0) contact = true;
+    }
+    // ---- outputs and the gradient (FP64 transforms)
+    const bool found = S.b2 < DBL_MAX;
+    const double d = found ? kx_sqrt(S.b2) : A.cutoff;
+    if (lane == 0) {
+      A.d[b] = d;
+      A.pair[2 * (size_t)b] = found ? S.bi : -1;
+      A.pair[2 * (size_t)b + 1] = found ? S.bj : -1;
+    }
+    if (lane < 6) A.cp[6 * (size_t)b + lane] = found && d > 0.0 ? (lane < 3 ? S.bcp[lane] : S.bcq[lane - 3]) : 0.0;
+    if (A.grad && lane < nl) {
+      double g = 0.0;
+      if (found && d > 0.0 && R.jtype[lane] != KX_JOINT_WELD) {
+        double u[3];
+        for (int c = 0; c < 3; ++c) u[c] = (S.bcp[c] - S.bcq[c]) / d;
+        const double* Tk = S.T64[lane];
+        double w[3];
+        for (int r = 0; r < 3; ++r) w[r] = Tk[3 * r] * R.axis64[lane][0] + Tk[3 * r + 1] * R.axis64[lane][1] +
+                                          Tk[3 * r + 2] * R.axis64[lane][2];
+        for (int side = 0; side < 2; ++side) {
+          const int link = side == 0 ? S.bi : S.bj;
+          bool anc = false;
+          for (int a = link; a >= 0; a = R.parents[a])
+            if (a == lane) { anc = true; break; }
+          if (!anc) continue;
+          const double* x = side == 0 ? S.bcp : S.bcq;
+          double v[3];
+          if (R.jtype[lane] == KX_JOINT_REVOLUTE) {
+            const double rx = x[0] - Tk[9], ry = x[1] - Tk[10], rz = x[2] - Tk[11];
+            v[0] = w[1] * rz - w[2] * ry;
+            v[1] = w[2] * rx - w[0] * rz;
+            v[2] = w[0] * ry - w[1] * rx;
+          } else {
+            v[0] = w[0]; v[1] = w[1]; v[2] = w[2];
+          }
+          const double t = u[0] * v[0] + u[1] * v[1] + u[2] * v[2];
+          g += side == 0 ? t : -t;
+        }
+      }
+      A.grad[(size_t)b * nl + lane] = (float)g;
+    }
+    __syncwarp();
+  }
+}
+
 }  // namespace
 
 cudaError_t dist_init()
@@ -1032,6 +1400,35 @@ cudaError_t launch_softmin(const KWorldDev* Wd, const Scratch& S, int robot, con
   A.head = S.counters + 9;
   k_dist<<<num_sms * 2, kDW * 32, sizeof(DistSmem) * kDW, s>>>(Wd, A);
   k_softmin_final<<<(T + 127) / 128, 128, 0, s>>>(wsum, mt, T, Wn, nl, tau, L, dLdq);
+  return cudaGetLastError();
+}
+
+}  // namespace kgpu
+
+namespace kgpu {
+
+cudaError_t launch_self_distance(const KWorldDev* Wd, int robot, const float* q, int B, double cutoff, double* d,
+                                 int* pair, double* cp, float* grad, int num_sms, cudaStream_t s)
+{
+  if (B <= 0) return cudaSuccess;
+  static bool attr = false;
+  const size_t smem = sizeof(SelfDistSmem) * kDW;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(k_self_dist, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  SelfDistArgs A;
+  A.robot = robot;
+  A.q = q;
+  A.B = B;
+  A.cutoff = cutoff;
+  A.d = d;
+  A.pair = pair;
+  A.cp = cp;
+  A.grad = grad;
+  const int blocks = min((B + kDW - 1) / kDW, 4 * num_sms);
+  k_self_dist<<<blocks, kDW * 32, smem, s>>>(Wd, A);
   return cudaGetLastError();
 }
 

@@ -267,6 +267,22 @@ class World:
             self.sync()
         return d, pair, cp, g
 
+    def self_distance(self, q, cutoff: float, robot: int = 0, want_grad: bool = True, sync: bool = True):
+        """Minimum distance between the robot's own links over its enabled self
+        pairs: (d [B], pair [B, 2] (i, j), cp [B, 6], grad [B, L] or None)."""
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L).contiguous()
+        B = qd.shape[0]
+        d = torch.empty(B, dtype=torch.float64, device="cuda")
+        pair = torch.empty((B, 2), dtype=torch.int32, device="cuda")
+        cp = torch.empty((B, 6), dtype=torch.float64, device="cuda")
+        g = torch.empty((B, L), dtype=torch.float32, device="cuda") if want_grad else None
+        check(lib().kgpu_self_distance(self.handle, robot, _dptr(qd), B, float(cutoff), _dptr(d), _dptr(pair),
+                                       _dptr(cp), _dptr(g), _stream()))
+        if sync:
+            self.sync()
+        return d, pair, cp, g
+
     def softmin(self, q, tau: float, robot: int = 0, want_grad: bool = True, sync: bool = True):
         L = self.robots[robot].num_links
         qd = _dev(q, torch.float32)

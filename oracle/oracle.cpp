@@ -529,6 +529,84 @@ void feature_gradient(const Ctx& c, int l, const double* p, const double* u, dou
   }
 }
 
+// distance between links i and j of the robot (both in the world frame):
+// min over triangle pairs of kx_tri_tri_dist2, ties to the smallest
+// (triangle of i, triangle of j) in mesh order; only distances strictly
+// below `bound` are found.  No signed part: 0 when the surfaces meet.
+PairResult self_pair_distance(Ctx& c, int i, int j, double bound)
+{
+  const Robot& R = *c.R;
+  PairResult res;
+  res.found = 0;
+  res.d = bound;
+  res.signed_pen = 0;
+  res.ta = res.tb = -1;
+  const Bvh& A = R.bvh[i];
+  const Bvh& B = R.bvh[j];
+  if (A.empty() || B.empty()) return res;
+  double ub = bound > 0 ? bound : 0.0;
+  double best2 = ub * ub > 1e-300 ? ub * ub : 1e-300;
+  int bta = -1, btb = -1;
+  double bcp[3] = {0, 0, 0}, bcq[3] = {0, 0, 0};
+  bool have = false;
+  std::vector<std::pair<int, int>> st;
+  st.push_back({0, 0});
+  while (!st.empty()) {
+    auto pr = st.back();
+    st.pop_back();
+    const Node& na = A.nodes[pr.first];
+    const Node& nb = B.nodes[pr.second];
+    double ca[3], ha[3], cb[3], hb[3];
+    xform_box(c.T[i], na, ca, ha);
+    xform_box(c.T[j], nb, cb, hb);
+    double lb2 = 0.0;
+    for (int k = 0; k < 3; ++k) {
+      double g = fabs(ca[k] - cb[k]) - ha[k] - hb[k];
+      if (g > 0) lb2 += g * g;
+    }
+    c.cnt.node_pairs++;
+    if (have ? lb2 > best2 * (1 + 1e-9) + 1e-24 : lb2 >= best2 * (1 + 1e-9) + 1e-24) continue;
+    bool la_leaf = na.left < 0, lb_leaf = nb.left < 0;
+    if (la_leaf && lb_leaf) {
+      for (int x = 0; x < na.count; ++x) {
+        int ta = A.order[na.first + x];
+        const double* P = c.link_tri(i, ta);
+        for (int y = 0; y < nb.count; ++y) {
+          int tb = B.order[nb.first + y];
+          c.cnt.tri_pairs++;
+          double cp[3], cq[3];
+          double d2 = kx_tri_tri_dist2(P, c.link_tri(j, tb), cp, cq);
+          bool better = have ? (d2 < best2 || (d2 == best2 && (ta < bta || (ta == bta && tb < btb))))
+                             : (d2 < best2);
+          if (better) {
+            have = true;
+            best2 = d2;
+            bta = ta; btb = tb;
+            std::memcpy(bcp, cp, sizeof bcp);
+            std::memcpy(bcq, cq, sizeof bcq);
+          }
+        }
+      }
+    } else if (la_leaf || (!lb_leaf && node_size(nb) > node_size(na))) {
+      st.push_back({pr.first, nb.left + 1});
+      st.push_back({pr.first, nb.left});
+    } else {
+      st.push_back({na.left + 1, pr.second});
+      st.push_back({na.left, pr.second});
+    }
+  }
+  if (!have) return res;
+  double d = kx_sqrt(best2);
+  if (!(d < bound)) return res;
+  res.found = 1;
+  res.d = d;
+  res.ta = bta;
+  res.tb = btb;
+  std::memcpy(res.cp, bcp, sizeof bcp);
+  std::memcpy(res.cq, bcq, sizeof bcq);
+  return res;
+}
+
 bool pair_enabled(const Ctx& c, int l, int o)
 {
   return ((c.masks[l] >> c.E->groups[o]) & 1u) && !c.R->tloc[l].empty();
@@ -1191,6 +1269,64 @@ int orc_indep_pairs(void* robot, void* env, const float* q, int B, const unsigne
   });
   for (auto& m : part)
     for (int i = 0; i < L; ++i) mask[i] |= m[i];
+  return 0;
+}
+
+/* Minimum distance between the robot's own links over its enabled self
+   pairs: the link-link part of WorldPlannerSettings::DistanceLowerBound when
+   a robot is checked against itself (Cpp/Planning/PlannerSettings.cpp:
+   385-395).  d = min over enabled pairs i < j of self_pair_distance, pairs
+   below `cutoff` only, ties to the smallest (i, j); none: d = cutoff, pair
+   (-1, -1).  cp = (point on i, point on j), 0 when none or d = 0; grad[L]
+   (may be null) = u . (dcp/dq - dcq/dq), u = (cp - cq) / d, 0 when d = 0. */
+int orc_self_distance(void* robot, void* env, const float* q, int B, double cutoff, double* d, int* pair,
+                      double* cp, double* grad, int nthreads)
+{
+  Robot* R = (Robot*)robot;
+  Env* E = (Env*)env;
+  const int L = R->L;
+  parallel_for(B, nthreads, [&](int, int b0, int b1) {
+    Ctx c;
+    std::vector<uint32_t> masks(L, 0u);
+    c.init(R, E, masks.data());
+    std::vector<double> qd(L);
+    for (int b = b0; b < b1; ++b) {
+      for (int i = 0; i < L; ++i) qd[i] = (double)q[(size_t)b * L + i];
+      c.set_config(qd.data());
+      double best = cutoff;
+      int bi = -1, bj = -1;
+      double bcp[3] = {0, 0, 0}, bcq[3] = {0, 0, 0};
+      for (int i = 0; i < L && best > 0.0; ++i)
+        for (int j = i + 1; j < L && best > 0.0; ++j) {
+          if (!R->self_mask[i * L + j] || R->tloc[i].empty() || R->tloc[j].empty()) continue;
+          PairResult pr = self_pair_distance(c, i, j, best);
+          if (!pr.found) continue;
+          best = pr.d;
+          bi = i;
+          bj = j;
+          std::memcpy(bcp, pr.cp, sizeof bcp);
+          std::memcpy(bcq, pr.cq, sizeof bcq);
+        }
+      d[b] = best;
+      pair[2 * (size_t)b] = bi;
+      pair[2 * (size_t)b + 1] = bj;
+      const bool pos = bi >= 0 && best > 0.0;
+      for (int k = 0; k < 3; ++k) {
+        cp[6 * (size_t)b + k] = pos ? bcp[k] : 0.0;
+        cp[6 * (size_t)b + 3 + k] = pos ? bcq[k] : 0.0;
+      }
+      if (grad) {
+        double* g = grad + (size_t)b * L;
+        for (int k = 0; k < L; ++k) g[k] = 0.0;
+        if (pos) {
+          double u[3];
+          for (int k = 0; k < 3; ++k) u[k] = (bcp[k] - bcq[k]) / best;
+          feature_gradient(c, bi, bcp, u, 1.0, g);
+          feature_gradient(c, bj, bcq, u, -1.0, g);
+        }
+      }
+    }
+  });
   return 0;
 }
 

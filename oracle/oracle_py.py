@@ -41,7 +41,7 @@ def lib():
         L.orc_env_create.restype = P
         for name in ("orc_check_configs", "orc_check_edges", "orc_is_feasible", "orc_pair_distance",
                      "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian", "orc_self_pairs", "orc_ik",
-                     "orc_indep_pairs"):
+                     "orc_indep_pairs", "orc_self_distance"):
             getattr(L, name).restype = ctypes.c_int
         L.orc_robot_destroy.argtypes = [P]
         L.orc_env_destroy.argtypes = [P]
@@ -226,6 +226,21 @@ def indep_pairs(oracle: "Oracle", q, cand, nthreads: int = 1, mask=None) -> np.n
     lib().orc_indep_pairs(ctypes.c_void_p(oracle.robot), ctypes.c_void_p(oracle.env), _p(q), ctypes.c_int(q.shape[0]),
                           _p(c), _p(m), ctypes.c_int(nthreads))
     return m
+
+
+def self_distance(oracle: "Oracle", q, cutoff: float = 1e3, nthreads: int = 1):
+    """Minimum distance between the robot's own links over its enabled self
+    pairs: (d [B], pair [B, 2], cp [B, 6], grad [B, L])."""
+    L = oracle.nl
+    q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, L)
+    B = q.shape[0]
+    d = np.zeros(B, np.float64)
+    pair = np.zeros((B, 2), np.int32)
+    cp = np.zeros((B, 6), np.float64)
+    g = np.zeros((B, L), np.float64)
+    lib().orc_self_distance(ctypes.c_void_p(oracle.robot), ctypes.c_void_p(oracle.env), _p(q), ctypes.c_int(B),
+                            ctypes.c_double(cutoff), _p(d), _p(pair), _p(cp), _p(g), ctypes.c_int(nthreads))
+    return d, pair, cp, g
 
 
 def jacobian(oracle: "Oracle", q, links, plocal):

@@ -117,3 +117,86 @@ def test_softmin_finite_differences(cfg2):
         total += err.size
     # kinks (a closest feature switching inside +-h) may spoil a few entries
     assert ok >= 0.95 * total, (ok, total)
+
+
+@pytest.mark.parametrize("which", ["arm", "dual_arm", "humanoid"])
+def test_self_distance_matches_oracle(built, which):
+    """Link-link minimum distance over the enabled self pairs: closest pair
+    exact, distance within 1e-6 relative, closest points within 1e-9,
+    gradient within 1e-4 of the FP64 oracle; contacts give 0 on the smallest
+    colliding pair."""
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle, self_distance
+    robot = {"arm": lambda: sc.arm(7, rings=8, segments=16), "dual_arm": sc.dual_arm,
+             "humanoid": sc.humanoid}[which]()
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    rng = np.random.default_rng(51)
+    # configurations scaled towards zero by a random factor: a mix of
+    # contacts and separated links (uniform humanoid configurations all
+    # self-collide)
+    q = (sc.uniform_configs(robot, 256, rng) * rng.uniform(0, 1, (256, 1))).astype(np.float32)
+    d_o, p_o, cp_o, g_o = self_distance(o, q, cutoff=1e3, nthreads=NT)
+    d, p, cp, g = (x.cpu().numpy() for x in w.self_distance(q, 1e3))
+    assert np.array_equal(p, p_o), np.flatnonzero((p != p_o).any(1))[:5]
+    rel = np.abs(d - d_o) / np.maximum(np.abs(d_o), 1e-12)
+    assert rel.max() <= 1e-6, (rel.max(), np.argmax(rel))
+    assert np.array_equal(d == 0, d_o == 0)
+    nz = d_o != 0
+    assert np.allclose(cp[nz], cp_o[nz], rtol=0, atol=1e-9)
+    assert (cp[~nz] == 0).all()
+    for b in range(len(q)):
+        assert _grad_close(g[b], g_o[b]), (b, g[b], g_o[b])
+    assert nz.any()
+    # cutoff below most distances: (cutoff, -1, -1) where nothing is closer
+    c = float(np.quantile(d_o[nz], 0.3))
+    d_c, p_c, _, _ = self_distance(o, q, cutoff=c, nthreads=NT)
+    d2, p2, _, g2 = (x.cpu().numpy() if x is not None else None for x in w.self_distance(q, c, want_grad=False))
+    assert g2 is None
+    assert np.array_equal(p2, p_c) and np.allclose(d2, d_c, rtol=1e-6, atol=0)
+    assert (p_c[:, 0] < 0).any() and (p_c[:, 0] >= 0).any()
+    w.close()
+
+
+def test_self_distance_finite_differences(built):
+    """d/dq of the self distance against central differences of the oracle
+    (h = 1e-3 on FP32 configurations, where the closest pair is unchanged)."""
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle, self_distance
+    robot = sc.arm(7, rings=8, segments=16)
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    q = sc.uniform_configs(robot, 32, np.random.default_rng(52))
+    d, p, _, g = (x.cpu().numpy() for x in w.self_distance(q, 1e3))
+    h = 1e-3
+    checked = 0
+    for b in np.flatnonzero(d > 1e-2)[:12]:
+        for k in range(robot.num_links):
+            qp, qm = q[b].copy(), q[b].copy()
+            qp[k] += h
+            qm[k] -= h
+            dp, pp, _, _ = self_distance(o, qp[None], cutoff=1e3)
+            dm, pm, _, _ = self_distance(o, qm[None], cutoff=1e3)
+            if tuple(pp[0]) != tuple(p[b]) or tuple(pm[0]) != tuple(p[b]):
+                continue
+            fd = (dp[0] - dm[0]) / (float(qp[k]) - float(qm[k]))
+            assert abs(fd - g[b, k]) <= 2e-2 * max(1.0, abs(g[b, k])), (b, k, fd, g[b, k])
+            checked += 1
+    assert checked > 20
+    w.close()
+
+
+def test_self_distance_empty_and_errors(built):
+    from klampt_gb300.engine import World
+    robot = sc.arm(3, rings=4, segments=8)
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    w = World(env, [robot])
+    d, p, cp, g = w.self_distance(np.zeros((0, 3), np.float32), 1.0)
+    assert d.shape == (0,) and p.shape == (0, 2)
+    with pytest.raises(Exception):
+        w.self_distance(np.zeros((4, 3), np.float32), -1.0)
+    with pytest.raises(Exception):
+        w.self_distance(np.zeros((4, 3), np.float32), float("nan"))
+    w.close()

@@ -301,3 +301,57 @@ def test_oracle_ik_reaches_reachable_targets():
         assert np.abs(Tb[:9].reshape(3, 3) @ pl[b] + Tb[9:] - pt[b]).max() <= 1e-6
     q, ok, res, its = ik_solve(o, q0, np.full(B, 6), pl, pt, Rtarget=T[:, :9], tol=1e-6)
     assert ok.mean() > 0.8
+
+
+def test_self_distance_brute_force():
+    """Self distance of a small arm against all triangle pairs of its enabled
+    self pairs (FP64 placements, canonical triangle distance): value, pair,
+    contact as 0, cutoff, and the gradient against central differences."""
+    from oracle.oracle_py import Oracle, self_distance, tri_tri
+    robot = sc.arm(4, rings=2, segments=6)
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    o = Oracle(robot, env)
+    rng = np.random.default_rng(41)
+    q = sc.uniform_configs(robot, 24, rng)
+    d, pair, cp, g = self_distance(o, q, cutoff=10.0)
+    L = robot.num_links
+    mask = robot.packed()["self_mask"].astype(bool).reshape(L, L)
+    for b in range(len(q)):
+        T = o.fk(q[b].astype(np.float64))
+        world = []
+        for l, (V, F) in enumerate(robot.meshes):
+            R, t = T[l, :9].reshape(3, 3), T[l, 9:]
+            world.append((V.astype(np.float64) @ R.T + t)[np.asarray(F)])
+        best, bp = np.inf, (-1, -1)
+        for i in range(L):
+            for j in range(i + 1, L):
+                if not mask[i, j]:
+                    continue
+                m = min(tri_tri(world[i][a], world[j][c])[1] for a in range(len(world[i])) for c in range(len(world[j])))
+                if np.sqrt(m) < best - 1e-12:
+                    best, bp = np.sqrt(m), (i, j)
+        assert abs(d[b] - best) <= 1e-9 * max(1.0, best), (b, d[b], best)
+        if best > 1e-6:
+            assert tuple(pair[b]) == bp, (b, pair[b], bp)
+    # cutoff: nothing below it gives (cutoff, -1, -1)
+    d2, p2, _, _ = self_distance(o, q[:4], cutoff=1e-9)
+    assert np.all((d2 == 1e-9) == (p2[:, 0] < 0))
+    # gradient against central differences (FP64 evaluation, steps where the
+    # closest pair stays the same)
+    h = 1e-5
+    checked = 0
+    for b in range(len(q)):
+        if not (d[b] > 1e-3):
+            continue
+        for k in range(L):
+            qp, qm = q[b].astype(np.float64).copy(), q[b].astype(np.float64).copy()
+            qp[k] += h
+            qm[k] -= h
+            dp, pp, _, _ = self_distance(o, qp.astype(np.float32)[None], cutoff=10.0)
+            dm, pm, _, _ = self_distance(o, qm.astype(np.float32)[None], cutoff=10.0)
+            if tuple(pp[0]) != tuple(pair[b]) or tuple(pm[0]) != tuple(pair[b]):
+                continue
+            fd = (dp[0] - dm[0]) / (np.float32(qp[k]) - np.float32(qm[k]))
+            assert abs(fd - g[b, k]) <= 2e-3 * max(1.0, abs(g[b, k])), (b, k, fd, g[b, k])
+            checked += 1
+    assert checked > 10
