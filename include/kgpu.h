@@ -297,14 +297,24 @@ kgpu_status kgpu_distance(kgpu_world world, int32_t robot, const float* q, int32
 /* Minimum distance between the robot's own links over its enabled self pairs,
  * clamped at `cutoff`, with its gradient d/dq: the link-link part of
  * WorldPlannerSettings::DistanceLowerBound when a robot is checked against
- * itself (PlannerSettings.cpp:385-395) and of geometry_ad.MinDistance over
+ * itself (Cpp/Planning/PlannerSettings.cpp:385-395) and of geometry_ad.MinDistance over
  * link geometries.  d(i, j) = exact minimum triangle distance (0 when the
- * surfaces meet); d: [B] = min over enabled pairs i < j, ties to the smallest
- * (i, j) (cutoff when nothing is closer); pair: [B*2] (i, j) or (-1,-1); cp:
+ * surfaces meet); d: [B] = min over enabled pairs i < j, equal distances to the
+ * smallest (i, j) (cutoff when nothing is closer); pair: [B*2] (i, j) or (-1,-1); cp:
  * [B*6] closest points in world frame (link i side, link j side; 0 when
  * d = 0); grad: [B*num_links] (may be NULL; 0 when d = 0). */
 kgpu_status kgpu_self_distance(kgpu_world world, int32_t robot, const float* q, int32_t B, double cutoff,
                                double* d, int32_t* pair, double* cp, float* grad, kgpu_stream stream);
+
+/* Every enabled self pair's own minimum distance, for the per-pair minima
+ * and maxima over sampled configurations of RandomizedSelfCollisionDistances
+ * (Cpp/Modeling/RandomizedSelfCollisions.cpp:142-180, which keeps, for each
+ * pair, the smallest and largest distance seen over numSamples samples).
+ * dpair: [B * L(L-1)/2], entry i*L - i(i+1)/2 + (j-i-1) for the pair i < j:
+ * the pair's exact minimum triangle distance (0 when the surfaces meet),
+ * clamped at `cutoff`; -1 for pairs that are not enabled or lack geometry. */
+kgpu_status kgpu_self_pair_distances(kgpu_world world, int32_t robot, const float* q, int32_t B, double cutoff,
+                                     double* dpair, kgpu_stream stream);
 
 /* Soft-min over all (waypoint, link, object) pairs of a trajectory of the
  * signed distance, L = -tau * log sum exp(-d/tau), and dL/dq by the adjoint

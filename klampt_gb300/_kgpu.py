@@ -86,6 +86,7 @@ _SIGS = {
     "kgpu_check_edges_plain64": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
     "kgpu_distance": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p, _c_p, _c_p, _c_p],
     "kgpu_self_distance": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p, _c_p, _c_p, _c_p],
+    "kgpu_self_pair_distances": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p],
     "kgpu_softmin_grad": [_c_p, _i32, _c_p, _i32, _i32, ctypes.c_double, _c_p, _c_p, _c_p],
     "kgpu_ik_solve": [_c_p, _i32, _i32, _c_p, _c_p, _i32, _c_p, _c_p, _c_p, _i32, ctypes.c_float, _c_p, _c_p, _c_p,
                       _c_p],

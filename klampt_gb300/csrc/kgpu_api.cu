@@ -937,9 +937,21 @@ kgpu_status kgpu_self_distance(kgpu_world w, int32_t robot, const float* q, int3
   if (st) return st;
   if (B < 0 || (B > 0 && (!q || !d || !pair || !cp))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if (!(cutoff > 0) || !(cutoff < 1e30)) return fail(KGPU_ERR_INVALID, "cutoff must be positive and finite");
-  return launch_status(launch_self_distance(w->d_dev, robot, q, B, cutoff, d, pair, cp, grad, w->num_sms,
+  return launch_status(launch_self_distance(w->d_dev, robot, q, B, cutoff, d, pair, cp, grad, nullptr, w->num_sms,
                                             (cudaStream_t)s),
                        "kgpu_self_distance");
+}
+
+kgpu_status kgpu_self_pair_distances(kgpu_world w, int32_t robot, const float* q, int32_t B, double cutoff,
+                                     double* dpair, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && (!q || !dpair))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  if (!(cutoff > 0) || !(cutoff < 1e30)) return fail(KGPU_ERR_INVALID, "cutoff must be positive and finite");
+  return launch_status(launch_self_distance(w->d_dev, robot, q, B, cutoff, nullptr, nullptr, nullptr, nullptr, dpair,
+                                            w->num_sms, (cudaStream_t)s),
+                       "kgpu_self_pair_distances");
 }
 
 kgpu_status kgpu_softmin_grad(kgpu_world w, int32_t robot, const float* q, int32_t T, int32_t Wn, double tau,

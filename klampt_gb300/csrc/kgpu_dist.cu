@@ -1018,6 +1018,7 @@ struct SelfDistArgs {
   int* pair;       // [B, 2]
   double* cp;      // [B, 6] (point on link i, point on link j)
   float* grad;     // [B, L] or null
+  double* dpair;   // per-pair mode: [B, L (L - 1) / 2], each pair's own minimum
 };
 
 // FP64 finalisation of candidates of pair (i, j), merged into the pair's
@@ -1097,6 +1098,12 @@ __global__ void __launch_bounds__(kDW * 32, 1) k_self_dist(const KWorldDev* __re
     }
     __syncwarp();
     warp_fk64(R, S.q64, S.T64, lane);
+    const bool per_pair = A.dpair != nullptr;
+    const int npair = nl * (nl - 1) / 2;
+    if (per_pair) {
+      for (int k = lane; k < npair; k += 32) A.dpair[(size_t)b * npair + k] = -1.0;  // pairs not queried
+      __syncwarp();
+    }
     float m32 = fcut;  // upper bound on the minimum so far (warp-uniform)
     bool contact = false;
 #pragma unroll 1
@@ -1108,7 +1115,10 @@ __global__ void __launch_bounds__(kDW * 32, 1) k_self_dist(const KWorldDev* __re
       const float* TB = S.T[j];
       const float dd = S.delta[i] + S.delta[j];
       int top = 1, njobs = 0, ncand = 0;
+      bool pc = false;  // certified contact of this pair
+      if (per_pair) m32 = fcut;  // every pair on its own
       if (lane == 0) {
+        if (per_pair) S.bd = A.cutoff;
         S.stack[0] = make_uint2((uint32_t)R.link_root[i], (uint32_t)R.link_root[j]);
         const double bb = kx_mul(S.bd, S.bd);
         S.pb2 = bb > 1e-300 ? bb : 1e-300;
@@ -1117,7 +1127,7 @@ __global__ void __launch_bounds__(kDW * 32, 1) k_self_dist(const KWorldDev* __re
       }
       __syncwarp();
 #pragma unroll 1
-      while ((top > 0 || njobs > 0) && !contact) {
+      while ((top > 0 || njobs > 0) && !pc) {
         if (njobs >= 16 || (top == 0 && njobs > 0)) {
           // ---- triangle pairs, one per lane
           uint32_t carry = 0;
@@ -1179,8 +1189,8 @@ __global__ void __launch_bounds__(kDW * 32, 1) k_self_dist(const KWorldDev* __re
               }
             }
             if (__any_sync(0xffffffffu, certain)) {
-              contact = true;  // distance 0: no later pair can be smaller
-              if (lane == 0) {
+              pc = true;  // distance 0: no later pair can be smaller
+              if (lane == 0 && !per_pair) {
                 S.b2 = 0.0;
                 S.bd = 0.0;
                 S.bi = i;
@@ -1272,12 +1282,19 @@ __global__ void __launch_bounds__(kDW * 32, 1) k_self_dist(const KWorldDev* __re
         njobs += __popc(m2);
         __syncwarp();
       }
-      if (!contact && ncand > 0) {
+      if (!pc && ncand > 0) {
         sd_flush(S, W, lane, i, j, ncand, m32 * (1.f + 2e-5f) + 1e-6f);
         if (S.phave) m32 = fminf(m32, (float)sqrt(S.pb2) * (1.f + 1e-6f));
       }
+      if (per_pair) {
+        if (lane == 0)
+          A.dpair[(size_t)b * npair + i * nl - i * (i + 1) / 2 + (j - i - 1)] =
+              pc ? 0.0 : (S.phave ? kx_sqrt(S.pb2) : A.cutoff);
+        __syncwarp();
+        continue;
+      }
       // the pair replaces the best only with a strictly smaller distance
-      if (!contact && S.phave) {
+      if (!pc && S.phave) {
         const double dp = kx_sqrt(S.pb2);
         if (dp < S.bd) {
           __syncwarp();
@@ -1293,6 +1310,7 @@ __global__ void __launch_bounds__(kDW * 32, 1) k_self_dist(const KWorldDev* __re
       __syncwarp();
       if (S.b2 == 0.0) contact = true;
     }
+    if (per_pair) continue;
     // ---- outputs and the gradient (FP64 transforms)
     const bool found = S.b2 < DBL_MAX;
     const double d = found ? kx_sqrt(S.b2) : A.cutoff;
@@ -1408,7 +1426,7 @@ cudaError_t launch_softmin(const KWorldDev* Wd, const Scratch& S, int robot, con
 namespace kgpu {
 
 cudaError_t launch_self_distance(const KWorldDev* Wd, int robot, const float* q, int B, double cutoff, double* d,
-                                 int* pair, double* cp, float* grad, int num_sms, cudaStream_t s)
+                                 int* pair, double* cp, float* grad, double* dpair, int num_sms, cudaStream_t s)
 {
   if (B <= 0) return cudaSuccess;
   static bool attr = false;
@@ -1427,6 +1445,7 @@ cudaError_t launch_self_distance(const KWorldDev* Wd, int robot, const float* q,
   A.pair = pair;
   A.cp = cp;
   A.grad = grad;
+  A.dpair = dpair;
   const int blocks = min((B + kDW - 1) / kDW, 4 * num_sms);
   k_self_dist<<<blocks, kDW * 32, smem, s>>>(Wd, A);
   return cudaGetLastError();

@@ -281,7 +281,7 @@ cudaError_t launch_distance(const KWorldDev* Wd, const Scratch& S, int robot, co
                             double cutoff, double* d, int* pair, double* cp, float* grad, int num_sms,
                             cudaStream_t s);
 cudaError_t launch_self_distance(const KWorldDev* Wd, int robot, const float* q, int B, double cutoff, double* d,
-                                 int* pair, double* cp, float* grad, int num_sms, cudaStream_t s);
+                                 int* pair, double* cp, float* grad, double* dpair, int num_sms, cudaStream_t s);
 // work: 2*T*Wn + T doubles of device scratch
 cudaError_t launch_softmin(const KWorldDev* Wd, const Scratch& S, int robot, const float* q, int T,
                            int Wn, double tau, double* L, float* dLdq, int nl, double* work,

@@ -283,6 +283,19 @@ class World:
             self.sync()
         return d, pair, cp, g
 
+    def self_pair_distances(self, q, cutoff: float, robot: int = 0, sync: bool = True):
+        """Every enabled self pair's own minimum distance: [B, L (L - 1) / 2]
+        in upper-triangle order (i < j), clamped at cutoff; -1 for pairs not
+        enabled."""
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L).contiguous()
+        B = qd.shape[0]
+        out = torch.empty((B, L * (L - 1) // 2), dtype=torch.float64, device="cuda")
+        check(lib().kgpu_self_pair_distances(self.handle, robot, _dptr(qd), B, float(cutoff), _dptr(out), _stream()))
+        if sync:
+            self.sync()
+        return out
+
     def softmin(self, q, tau: float, robot: int = 0, want_grad: bool = True, sync: bool = True):
         L = self.robots[robot].num_links
         qd = _dev(q, torch.float32)

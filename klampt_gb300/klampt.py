@@ -373,6 +373,27 @@ def RandomizedIndependentSelfCollisionPairs(robot: "RobotModel", numSamples: int
     return _words_to_matrix(words, robot.spec.num_links)
 
 
+def RandomizedSelfCollisionDistances(robot: "RobotModel", numSamples: int, seed: int = 0,
+                                     cutoff: float = 1e3):
+    """(minDistance, maxDistance) [L, L]: for each enabled self pair i < j the
+    smallest and largest distance over numSamples configurations drawn like
+    SampleRobot (Cpp/Modeling/RandomizedSelfCollisions.cpp:142-180); +inf /
+    -inf for pairs that are not enabled (the reference's initial values).
+    Distances are exact (the reference asks its geometry backend for 0.001
+    absolute / 1% relative accuracy)."""
+    L = robot.spec.num_links
+    Q = _sample_configs(robot, numSamples, np.random.default_rng(seed))
+    dp = robot.world.engine.self_pair_distances(Q, cutoff, robot=robot.index).cpu().numpy()
+    lo = np.full((L, L), np.inf)
+    hi = np.full((L, L), -np.inf)
+    iu, ju = np.triu_indices(L, 1)
+    valid = (dp >= 0).all(0) if len(dp) else np.zeros(len(iu), bool)
+    if len(dp):
+        lo[iu[valid], ju[valid]] = dp[:, valid].min(0)
+        hi[iu[valid], ju[valid]] = dp[:, valid].max(0)
+    return lo, hi
+
+
 class RobotCSpace:
     """robotcspace.py:31: feasibility = joint limits, then environment, then
     self collision (RobotCSpace.cpp:786-823); visibility = every

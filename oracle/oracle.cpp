@@ -1330,6 +1330,38 @@ int orc_self_distance(void* robot, void* env, const float* q, int B, double cuto
   return 0;
 }
 
+/* Each enabled self pair's own minimum distance, clamped at the cutoff (the
+   per-sample distances RandomizedSelfCollisionDistances reduces to per-pair
+   minima and maxima, Cpp/Modeling/RandomizedSelfCollisions.cpp:142-180):
+   dpair[b * P + i*L - i(i+1)/2 + (j-i-1)], P = L(L-1)/2; -1 for pairs not
+   queried. */
+int orc_self_pair_distances(void* robot, void* env, const float* q, int B, double cutoff, double* dpair,
+                            int nthreads)
+{
+  Robot* R = (Robot*)robot;
+  Env* E = (Env*)env;
+  const int L = R->L, P = L * (L - 1) / 2;
+  parallel_for(B, nthreads, [&](int, int b0, int b1) {
+    Ctx c;
+    std::vector<uint32_t> masks(L, 0u);
+    c.init(R, E, masks.data());
+    std::vector<double> qd(L);
+    for (int b = b0; b < b1; ++b) {
+      for (int i = 0; i < L; ++i) qd[i] = (double)q[(size_t)b * L + i];
+      c.set_config(qd.data());
+      double* out = dpair + (size_t)b * P;
+      for (int k = 0; k < P; ++k) out[k] = -1.0;
+      for (int i = 0; i < L; ++i)
+        for (int j = i + 1; j < L; ++j) {
+          if (!R->self_mask[i * L + j] || R->tloc[i].empty() || R->tloc[j].empty()) continue;
+          PairResult pr = self_pair_distance(c, i, j, cutoff);
+          out[i * L - i * (i + 1) / 2 + (j - i - 1)] = pr.found ? pr.d : cutoff;
+        }
+    }
+  });
+  return 0;
+}
+
 /* Full Jacobians (KrisLibrary GetFullJacobian as called by
    RobotModelLink::getJacobian, Python/klampt/src/robotsim.cpp:4817-4825):
    J[b] = 6 x L row-major, rows 0-2 angular (world axis of each revolute

@@ -41,7 +41,7 @@ def lib():
         L.orc_env_create.restype = P
         for name in ("orc_check_configs", "orc_check_edges", "orc_is_feasible", "orc_pair_distance",
                      "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian", "orc_self_pairs", "orc_ik",
-                     "orc_indep_pairs", "orc_self_distance"):
+                     "orc_indep_pairs", "orc_self_distance", "orc_self_pair_distances"):
             getattr(L, name).restype = ctypes.c_int
         L.orc_robot_destroy.argtypes = [P]
         L.orc_env_destroy.argtypes = [P]
@@ -241,6 +241,18 @@ def self_distance(oracle: "Oracle", q, cutoff: float = 1e3, nthreads: int = 1):
     lib().orc_self_distance(ctypes.c_void_p(oracle.robot), ctypes.c_void_p(oracle.env), _p(q), ctypes.c_int(B),
                             ctypes.c_double(cutoff), _p(d), _p(pair), _p(cp), _p(g), ctypes.c_int(nthreads))
     return d, pair, cp, g
+
+
+def self_pair_distances(oracle: "Oracle", q, cutoff: float = 1e3, nthreads: int = 1):
+    """Each enabled self pair's own minimum distance: [B, L (L - 1) / 2] in
+    upper-triangle order, clamped at cutoff; -1 for pairs not queried."""
+    L = oracle.nl
+    q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, L)
+    B = q.shape[0]
+    out = np.zeros((B, L * (L - 1) // 2), np.float64)
+    lib().orc_self_pair_distances(ctypes.c_void_p(oracle.robot), ctypes.c_void_p(oracle.env), _p(q), ctypes.c_int(B),
+                                  ctypes.c_double(cutoff), _p(out), ctypes.c_int(nthreads))
+    return out
 
 
 def jacobian(oracle: "Oracle", q, links, plocal):

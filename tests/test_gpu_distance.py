@@ -200,3 +200,33 @@ def test_self_distance_empty_and_errors(built):
     with pytest.raises(Exception):
         w.self_distance(np.zeros((4, 3), np.float32), float("nan"))
     w.close()
+
+
+def test_self_pair_distances_matches_oracle(built):
+    """Every enabled pair's own minimum bit for bit, disabled pairs -1, and the
+    sampled per-pair minima and maxima of RandomizedSelfCollisionDistances."""
+    from klampt_gb300.engine import World
+    from klampt_gb300 import klampt as kl
+    from oracle.oracle_py import Oracle, self_pair_distances
+    robot = sc.dual_arm()
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    rng = np.random.default_rng(53)
+    q = (sc.uniform_configs(robot, 128, rng) * rng.uniform(0, 1, (128, 1))).astype(np.float32)
+    for cutoff in (1e3, 0.2):
+        dp_o = self_pair_distances(o, q, cutoff=cutoff, nthreads=NT)
+        dp = w.self_pair_distances(q, cutoff).cpu().numpy()
+        assert np.array_equal(dp, dp_o), np.argwhere(dp != dp_o)[:5]
+    assert (dp_o == 0).any() and (dp_o == 0.2).any() and ((dp_o > 0) & (dp_o < 0.2)).any()
+    w.close()
+    wm = kl.WorldModel([robot], env)
+    lo, hi = kl.RandomizedSelfCollisionDistances(wm.robot(0), 64, seed=3)
+    Q = kl._sample_configs(wm.robot(0), 64, np.random.default_rng(3))
+    ref = self_pair_distances(o, Q, cutoff=1e3, nthreads=NT)
+    L = robot.num_links
+    iu, ju = np.triu_indices(L, 1)
+    ok = (ref >= 0).all(0)
+    assert np.array_equal(lo[iu[ok], ju[ok]], ref[:, ok].min(0))
+    assert np.array_equal(hi[iu[ok], ju[ok]], ref[:, ok].max(0))
+    assert np.isinf(lo[iu[~ok], ju[~ok]]).all()

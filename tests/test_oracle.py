@@ -355,3 +355,32 @@ def test_self_distance_brute_force():
             assert abs(fd - g[b, k]) <= 2e-3 * max(1.0, abs(g[b, k])), (b, k, fd, g[b, k])
             checked += 1
     assert checked > 10
+
+
+def test_self_pair_distances_consistent():
+    """Per-pair self distances: the minimum over the enabled pairs is the self
+    distance (the earliest pair on equal distances), each entry matches the
+    brute force over the pair's triangles, disabled pairs read -1."""
+    from oracle.oracle_py import Oracle, self_distance, self_pair_distances, tri_tri
+    robot = sc.arm(4, rings=2, segments=6)
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    o = Oracle(robot, env)
+    q = sc.uniform_configs(robot, 12, np.random.default_rng(43))
+    dp = self_pair_distances(o, q, cutoff=10.0)
+    d, pair, _, _ = self_distance(o, q, cutoff=10.0)
+    L = robot.num_links
+    iu, ju = np.triu_indices(L, 1)
+    mask = robot.packed()["self_mask"].astype(bool).reshape(L, L)[iu, ju]
+    assert (dp[:, ~mask] == -1).all() and (dp[:, mask] >= 0).all()
+    for b in range(len(q)):
+        k = int(np.argmin(np.where(mask, dp[b], np.inf)))
+        assert dp[b, k] == d[b] and (iu[k], ju[k]) == tuple(pair[b])
+        T = o.fk(q[b].astype(np.float64))
+        world = []
+        for l, (V, F) in enumerate(robot.meshes):
+            R, t = T[l, :9].reshape(3, 3), T[l, 9:]
+            world.append((V.astype(np.float64) @ R.T + t)[np.asarray(F)])
+        for k in np.flatnonzero(mask):
+            i, j = iu[k], ju[k]
+            m = min(tri_tri(a, c)[1] for a in world[i] for c in world[j])
+            assert abs(dp[b, k] - np.sqrt(m)) <= 1e-12
