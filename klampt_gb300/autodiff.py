@@ -48,3 +48,20 @@ class MinDistance(torch.autograd.Function):
     def backward(ctx, gd: torch.Tensor):
         (g,) = ctx.saved_tensors
         return (gd.to(g.dtype)[:, None] * g), None, None, None
+
+
+class SelfMinDistance(torch.autograd.Function):
+    """Minimum distance between the robot's own links over its enabled self
+    pairs per configuration, clamped at `cutoff` (gradient zero when clamped
+    or in contact), q: [B, L].  Returns float64 [B]."""
+
+    @staticmethod
+    def forward(ctx, q: torch.Tensor, world: World, cutoff: float = 1.0, robot: int = 0):
+        d, pair, cp, g = world.self_distance(q.detach(), cutoff, robot=robot, want_grad=True)
+        ctx.save_for_backward(g)
+        return d
+
+    @staticmethod
+    def backward(ctx, gd: torch.Tensor):
+        (g,) = ctx.saved_tensors
+        return (gd.to(g.dtype)[:, None] * g), None, None, None

@@ -230,3 +230,22 @@ def test_self_pair_distances_matches_oracle(built):
     assert np.array_equal(lo[iu[ok], ju[ok]], ref[:, ok].min(0))
     assert np.array_equal(hi[iu[ok], ju[ok]], ref[:, ok].max(0))
     assert np.isinf(lo[iu[~ok], ju[~ok]]).all()
+
+
+def test_self_min_distance_autograd(built):
+    """The autograd Function's backward applies the kernel's gradient."""
+    import torch
+    from klampt_gb300.autodiff import SelfMinDistance
+    from klampt_gb300.engine import World
+    robot = sc.arm(7, rings=8, segments=16)
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    w = World(env, [robot])
+    rng = np.random.default_rng(54)
+    q = (sc.uniform_configs(robot, 64, rng) * rng.uniform(0, 1, (64, 1))).astype(np.float32)
+    d_ref, _, _, g_ref = w.self_distance(q, 1e3)
+    qt = torch.tensor(q, device="cuda", requires_grad=True)
+    d = SelfMinDistance.apply(qt, w, 1e3)
+    assert torch.allclose(d.detach(), d_ref, rtol=1e-12, atol=0)
+    (2.0 * d).sum().backward()
+    assert torch.allclose(qt.grad, 2.0 * g_ref)
+    w.close()
