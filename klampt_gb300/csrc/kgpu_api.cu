@@ -947,8 +947,9 @@ kgpu_status kgpu_self_pair_distances(kgpu_world w, int32_t robot, const float* q
 {
   kgpu_status st = check_world(w, robot);
   if (st) return st;
-  if (B < 0 || (B > 0 && (!q || !dpair))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if (!(cutoff > 0) || !(cutoff < 1e30)) return fail(KGPU_ERR_INVALID, "cutoff must be positive and finite");
+  if (w->robots[robot]->nlinks < 2) return B < 0 ? fail(KGPU_ERR_INVALID, "bad buffers") : KGPU_OK;  // no pairs
+  if (B < 0 || (B > 0 && (!q || !dpair))) return fail(KGPU_ERR_INVALID, "bad buffers");
   return launch_status(launch_self_distance(w->d_dev, robot, q, B, cutoff, nullptr, nullptr, nullptr, nullptr, dpair,
                                             w->num_sms, (cudaStream_t)s),
                        "kgpu_self_pair_distances");
