@@ -384,3 +384,26 @@ def test_self_pair_distances_consistent():
             i, j = iu[k], ju[k]
             m = min(tri_tri(a, c)[1] for a in world[i] for c in world[j])
             assert abs(dp[b, k] - np.sqrt(m)) <= 1e-12
+
+
+def test_self_distance_pair_ties_keep_earlier_pair():
+    """The 7-link arm's (3, 5) and (4, 6) pairs are mirror images: their
+    distances are often the same double while the squared distances differ in
+    the last bit.  The pair loop keeps the earlier pair unless a later one is
+    strictly closer, so the result is (3, 5) whenever the two distances are
+    equal."""
+    from oracle.oracle_py import Oracle, self_distance, self_pair_distances
+    robot = sc.arm(7, rings=8, segments=16)
+    env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+    o = Oracle(robot, env)
+    rng = np.random.default_rng(51)
+    q = (sc.uniform_configs(robot, 256, rng) * rng.uniform(0, 1, (256, 1))).astype(np.float32)
+    q = q[:32]
+    d, pair, _, _ = self_distance(o, q, cutoff=1e3, nthreads=os.cpu_count() or 4)
+    dp = self_pair_distances(o, q, cutoff=1e3, nthreads=os.cpu_count() or 4)
+    L = robot.num_links
+    k35 = 3 * L - 3 * 4 // 2 + (5 - 3 - 1)
+    k46 = 4 * L - 4 * 5 // 2 + (6 - 4 - 1)
+    tied = np.flatnonzero((dp[:, k35] == dp[:, k46]) & (dp[:, k35] == d) & (d > 0))
+    assert len(tied) >= 2
+    assert (pair[tied] == [3, 5]).all()
