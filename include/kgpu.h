@@ -197,6 +197,14 @@ kgpu_status kgpu_world_reset_stats(kgpu_world world);
 kgpu_status kgpu_fk(kgpu_world world, int32_t robot, const float* q, int32_t B, float* T_out,
                     float* err_out, kgpu_stream stream);
 
+/* Forward kinematics in the canonical FP64 arithmetic (include/kgpu_exact.h):
+ * the link transforms every FP64 decision of the engine and the oracle uses,
+ * bit for bit (RobotModel::setConfig -> UpdateFrames in double precision,
+ * robotsim.cpp:5311-5321).  q: [B*num_links] float (widened exactly),
+ * T_out: [B*num_links*12] double. */
+kgpu_status kgpu_fk64(kgpu_world world, int32_t robot, const float* q, int32_t B, double* T_out,
+                      kgpu_stream stream);
+
 /* Batched inverse kinematics: B problems, each moving point plocal[b] (link
  * frame) of link links[b] (or `link` when links is NULL) to ptarget[b] and,
  * when Rtarget is not NULL, the link's rotation to Rtarget[b] (row-major).
@@ -306,15 +314,18 @@ kgpu_status kgpu_distance(kgpu_world world, int32_t robot, const float* q, int32
 kgpu_status kgpu_self_distance(kgpu_world world, int32_t robot, const float* q, int32_t B, double cutoff,
                                double* d, int32_t* pair, double* cp, float* grad, kgpu_stream stream);
 
-/* Every enabled self pair's own minimum distance, for the per-pair minima
- * and maxima over sampled configurations of RandomizedSelfCollisionDistances
+/* Each self pair's own minimum distance, for the per-pair minima and maxima
+ * over sampled configurations of RandomizedSelfCollisionDistances
  * (Cpp/Modeling/RandomizedSelfCollisions.cpp:142-180, which keeps, for each
- * pair, the smallest and largest distance seen over numSamples samples).
+ * pair i < j whose links both have geometry, the smallest and largest
+ * distance seen over numSamples samples).  all_pairs != 0 queries every such
+ * pair, as that function does, whatever the self-collision mask says;
+ * all_pairs == 0 only the enabled self pairs.
  * dpair: [B * L(L-1)/2], entry i*L - i(i+1)/2 + (j-i-1) for the pair i < j:
  * the pair's exact minimum triangle distance (0 when the surfaces meet),
- * clamped at `cutoff`; -1 for pairs that are not enabled or lack geometry. */
+ * clamped at `cutoff`; -1 for pairs that are not queried or lack geometry. */
 kgpu_status kgpu_self_pair_distances(kgpu_world world, int32_t robot, const float* q, int32_t B, double cutoff,
-                                     double* dpair, kgpu_stream stream);
+                                     int32_t all_pairs, double* dpair, kgpu_stream stream);
 
 /* Soft-min over all (waypoint, link, object) pairs of a trajectory of the
  * signed distance, L = -tau * log sum exp(-d/tau), and dL/dq by the adjoint
@@ -337,6 +348,56 @@ kgpu_status kgpu_softmin_grad(kgpu_world world, int32_t robot, const float* q, i
  * (Python/klampt/model/collide.py:219-243), one call for R rays. */
 kgpu_status kgpu_raycast(kgpu_world world, const float* s, const float* d, int32_t R, int32_t* obj,
                          int32_t* tri, double* t, double* point, kgpu_stream stream);
+
+/* ---- free geometries: Geometry3D pair queries -------------------------------- */
+/* A triangle mesh with its own BVH, placed by a caller-supplied transform per
+ * query: the analogue of a TriangleMesh Geometry3D (Python/klampt/src/
+ * geometry.h:810) with its collision margin (setCollisionMargin,
+ * geometry.h:930).  Vertices are in the geometry's own frame. */
+typedef struct kgpu_geom_s* kgpu_geom;
+typedef struct {
+  int32_t num_verts;
+  const double* verts;  /* [num_verts*3] */
+  int32_t num_tris;
+  const int32_t* tris;  /* [num_tris*3] vertex indices */
+  double margin;        /* collision margin (>= 0) */
+} kgpu_geom_desc;
+kgpu_status kgpu_geom_create(const kgpu_geom_desc* desc, kgpu_geom* out);
+kgpu_status kgpu_geom_destroy(kgpu_geom geom);
+/* Geometry3D::setCollisionMargin / getCollisionMargin (robotsim.cpp). */
+kgpu_status kgpu_geom_set_margin(kgpu_geom geom, double margin);
+kgpu_status kgpu_geom_get_margin(kgpu_geom geom, double* margin);
+
+/* Batched pair queries between geometry a at transform Ta[b] and geometry
+ * b at transform Tb[b] (device buffers of B*12 doubles, R row-major then t;
+ * with KGPU_GEOM_FIXED_A / _B in flags, Ta / Tb is one transform used for
+ * every query).  Results are those of the canonical FP64 arithmetic on the
+ * world-placed triangles (include/kgpu_exact.h). */
+#define KGPU_GEOM_FIXED_A 1
+#define KGPU_GEOM_FIXED_B 2
+/* hit[b] = 1 when the geometries are within (m_a + tol) + m_b of each other
+ * (tol = 0: Geometry3D::collides, robotsim.cpp:1656-1662, touching counts;
+ * tol > 0: Geometry3D::withinDistance, robotsim.cpp:1685-1690 and
+ * ::CheckCollision(m1, m2, tol), Cpp/Planning/PlannerSettings.cpp:96-107). */
+kgpu_status kgpu_geom_collide(kgpu_geom a, kgpu_geom b, const double* Ta, const double* Tb, int32_t B, int32_t flags,
+                              double tol, uint8_t* hit, kgpu_stream stream);
+/* Geometry3D::distance_ext (robotsim.cpp:1782-1819) with
+ * DistanceQuerySettings.upperBound = upper_bound (+inf for none; relErr and
+ * absErr are met with 0): d[b] = mesh distance - (m_a + m_b) (triangle
+ * meshes give unsigned mesh distances, 0 when they meet), or upper_bound
+ * when nothing is closer; cp[b*6] the closest points (on a, then on b, world
+ * frame; on contact both are a vertex of a's touching triangle); elem[b*2]
+ * the closest triangle pair (mesh order; ties to the smallest, (-1,-1) when
+ * nothing is closer); dir[b*3] (may be NULL) grad1 = (cp_a - cp_b)/|cp_a -
+ * cp_b| (grad2 = -grad1, geometry.h:660-662), 0 on contact.  An empty
+ * geometry is KGPU_ERR_EMPTY (robotsim.cpp:1786-1787). */
+kgpu_status kgpu_geom_distance(kgpu_geom a, kgpu_geom b, const double* Ta, const double* Tb, int32_t B, int32_t flags,
+                               double upper_bound, double* d, double* cp, int32_t* elem, double* dir,
+                               kgpu_stream stream);
+/* Waits for the stream, then returns (and clears) geometry a's device status
+ * word set by the pair queries it was the first geometry of (non-finite or
+ * |entry| >= 1e6 transforms: KGPU_ERR_NOT_FINITE). */
+kgpu_status kgpu_geom_sync(kgpu_geom a, kgpu_stream stream);
 
 /* ---- host-buffer variants (pinned staging inside; synchronous) ------------ */
 kgpu_status kgpu_check_configs_host(kgpu_world world, int32_t robot, const float* q, int32_t B,

@@ -26,6 +26,9 @@ KGPU_ERR_NOT_FINITE = 6
 KGPU_ERR_EMPTY = 7
 KGPU_ERR_UNSUPPORTED = 8
 
+GEOM_FIXED_A = 1
+GEOM_FIXED_B = 2
+
 GROUP_RIGID_OBJECT = 0
 GROUP_TERRAIN = 1
 MAX_LINKS = 32
@@ -43,6 +46,11 @@ class RobotDesc(ctypes.Structure):
 class EnvDesc(ctypes.Structure):
     _fields_ = [("num_objects", _i32), ("vert_offset", _c_p), ("verts", _c_p), ("tri_offset", _c_p),
                 ("tris", _c_p), ("groups", _c_p), ("convex", _c_p), ("margins", _c_p)]
+
+
+class GeomDesc(ctypes.Structure):
+    _fields_ = [("num_verts", ctypes.c_int32), ("verts", ctypes.c_void_p), ("num_tris", ctypes.c_int32),
+                ("tris", ctypes.c_void_p), ("margin", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -78,6 +86,7 @@ _SIGS = {
     "kgpu_world_get_stats": [_c_p, _c_p],
     "kgpu_world_reset_stats": [_c_p],
     "kgpu_fk": [_c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
+    "kgpu_fk64": [_c_p, _i32, _c_p, _i32, _c_p, _c_p],
     "kgpu_check_configs": [_c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
     "kgpu_check_configs_multi": [_c_p, _c_p, _c_p, _i32, _i32, _c_p, _c_p, _c_p],
     "kgpu_is_feasible": [_c_p, _i32, _c_p, _i32, _c_p, _c_p],
@@ -86,7 +95,7 @@ _SIGS = {
     "kgpu_check_edges_plain64": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
     "kgpu_distance": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p, _c_p, _c_p, _c_p],
     "kgpu_self_distance": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p, _c_p, _c_p, _c_p],
-    "kgpu_self_pair_distances": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p],
+    "kgpu_self_pair_distances": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _i32, _c_p, _c_p],
     "kgpu_softmin_grad": [_c_p, _i32, _c_p, _i32, _i32, ctypes.c_double, _c_p, _c_p, _c_p],
     "kgpu_ik_solve": [_c_p, _i32, _i32, _c_p, _c_p, _i32, _c_p, _c_p, _c_p, _i32, ctypes.c_float, _c_p, _c_p, _c_p,
                       _c_p],
@@ -94,6 +103,13 @@ _SIGS = {
     "kgpu_independent_self_collision_pairs": [_c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
     "kgpu_jacobian": [_c_p, _i32, _c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
     "kgpu_raycast": [_c_p, _c_p, _c_p, _i32, _c_p, _c_p, _c_p, _c_p, _c_p],
+    "kgpu_geom_create": [_c_p, _c_p],
+    "kgpu_geom_destroy": [_c_p],
+    "kgpu_geom_set_margin": [_c_p, ctypes.c_double],
+    "kgpu_geom_get_margin": [_c_p, _c_p],
+    "kgpu_geom_collide": [_c_p, _c_p, _c_p, _c_p, _i32, _i32, ctypes.c_double, _c_p, _c_p],
+    "kgpu_geom_distance": [_c_p, _c_p, _c_p, _c_p, _i32, _i32, ctypes.c_double, _c_p, _c_p, _c_p, _c_p, _c_p],
+    "kgpu_geom_sync": [_c_p, _c_p],
     "kgpu_check_configs_host": [_c_p, _i32, _c_p, _i32, _c_p, _c_p],
     "kgpu_check_edges_host": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p],
     "kgpu_check_edges_noalloc": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],

@@ -23,9 +23,9 @@ OBJ_DIR = os.path.join(OUT_DIR, "obj")
 LIB = os.path.join(OUT_DIR, "libkgpu.so")
 
 CU_SOURCES = ["kgpu_api.cu", "kgpu_collide.cu", "kgpu_plain.cu", "kgpu_dist.cu", "kgpu_noalloc.cu", "kgpu_ray.cu", "kgpu_ik.cu",
-              "kgpu_lbvh.cu"]
+              "kgpu_lbvh.cu", "kgpu_geom.cu"]
 CPP_SOURCES = ["bvh.cpp"]
-HEADERS = ["kgpu_internal.h", "kgpu_device.cuh"]
+HEADERS = ["kgpu_internal.h", "kgpu_device.cuh", "kgpu_dist32.cuh"]
 INCLUDE_HEADERS = ["kgpu.h", "kgpu_exact.h"]
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

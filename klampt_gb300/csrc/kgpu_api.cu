@@ -33,6 +33,7 @@ kgpu_status record_error(kgpu_status code, const char* msg)
 cudaError_t engine_init();
 size_t engine_smem_per_warp();
 int engine_warps_per_block();
+int engine_scratch_doubles();
 }
 
 namespace {
@@ -231,6 +232,22 @@ kgpu_status refresh_tables(kgpu_world w)
 }
 
 int grid_blocks(kgpu_world w) { return w->num_sms * w->blocks_per_sm; }
+
+}  // namespace
+
+namespace kgpu {
+// The world's engine scratch with the optional caps applied (a copy: the
+// allocation is unchanged).
+Scratch engine_scratch(kgpu_world w, Scratch S)
+{
+  if (w->pend_cap_opt > 0 && w->pend_cap_opt < S.pend_cap) S.pend_cap = w->pend_cap_opt;
+  const size_t spill = (size_t)w->spill_cap_opt + (size_t)engine_scratch_doubles();
+  if (w->spill_cap_opt > 0 && spill < S.spill_per_warp) S.spill_per_warp = spill;
+  return S;
+}
+}  // namespace kgpu
+
+namespace {
 
 kgpu_status ensure_edge_scratch(kgpu_world w, int E)
 {
@@ -571,6 +588,7 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&w->num_sms, cudaDevAttrMultiProcessorCount, dev);
   if (e == cudaSuccess) e = engine_init();
   if (e == cudaSuccess) e = dist_init();
+  if (e == cudaSuccess) e = noalloc_prepare();  // kgpu_check_edges_noalloc's array, loaded now
   if (e != cudaSuccess) {
     delete w;
     return cuda_fail(e, "device query");
@@ -761,6 +779,20 @@ kgpu_status kgpu_world_set_option(kgpu_world w, const char* name, double v)
     int k = (int)v;
     if (k < 1 || k > 64) return fail(KGPU_ERR_INVALID, "edge_chunk must be in [1,64]");
     w->edge_chunk = k;
+  } else if (!strcmp(name, "pend_cap")) {
+    if (!(v >= 0 && v <= 1e9)) return fail(KGPU_ERR_INVALID, "pend_cap must be in [0, 1e9] (0: no cap)");
+    w->pend_cap_opt = (int)v;
+  } else if (!strcmp(name, "spill_cap")) {
+    if (!(v >= 0 && v <= 1e9)) return fail(KGPU_ERR_INVALID, "spill_cap must be in [0, 1e9] (0: no cap)");
+    w->spill_cap_opt = (int)v;
+  } else if (!strcmp(name, "share_wait_polls")) {
+    if (!(v >= 0 && v <= (double)(1 << 20))) return fail(KGPU_ERR_INVALID, "share_wait_polls must be in [0, 2^20]");
+    w->dev.share_wait = (int)v;
+    w->tables_dirty = true;
+  } else if (!strcmp(name, "share_no_release")) {
+    if (v != 0 && v != 1) return fail(KGPU_ERR_INVALID, "share_no_release must be 0 or 1");
+    w->dev.share_no_release = (int)v;
+    w->tables_dirty = true;
   } else {
     return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
   }
@@ -781,6 +813,10 @@ kgpu_status kgpu_world_get_option(kgpu_world w, const char* name, double* v)
   else if (!strcmp(name, "edge_chunk")) *v = w->edge_chunk;
   else if (!strcmp(name, "fp64_inline")) *v = w->fp64_inline;
   else if (!strcmp(name, "num_sms")) *v = w->num_sms;
+  else if (!strcmp(name, "pend_cap")) *v = w->pend_cap_opt;
+  else if (!strcmp(name, "spill_cap")) *v = w->spill_cap_opt;
+  else if (!strcmp(name, "share_wait_polls")) *v = w->dev.share_wait;
+  else if (!strcmp(name, "share_no_release")) *v = w->dev.share_no_release;
   else return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);
   return KGPU_OK;
 }
@@ -838,6 +874,14 @@ kgpu_status kgpu_fk(kgpu_world w, int32_t robot, const float* q, int32_t B, floa
   return launch_status(launch_fk(w->d_dev, robot, q, B, T, err, (cudaStream_t)s), "kgpu_fk");
 }
 
+kgpu_status kgpu_fk64(kgpu_world w, int32_t robot, const float* q, int32_t B, double* T, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (B < 0 || (B > 0 && (!q || !T))) return fail(KGPU_ERR_INVALID, "bad buffers");
+  return launch_status(launch_fk64(w->d_dev, robot, q, B, T, (cudaStream_t)s), "kgpu_fk64");
+}
+
 kgpu_status kgpu_check_configs(kgpu_world w, int32_t robot, const float* q, int32_t B,
                                uint8_t* env_hit, uint8_t* self_hit, kgpu_stream s)
 {
@@ -845,7 +889,7 @@ kgpu_status kgpu_check_configs(kgpu_world w, int32_t robot, const float* q, int3
   if (st) return st;
   if (B < 0 || (B > 0 && !q)) return fail(KGPU_ERR_INVALID, "bad buffers");
   if (!env_hit && !self_hit) return KGPU_OK;
-  return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
+  return launch_status(launch_check_configs(w->d_dev, engine_scratch(w, w->scratch), robot, nullptr, q, w->robots[robot]->nlinks, B,
                                             env_hit, self_hit, nullptr, grid_blocks(w), w->blocks_per_sm,
                                             (cudaStream_t)s, w->grab, w->job_flush, w->fp64_inline),
                        "kgpu_check_configs");
@@ -866,7 +910,7 @@ kgpu_status kgpu_check_configs_multi(kgpu_world w, const int32_t* robot_ids, con
   // the edge permutation buffer holds the robot-sorted order (grown on demand)
   st = ensure_edge_scratch(w, B);
   if (st) return st;
-  return launch_status(launch_check_configs(w->d_dev, w->scratch, -1, robot_ids, q, q_stride, B, env_hit, self_hit,
+  return launch_status(launch_check_configs(w->d_dev, engine_scratch(w, w->scratch), -1, robot_ids, q, q_stride, B, env_hit, self_hit,
                                             nullptr, grid_blocks(w), w->blocks_per_sm, (cudaStream_t)s, w->grab,
                                             w->job_flush, w->fp64_inline, (int)w->robots.size(), w->d_status),
                        "kgpu_check_configs_multi");
@@ -878,7 +922,7 @@ kgpu_status kgpu_is_feasible(kgpu_world w, int32_t robot, const float* q, int32_
   kgpu_status st = check_world(w, robot);
   if (st) return st;
   if (B < 0 || (B > 0 && (!q || !feasible))) return fail(KGPU_ERR_INVALID, "bad buffers");
-  return launch_status(launch_check_configs(w->d_dev, w->scratch, robot, nullptr, q, w->robots[robot]->nlinks, B,
+  return launch_status(launch_check_configs(w->d_dev, engine_scratch(w, w->scratch), robot, nullptr, q, w->robots[robot]->nlinks, B,
                                             nullptr, nullptr, feasible, grid_blocks(w), w->blocks_per_sm,
                                             (cudaStream_t)s, w->grab, w->job_flush, w->fp64_inline),
                        "kgpu_is_feasible");
@@ -891,7 +935,7 @@ kgpu_status kgpu_check_edges(kgpu_world w, int32_t robot, const float* qa, const
   if (st) return st;
   if (E < 0 || (E > 0 && (!qa || !qb || !nsteps || !first_hit))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if ((st = ensure_edge_scratch(w, E))) return st;
-  return launch_status(launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
+  return launch_status(launch_check_edges(w->d_dev, w->d_status, engine_scratch(w, w->scratch), robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
                                           w->blocks_per_sm, (cudaStream_t)s, w->grab, w->job_flush, w->edge_chunk,
                                           w->fp64_inline),
                        "kgpu_check_edges");
@@ -937,13 +981,13 @@ kgpu_status kgpu_self_distance(kgpu_world w, int32_t robot, const float* q, int3
   if (st) return st;
   if (B < 0 || (B > 0 && (!q || !d || !pair || !cp))) return fail(KGPU_ERR_INVALID, "bad buffers");
   if (!(cutoff > 0) || !(cutoff < 1e30)) return fail(KGPU_ERR_INVALID, "cutoff must be positive and finite");
-  return launch_status(launch_self_distance(w->d_dev, robot, q, B, cutoff, d, pair, cp, grad, nullptr, w->num_sms,
+  return launch_status(launch_self_distance(w->d_dev, robot, q, B, cutoff, d, pair, cp, grad, nullptr, 0, w->num_sms,
                                             (cudaStream_t)s),
                        "kgpu_self_distance");
 }
 
 kgpu_status kgpu_self_pair_distances(kgpu_world w, int32_t robot, const float* q, int32_t B, double cutoff,
-                                     double* dpair, kgpu_stream s)
+                                     int32_t all_pairs, double* dpair, kgpu_stream s)
 {
   kgpu_status st = check_world(w, robot);
   if (st) return st;
@@ -951,7 +995,7 @@ kgpu_status kgpu_self_pair_distances(kgpu_world w, int32_t robot, const float* q
   if (w->robots[robot]->nlinks < 2) return B < 0 ? fail(KGPU_ERR_INVALID, "bad buffers") : KGPU_OK;  // no pairs
   if (B < 0 || (B > 0 && (!q || !dpair))) return fail(KGPU_ERR_INVALID, "bad buffers");
   return launch_status(launch_self_distance(w->d_dev, robot, q, B, cutoff, nullptr, nullptr, nullptr, nullptr, dpair,
-                                            w->num_sms, (cudaStream_t)s),
+                                            all_pairs, w->num_sms, (cudaStream_t)s),
                        "kgpu_self_pair_distances");
 }
 
@@ -1122,7 +1166,7 @@ kgpu_status kgpu_edge_plan_create(kgpu_world w, int32_t robot, const float* qa, 
   p->world = w;
   cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaError_t le = launch_check_edges(w->d_dev, w->d_status, w->scratch, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
+    cudaError_t le = launch_check_edges(w->d_dev, w->d_status, engine_scratch(w, w->scratch), robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
                                         w->blocks_per_sm, cs, w->grab, w->job_flush, w->edge_chunk, w->fp64_inline);
     e = cudaStreamEndCapture(cs, &p->graph);
     if (e == cudaSuccess && le != cudaSuccess) e = le;

@@ -87,6 +87,7 @@ static_assert(sizeof(float) * 12 % 16 == 0, "link rows of WarpSmem::T stay 16-by
 struct BlockShare {
   int idle;
   int flag[kWarps];
+  int no_release;  // failure-path test switch (KWorldDev::share_no_release)
 };
 constexpr int kDonateMin = 32;     // stack entries a warp needs before it shares
 constexpr int kShareSpins = 1 << 20;  // bound on a waiting warp's polls (~0.3 s)
@@ -404,7 +405,7 @@ __device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, in
       if (w != me && *((volatile int*)&B.flag[w]) == 0 && atomicCAS(&B.flag[w], 0, 3) == 0) t = w;
   }
   t = __shfl_sync(0xffffffffu, t, 0);
-  if (t < 0) return 0;
+  if (t < 0 || B.no_release) return 0;  // (test switch: claimed, never handed over, entries kept)
   WarpSmem& S = all[me];
   WarpSmem& D = all[t];
   const int h = top / 2;
@@ -620,6 +621,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
   if (threadIdx.x == 0) {
     B.idle = 0;
     for (int w = 0; w < kWarps; ++w) B.flag[w] = 2;
+    B.no_release = W->share_no_release;
   }
   __syncthreads();
   // configurations of one robot go in groups of G = 32 / L (L = its link
@@ -898,7 +900,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           if (__shfl_sync(0xffffffffu, old, 0) == 0) break;  // left: no longer claimable
           continue;  // claimed meanwhile: the hand-over is in progress
         }
-      } else if (++waits > kShareSpins) {
+      } else if (++waits > (W->share_wait > 0 ? W->share_wait : kShareSpins)) {
         // a hand-over that does not complete: report it and stop
         if (lane == 0) set_status(W->status, KGPU_ERR_TIMEOUT);
         break;
@@ -1314,6 +1316,32 @@ __global__ void k_fk(const KWorldDev* __restrict__ W, int robot, const float* q,
   }
 }
 
+// Canonical FP64 forward kinematics (the transforms every FP64 decision of
+// the engine uses), one warp per configuration, lane i link i by the
+// sequential chain root -> i (bit-identical to the composition in link
+// order).
+__global__ void k_fk64(const KWorldDev* __restrict__ W, int robot, const float* q, int B, double* T)
+{
+  __shared__ double qs[8][kMaxLinks];
+  const int lane = threadIdx.x & 31, wib = (threadIdx.x >> 5) & 7;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  if (warp >= B) return;
+  const KRobotDev& R = W->robots[robot];
+  const int nl = R.nlinks;
+  const float qv = lane < nl ? q[(size_t)warp * nl + lane] : 0.f;
+  if (__any_sync(0xffffffffu, lane < nl && !(fabsf(qv) < 1.0e6f))) {
+    if (lane == 0) set_status(W->status, KGPU_ERR_NOT_FINITE);
+    return;
+  }
+  if (lane < nl) qs[wib][lane] = (double)qv;
+  __syncwarp();
+  if (lane < nl) {
+    double Tl[12];
+    chain64(R, qs[wib], lane, Tl);
+    for (int i = 0; i < 12; ++i) T[((size_t)warp * nl + lane) * 12 + i] = Tl[i];
+  }
+}
+
 // Full Jacobian of a point on a link, one warp per configuration: rows 0-2
 // the angular part (column j = world axis of joint j for a revolute ancestor,
 // 0 otherwise), rows 3-5 the linear part (w_j x (p - o_j) revolute, w_j
@@ -1449,6 +1477,15 @@ cudaError_t launch_fk(const KWorldDev* W, int robot, const float* q, int B, floa
   long long warps = B;
   int blocks = (int)((warps * 32 + threads - 1) / threads);
   k_fk<<<blocks, threads, 0, s>>>(W, robot, q, B, T, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fk64(const KWorldDev* W, int robot, const float* q, int B, double* T, cudaStream_t s)
+{
+  if (B <= 0) return cudaSuccess;
+  const int threads = 256;
+  const int blocks = (int)(((long long)B * 32 + threads - 1) / threads);
+  k_fk64<<<blocks, threads, 0, s>>>(W, robot, q, B, T);
   return cudaGetLastError();
 }
 

@@ -120,6 +120,12 @@ struct KWorldDev {
   // an optional additional inflation (world option, default 0)
   float eps_env;
   float eps_extra;
+  // work sharing of the edge engine: polls a warp waits for a claimed
+  // hand-over before it reports KGPU_ERR_TIMEOUT (0: the default bound), and
+  // a failure-path test switch under which a donor claims a waiting warp but
+  // never hands work over (it keeps its entries, so no work is lost)
+  int share_wait;
+  int share_no_release;
   // diagnostics
   int* status;               // device status word
   unsigned long long* stats; // kgpu_stats counters
@@ -224,6 +230,11 @@ struct kgpu_world_s {
   int job_flush = 64;      // triangle-pair jobs collected before testing them (8..64)
   int edge_chunk = 16;     // consecutive steps of an edge per work item (1..64)
   int fp64_inline = -1;    // FP64 triangle tests inline (1) or deferred to k_band (0); -1: deferred
+  // caps below the allocated scratch (0 = none): the undecided-pair list and
+  // the traversal spill stack per warp; they exist to drive the list-overflow
+  // fallback pass and spill exhaustion in tests
+  int pend_cap_opt = 0;
+  int spill_cap_opt = 0;
   int num_sms = 0;
   bool tables_dirty = true;
   // pinned staging for the host-buffer entry points
@@ -262,6 +273,7 @@ cudaError_t launch_check_edges(const KWorldDev* Wd, int* status, const Scratch& 
                                const float* qa, const float* qb, const int* nsteps, int E,
                                int* first_hit, int blocks, int per_sm, cudaStream_t s,
                                int grab = 0, int job_flush = 0, int chunk = 0, int fp64_inline = -1);
+cudaError_t launch_fk64(const KWorldDev* Wd, int robot, const float* q, int B, double* T, cudaStream_t s);
 cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q, int B,
                                    uint8_t* env_hit, uint8_t* self_hit, cudaStream_t s);
 cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,
@@ -277,11 +289,19 @@ cudaError_t launch_jacobian(const KWorldDev* W, int robot, const float* q, const
 cudaError_t launch_raycast(const KWorldDev* Wd, const float* s, const float* d, int R, int* obj, int* tri,
                            double* t, double* point, cudaStream_t st);
 cudaError_t dist_init();
+// loads kgpu_check_edges_noalloc's static array on the current device and
+// caches its address (kgpu_noalloc.cu)
+cudaError_t noalloc_prepare();
+// the world's scratch with its optional test caps applied (kgpu_api.cu)
+Scratch engine_scratch(kgpu_world w, Scratch S);
 cudaError_t launch_distance(const KWorldDev* Wd, const Scratch& S, int robot, const float* q, int B,
                             double cutoff, double* d, int* pair, double* cp, float* grad, int num_sms,
                             cudaStream_t s);
+// dpair != null: per-pair mode; all_pairs: every pair whose links have
+// geometry instead of the enabled self pairs
 cudaError_t launch_self_distance(const KWorldDev* Wd, int robot, const float* q, int B, double cutoff, double* d,
-                                 int* pair, double* cp, float* grad, double* dpair, int num_sms, cudaStream_t s);
+                                 int* pair, double* cp, float* grad, double* dpair, int all_pairs, int num_sms,
+                                 cudaStream_t s);
 // work: 2*T*Wn + T doubles of device scratch
 cudaError_t launch_softmin(const KWorldDev* Wd, const Scratch& S, int robot, const float* q, int T,
                            int Wn, double tau, double* L, float* dLdq, int nl, double* work,

@@ -9,21 +9,27 @@
 // (kgpu_check_edges) grows its permutation table on demand; this variant
 // instead works entirely inside one fixed, file-scope device array.
 //
-// The array (kNoAllocBytes, 20 MiB) holds the work-queue heads, the edge
+// The array (kNoAllocBytes, 32 MiB) holds the work-queue heads, the edge
 // ordering tables for at most KGPU_NOALLOC_MAX_EDGES edges, the list of
 // triangle pairs left to the FP64 re-test (65,536 entries; a longer list
-// makes a fallback pass re-check every step), and per-warp
-// regions (FP64 link transforms + a 1,024-entry traversal spill stack) for
-// one block of 8 warps per SM.  Every GPU that loads the library keeps this
-// array until the process exits.
+// makes a fallback pass re-check every step, so results stay exact), and
+// per-warp regions (FP64 link transforms + a 1,024-entry traversal spill
+// stack) for up to 2,560 warps: the world's blocks per SM on GPUs of up to
+// 160 SMs at two 8-warp blocks per SM (GB300: 152 SMs).  A world tuned for
+// more resident blocks per SM runs here with as many as the array serves.
+// Every GPU that loads the library keeps this array until the process exits.
 //
-// Set-up: the first call on a device, with that device current, looks up the
+// Set-up: kgpu_world_create, with the world's device current, looks up the
 // array's device address with cudaGetSymbolAddress (a host variable name is
-// not a device address) and caches it per device; make that first call
-// before any stream capture.  All calls share the array, and each call clears
-// what must start at zero (queue heads, histogram, counters) on its stream, so
-// calls that overlap on the GPU — on different streams, or from several host
-// threads — race on the array and must be serialised by the caller.
+// not a device address; the lookup also loads the module that holds the
+// array, which allocates it) and caches it per device, so the entry point
+// itself neither loads nor allocates anything.  A call on a device where no
+// world was created does that look-up itself on its first call; make that
+// first call before any stream capture.  All calls share the array, and each
+// call clears what must start at zero (queue heads, histogram, counters) on
+// its stream, so calls that overlap on the GPU — on different streams, or
+// from several host threads — race on the array and must be serialised by
+// the caller.
 #include <mutex>
 
 #include "kgpu_internal.h"
@@ -36,9 +42,9 @@ int engine_scratch_doubles();
 
 namespace {
 
-constexpr size_t kNoAllocBytes = 20u << 20;
+constexpr size_t kNoAllocBytes = 32u << 20;
 constexpr int kNoAllocSpill = 1024;   // traversal spill entries per warp
-constexpr int kNoAllocMaxWarps = 1536;
+constexpr int kNoAllocMaxWarps = 2560;
 constexpr int kNoAllocPend = 1 << 16;  // triangle pairs left to the FP64 re-test
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
@@ -69,7 +75,35 @@ Layout layout()
 std::mutex g_mu;
 void* g_addr[256] = {};  // per device
 
+// the array's device address on the current device, looked up once
+cudaError_t scratch_address(unsigned char** base)
+{
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 256) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (!g_addr[dev]) {
+    void* p = nullptr;
+    if ((e = cudaGetSymbolAddress(&p, g_noalloc_scratch)) != cudaSuccess) return e;
+    if (!p) return cudaErrorInvalidSymbol;
+    g_addr[dev] = p;
+  }
+  *base = (unsigned char*)g_addr[dev];
+  return cudaSuccess;
+}
+
 }  // namespace
+
+namespace kgpu {
+// Called by kgpu_world_create on the world's device: loads the array and
+// caches its address, so that kgpu_check_edges_noalloc allocates nothing.
+cudaError_t noalloc_prepare()
+{
+  unsigned char* base = nullptr;
+  return scratch_address(&base);
+}
+}  // namespace kgpu
 
 extern "C" kgpu_status kgpu_check_edges_noalloc(kgpu_world w, int32_t robot, const float* qa, const float* qb,
                                                 const int32_t* nsteps, int32_t E, int32_t* first_hit,
@@ -96,20 +130,15 @@ extern "C" kgpu_status kgpu_check_edges_noalloc(kgpu_world w, int32_t robot, con
   const Layout L = layout();
   if (L.end > kNoAllocBytes)
     return record_error(KGPU_ERR_UNSUPPORTED, "kgpu_check_edges_noalloc: scratch layout exceeds the static array");
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256)
-    return record_error(KGPU_ERR_CUDA, "kgpu_check_edges_noalloc: no current CUDA device");
+  const int warps = kgpu::engine_warps_per_block();
+  // the main pass runs per_sm blocks per SM; its FP64 fallback pass runs two
+  // per SM: both must fit the per-warp regions
+  if (2 * w->num_sms * warps > kNoAllocMaxWarps)
+    return record_error(KGPU_ERR_UNSUPPORTED,
+                        "kgpu_check_edges_noalloc: the static scratch serves GPUs of at most 160 SMs");
   unsigned char* base = nullptr;
-  {
-    std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-      void* p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p)
-        return record_error(KGPU_ERR_CUDA, "kgpu_check_edges_noalloc: cudaGetSymbolAddress of the scratch failed");
-      g_addr[dev] = p;
-    }
-    base = (unsigned char*)g_addr[dev];
-  }
+  if (scratch_address(&base) != cudaSuccess)
+    return record_error(KGPU_ERR_CUDA, "kgpu_check_edges_noalloc: cudaGetSymbolAddress of the scratch failed");
   kgpu::Scratch S;
   S.counters = (unsigned int*)(base + L.counters);
   S.edge_hist = (int*)(base + L.hist);
@@ -122,11 +151,14 @@ extern "C" kgpu_status kgpu_check_edges_noalloc(kgpu_world w, int32_t robot, con
   S.spill = (uint2*)(base + L.warps);
   S.spill_per_warp = L.per_warp_entries;
   S.max_warps = kNoAllocMaxWarps;
-  const int warps = kgpu::engine_warps_per_block();
-  int blocks = w->num_sms;  // one block of `warps` warps per SM
-  if (blocks * warps > kNoAllocMaxWarps) blocks = kNoAllocMaxWarps / warps;
-  cudaError_t e = kgpu::launch_check_edges(w->d_dev, w->d_status, S, robot, qa, qb, nsteps, E, first_hit, blocks,
-                                           w->blocks_per_sm, (cudaStream_t)stream);
+  S = kgpu::engine_scratch(w, S);  // the world's caps, if any, below the array's sizes
+  // the world's tuned launch shape, with as many blocks per SM as the
+  // per-warp regions serve
+  int per_sm = w->blocks_per_sm;
+  while (per_sm > 1 && w->num_sms * per_sm * warps > kNoAllocMaxWarps) --per_sm;
+  cudaError_t e = kgpu::launch_check_edges(w->d_dev, w->d_status, S, robot, qa, qb, nsteps, E, first_hit,
+                                           w->num_sms * per_sm, per_sm, (cudaStream_t)stream, w->grab, w->job_flush,
+                                           w->edge_chunk, w->fp64_inline);
   if (e != cudaSuccess) return record_error(KGPU_ERR_CUDA, cudaGetErrorString(e));
   return KGPU_OK;
 }

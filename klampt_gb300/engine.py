@@ -85,6 +85,83 @@ class Environment:
             self.handle = None
 
 
+class Geometry:
+    """A free triangle mesh (kgpu_geom) with its collision margin: the
+    engine side of a TriangleMesh Geometry3D.  Pair queries place two
+    geometries by a transform each, batched over transforms."""
+
+    def __init__(self, verts, tris, margin: float = 0.0):
+        v = np.ascontiguousarray(verts, np.float64).reshape(-1, 3)
+        f = np.ascontiguousarray(tris, np.int32).reshape(-1, 3)
+        d = _kgpu.GeomDesc(num_verts=len(v), verts=v.ctypes.data, num_tris=len(f), tris=f.ctypes.data,
+                           margin=float(margin))
+        h = ctypes.c_void_p()
+        check(lib().kgpu_geom_create(ctypes.byref(d), ctypes.byref(h)))
+        self.handle = h
+        self.num_tris = len(f)
+
+    def close(self):
+        if getattr(self, "handle", None):
+            lib().kgpu_geom_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_margin(self, margin: float):
+        check(lib().kgpu_geom_set_margin(self.handle, float(margin)))
+
+    def margin(self) -> float:
+        v = ctypes.c_double()
+        check(lib().kgpu_geom_get_margin(self.handle, ctypes.byref(v)))
+        return v.value
+
+    @staticmethod
+    def _transforms(Ta, Tb):
+        A = _dev(Ta, torch.float64).reshape(-1, 12).contiguous()
+        B = _dev(Tb, torch.float64).reshape(-1, 12).contiguous()
+        n = max(A.shape[0], B.shape[0])
+        flags = 0
+        if A.shape[0] == 1 and n > 1:
+            flags |= _kgpu.GEOM_FIXED_A
+        if B.shape[0] == 1 and n > 1:
+            flags |= _kgpu.GEOM_FIXED_B
+        if A.shape[0] not in (1, n) or B.shape[0] not in (1, n):
+            raise ValueError("transform batches must have equal sizes (or one transform)")
+        return A, B, n, flags
+
+    def collide(self, other: "Geometry", Ta, Tb, tol: float = 0.0, sync: bool = True) -> torch.Tensor:
+        """[B] uint8: 1 where this geometry at Ta[b] and `other` at Tb[b] are
+        within (margin + tol) + other.margin (touching counts).  Ta / Tb:
+        [B, 12] (R row-major, t) or one transform."""
+        A, B, n, flags = self._transforms(Ta, Tb)
+        hit = torch.empty(n, dtype=torch.uint8, device="cuda")
+        check(lib().kgpu_geom_collide(self.handle, other.handle, _dptr(A), _dptr(B), n, flags, float(tol),
+                                      _dptr(hit), _stream()))
+        if sync:
+            self.sync()
+        return hit
+
+    def distance(self, other: "Geometry", Ta, Tb, upper_bound: float = float("inf"), sync: bool = True):
+        """(d [B], cp [B, 6], elem [B, 2], dir [B, 3]) as kgpu_geom_distance."""
+        A, B, n, flags = self._transforms(Ta, Tb)
+        d = torch.empty(n, dtype=torch.float64, device="cuda")
+        cp = torch.empty((n, 6), dtype=torch.float64, device="cuda")
+        elem = torch.empty((n, 2), dtype=torch.int32, device="cuda")
+        dr = torch.empty((n, 3), dtype=torch.float64, device="cuda")
+        check(lib().kgpu_geom_distance(self.handle, other.handle, _dptr(A), _dptr(B), n, flags, float(upper_bound),
+                                       _dptr(d), _dptr(cp), _dptr(elem), _dptr(dr), _stream()))
+        if sync:
+            self.sync()
+        return d, cp, elem, dr
+
+    def sync(self):
+        check(lib().kgpu_geom_sync(self.handle, _stream()))
+
+
 class EdgePlan:
     """A captured CUDA graph of one edge-check batch over fixed device buffers."""
 
@@ -179,6 +256,17 @@ class World:
         if sync:
             self.sync()
         return (T, err) if with_error else T
+
+    def fk64(self, q, robot: int = 0, sync: bool = True) -> torch.Tensor:
+        """World transforms [B, L, 12] (FP64, R row-major, t) in the
+        canonical arithmetic the engine's FP64 decisions use."""
+        L = self.robots[robot].num_links
+        qd = _dev(q, torch.float32).reshape(-1, L).contiguous()
+        T = torch.empty((qd.shape[0], L, 12), dtype=torch.float64, device="cuda")
+        check(lib().kgpu_fk64(self.handle, robot, _dptr(qd), qd.shape[0], _dptr(T), _stream()))
+        if sync:
+            self.sync()
+        return T
 
     def check_configs(self, q, robot: int = 0, env: bool = True, self_collision: bool = True,
                       sync: bool = True):
@@ -283,15 +371,17 @@ class World:
             self.sync()
         return d, pair, cp, g
 
-    def self_pair_distances(self, q, cutoff: float, robot: int = 0, sync: bool = True):
-        """Every enabled self pair's own minimum distance: [B, L (L - 1) / 2]
-        in upper-triangle order (i < j), clamped at cutoff; -1 for pairs not
-        enabled."""
+    def self_pair_distances(self, q, cutoff: float, robot: int = 0, all_pairs: bool = False, sync: bool = True):
+        """Each self pair's own minimum distance: [B, L (L - 1) / 2] in
+        upper-triangle order (i < j), clamped at cutoff; -1 for pairs not
+        queried (the enabled self pairs, or with all_pairs every pair whose
+        links have geometry)."""
         L = self.robots[robot].num_links
         qd = _dev(q, torch.float32).reshape(-1, L).contiguous()
         B = qd.shape[0]
         out = torch.empty((B, L * (L - 1) // 2), dtype=torch.float64, device="cuda")
-        check(lib().kgpu_self_pair_distances(self.handle, robot, _dptr(qd), B, float(cutoff), _dptr(out), _stream()))
+        check(lib().kgpu_self_pair_distances(self.handle, robot, _dptr(qd), B, float(cutoff), int(all_pairs),
+                                             _dptr(out), _stream()))
         if sync:
             self.sync()
         return out

@@ -206,6 +206,13 @@ struct Ctx {
     std::fill(tri_ready.begin(), tri_ready.end(), 0);
     std::fill(vert_ready.begin(), vert_ready.end(), 0);
   }
+  // world transforms given directly (free geometries: one per link)
+  void set_transforms(const double* const* Ts)
+  {
+    for (int i = 0; i < R->L; ++i) std::memcpy(T[i], Ts[i], sizeof(T[i]));
+    std::fill(tri_ready.begin(), tri_ready.end(), 0);
+    std::fill(vert_ready.begin(), vert_ready.end(), 0);
+  }
   const double* link_tri(int l, int t)
   {
     if (!tri_ready[l]) {
@@ -235,16 +242,16 @@ struct Ctx {
 // 1e-9 m + margins so that culling never removes a pair the FP64 predicate
 // would accept.  lb < 0: environment group `grp`; else link lb.
 // ---------------------------------------------------------------------------
-bool bvtt_collide(Ctx& c, int la, int lb, int grp)
+bool bvtt_collide(Ctx& c, int la, int lb, int grp, double tol_extra = 0.0)
 {
   const Robot& R = *c.R;
-  const Env& E = *c.E;
   const Bvh& A = R.bvh[la];
   const int g = grp < 0 ? 0 : grp;  // a group only when lb < 0
-  const Bvh& B = lb >= 0 ? R.bvh[lb] : E.group_bvh[g];
+  const Bvh& B = lb >= 0 ? R.bvh[lb] : c.E->group_bvh[g];
   if (A.empty() || B.empty()) return false;
-  double mA = R.margins[la];
-  double mB = lb >= 0 ? R.margins[lb] : E.group_margin[g];
+  // (a link-link query may add a distance tolerance to the first margin)
+  double mA = tol_extra != 0.0 ? R.margins[la] + tol_extra : R.margins[la];
+  double mB = lb >= 0 ? R.margins[lb] : c.E->group_margin[g];
   double tol = 1e-9 + mA + mB;
   std::vector<std::pair<int, int>> st;
   st.reserve(256);
@@ -270,8 +277,8 @@ bool bvtt_collide(Ctx& c, int la, int lb, int grp)
         const double* P = c.link_tri(la, ta);
         for (int j = 0; j < nb.count; ++j) {
           int tb = B.order[nb.first + j];
-          const double* Q = lb >= 0 ? c.link_tri(lb, tb) : &E.tri[9 * (size_t)tb];
-          double m = mA + (lb >= 0 ? mB : E.margins[E.tri_obj[tb]]);
+          const double* Q = lb >= 0 ? c.link_tri(lb, tb) : &c.E->tri[9 * (size_t)tb];
+          double m = mA + (lb >= 0 ? mB : c.E->margins[c.E->tri_obj[tb]]);
           c.cnt.tri_pairs++;
           bool hit;
           if (m == 0.0) hit = kx_tri_tri_overlap(P, Q) != 0;
@@ -533,7 +540,7 @@ void feature_gradient(const Ctx& c, int l, const double* p, const double* u, dou
 // min over triangle pairs of kx_tri_tri_dist2, ties to the smallest
 // (triangle of i, triangle of j) in mesh order; only distances strictly
 // below `bound` are found.  No signed part: 0 when the surfaces meet.
-PairResult self_pair_distance(Ctx& c, int i, int j, double bound)
+PairResult self_pair_distance(Ctx& c, int i, int j, double bound, bool bound_check = true)
 {
   const Robot& R = *c.R;
   PairResult res;
@@ -597,7 +604,7 @@ PairResult self_pair_distance(Ctx& c, int i, int j, double bound)
   }
   if (!have) return res;
   double d = kx_sqrt(best2);
-  if (!(d < bound)) return res;
+  if (bound_check && !(d < bound)) return res;
   res.found = 1;
   res.d = d;
   res.ta = bta;
@@ -809,6 +816,13 @@ int orc_tri_tri(const double* P, const double* Q, double* d2, double* cp, double
   return kx_tri_tri_overlap(P, Q);
 }
 
+/* the canonical FP64 predicate over n pairs: out[i] = kx_tri_tri_overlap */
+int orc_tri_tri_batch(const double* P, const double* Q, int n, unsigned char* out)
+{
+  for (int i = 0; i < n; ++i) out[i] = (unsigned char)kx_tri_tri_overlap(P + 9 * (size_t)i, Q + 9 * (size_t)i);
+  return 0;
+}
+
 /* environment / self verdicts of B configurations; counters[3] =
  * {node pairs, triangle pairs, configurations} */
 int orc_check_configs(void* robot, void* env, const unsigned* masks, const float* q, int B,
@@ -983,6 +997,94 @@ int orc_pair_distance(void* robot, void* env, const float* q, int link, int obj,
   return pr.found;
 }
 
+/* The enabled (link, object) pairs of one configuration whose signed
+ * distance lies below `bound`, each with its deciding feature pair: out[5k..]
+ * = (link, object, feature a, feature b, signed-branch flag), in (link,
+ * object) order; dist[k] the pair's distance.  Returns the number of pairs
+ * (at most max_out are written).  Lets a test tell where a closest feature
+ * switches between nearby configurations (a kink of the distance). */
+int orc_pair_features(void* robot, void* env, const unsigned* masks, const float* q, double bound, int* out,
+                      double* dist, int max_out)
+{
+  Robot* R = (Robot*)robot;
+  Env* E = (Env*)env;
+  Ctx c;
+  c.init(R, E, masks);
+  double qd[ORC_MAXL];
+  for (int i = 0; i < R->L; ++i) qd[i] = (double)q[i];
+  c.set_config(qd);
+  int n = 0;
+  for (int l = 0; l < R->L; ++l) {
+    if (R->bvh[l].empty()) continue;
+    for (int o = 0; o < E->N; ++o) {
+      if (!pair_enabled(c, l, o)) continue;
+      if (link_obj_lb(c, l, o) > std::max(bound, 0.0) + 1e-9) continue;
+      PairResult pr = pair_distance(c, l, o, bound);
+      if (!pr.found) continue;
+      if (n < max_out) {
+        int* r = out + 5 * (size_t)n;
+        r[0] = l; r[1] = o; r[2] = pr.ta; r[3] = pr.tb; r[4] = pr.signed_pen;
+        dist[n] = pr.d;
+      }
+      ++n;
+    }
+  }
+  return n;
+}
+
+/* Free-geometry pair queries (the engine's kgpu_geom_collide /
+ * kgpu_geom_distance; Geometry3D::collides / withinDistance / distance_ext,
+ * Python/klampt/src/robotsim.cpp:1656-1690, 1782-1819).  `robot` is an oracle
+ * robot of two links: link 0 holds geometry a's mesh and margin, link 1
+ * geometry b's; their world transforms are Ta[b], Tb[b] (stride 0 under the
+ * fixed flags 1 / 2).  collide: the pair is within (m_a + tol) + m_b
+ * (tol = 0 and no margins: the triangles meet).  distance: d_mesh searched
+ * below max(upper + (m_a + m_b), 0) (accepting d^2 below the square of that
+ * bound, or 1e-300), reported as d_mesh - (m_a + m_b), else `upper`. */
+int orc_geom_collide(void* robot, const double* Ta, const double* Tb, int B, int flags, double tol, uint8_t* hit,
+                     int nthreads)
+{
+  Robot* R = (Robot*)robot;
+  if (R->L != 2) return -1;
+  parallel_for(B, nthreads, [&](int, int b0, int b1) {
+    Ctx c;
+    c.init(R, nullptr, nullptr);
+    for (int b = b0; b < b1; ++b) {
+      const double* Ts[2] = {Ta + ((flags & 1) ? 0 : 12 * (size_t)b), Tb + ((flags & 2) ? 0 : 12 * (size_t)b)};
+      c.set_transforms(Ts);
+      hit[b] = bvtt_collide(c, 0, 1, -1, tol) ? 1 : 0;
+    }
+  });
+  return 0;
+}
+
+int orc_geom_distance(void* robot, const double* Ta, const double* Tb, int B, int flags, double upper, double* d,
+                      double* cp, int* elem, double* dir, int nthreads)
+{
+  Robot* R = (Robot*)robot;
+  if (R->L != 2) return -1;
+  const double msum = R->margins[0] + R->margins[1];
+  const double bound = upper < 1e30 ? std::max(0.0, upper + msum) : HUGE_VAL;
+  parallel_for(B, nthreads, [&](int, int b0, int b1) {
+    Ctx c;
+    c.init(R, nullptr, nullptr);
+    for (int b = b0; b < b1; ++b) {
+      const double* Ts[2] = {Ta + ((flags & 1) ? 0 : 12 * (size_t)b), Tb + ((flags & 2) ? 0 : 12 * (size_t)b)};
+      c.set_transforms(Ts);
+      PairResult pr = self_pair_distance(c, 0, 1, bound, false);
+      d[b] = pr.found ? pr.d - msum : upper;
+      elem[2 * b] = pr.found ? pr.ta : -1;
+      elem[2 * b + 1] = pr.found ? pr.tb : -1;
+      for (int i = 0; i < 3; ++i) {
+        cp[6 * b + i] = pr.found ? pr.cp[i] : 0.0;
+        cp[6 * b + 3 + i] = pr.found ? pr.cq[i] : 0.0;
+        if (dir) dir[3 * b + i] = pr.found && pr.d > 0.0 ? (pr.cp[i] - pr.cq[i]) / pr.d : 0.0;
+      }
+    }
+  });
+  return 0;
+}
+
 /* minimum signed link-object distance of B configurations, clamped at
  * `cutoff`: d[B], pair[2B] (link, object or -1), cp[6B], grad[B*L] */
 int orc_min_distance(void* robot, void* env, const unsigned* masks, const float* q, int B,
@@ -1018,8 +1120,8 @@ int orc_min_distance(void* robot, void* env, const unsigned* masks, const float*
 
 /* soft-min of the signed distance over all (waypoint, link, object) pairs of
  * each trajectory: L = m - tau*log(sum exp(-(d-m)/tau)), m the trajectory's
- * minimum, summing pairs with d < m + 12 tau (a pair beyond contributes less
- * than e^-12 of the leading term and is left out by definition); dL/dq by the
+ * minimum, summing pairs with d < m + 30 tau (a pair beyond contributes less
+ * than e^-30 of the leading term and is left out by definition); dL/dq by the
  * chain rule through each pair's feature point.  q [T*W*L]; Lout [T]; grad
  * [T*W*L] or NULL. */
 int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, int T, int W,
@@ -1027,7 +1129,7 @@ int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, i
 {
   Robot* R = (Robot*)robot;
   Env* E = (Env*)env;
-  const double K = 12.0;
+  const double K = 30.0;
   parallel_for(T, nthreads, [&](int, int t0, int t1) {
     Ctx c;
     c.init(R, E, masks);
@@ -1330,13 +1432,14 @@ int orc_self_distance(void* robot, void* env, const float* q, int B, double cuto
   return 0;
 }
 
-/* Each enabled self pair's own minimum distance, clamped at the cutoff (the
+/* Each self pair's own minimum distance, clamped at the cutoff (the
    per-sample distances RandomizedSelfCollisionDistances reduces to per-pair
    minima and maxima, Cpp/Modeling/RandomizedSelfCollisions.cpp:142-180):
    dpair[b * P + i*L - i(i+1)/2 + (j-i-1)], P = L(L-1)/2; -1 for pairs not
-   queried. */
+   queried.  all_pairs: every pair whose links have geometry (that function's
+   pair set, :145-151); otherwise the enabled self pairs. */
 int orc_self_pair_distances(void* robot, void* env, const float* q, int B, double cutoff, double* dpair,
-                            int nthreads)
+                            int all_pairs, int nthreads)
 {
   Robot* R = (Robot*)robot;
   Env* E = (Env*)env;
@@ -1353,7 +1456,7 @@ int orc_self_pair_distances(void* robot, void* env, const float* q, int B, doubl
       for (int k = 0; k < P; ++k) out[k] = -1.0;
       for (int i = 0; i < L; ++i)
         for (int j = i + 1; j < L; ++j) {
-          if (!R->self_mask[i * L + j] || R->tloc[i].empty() || R->tloc[j].empty()) continue;
+          if ((!all_pairs && !R->self_mask[i * L + j]) || R->tloc[i].empty() || R->tloc[j].empty()) continue;
           PairResult pr = self_pair_distance(c, i, j, cutoff);
           out[i * L - i * (i + 1) / 2 + (j - i - 1)] = pr.found ? pr.d : cutoff;
         }

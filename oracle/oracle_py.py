@@ -22,10 +22,9 @@ _lib = None
 
 def build(force: bool = False) -> str:
     """Compiles the oracle (make in oracle/); returns the library path."""
-    src = os.path.join(HERE, "oracle.cpp")
-    hdr = os.path.join(HERE, "..", "include", "kgpu_exact.h")
-    stale = (not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(
-        os.path.getmtime(src), os.path.getmtime(hdr)))
+    srcs = [os.path.join(HERE, f) for f in ("oracle.cpp", "exact_tri.cpp", "Makefile")]
+    srcs.append(os.path.join(HERE, "..", "include", "kgpu_exact.h"))
+    stale = (not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < max(os.path.getmtime(f) for f in srcs))
     if force or stale:
         subprocess.run(["make", "-s", "-C", HERE, "-B" if force else "all"], check=True)
     return LIB_PATH
@@ -41,7 +40,8 @@ def lib():
         L.orc_env_create.restype = P
         for name in ("orc_check_configs", "orc_check_edges", "orc_is_feasible", "orc_pair_distance",
                      "orc_min_distance", "orc_softmin", "orc_tri_tri", "orc_raycast", "orc_jacobian", "orc_self_pairs", "orc_ik",
-                     "orc_indep_pairs", "orc_self_distance", "orc_self_pair_distances"):
+                     "orc_indep_pairs", "orc_self_distance", "orc_self_pair_distances", "orc_pair_features", "orc_tri_tri_batch",
+                     "orc_tri_tri_exact", "orc_geom_collide", "orc_geom_distance"):
             getattr(L, name).restype = ctypes.c_int
         L.orc_robot_destroy.argtypes = [P]
         L.orc_env_destroy.argtypes = [P]
@@ -166,6 +166,18 @@ class Oracle:
         return dict(found=bool(found), d=out[0], cp=out[1:4], cq=out[4:7], dir=out[7:10],
                     feat=feat[:2].copy(), signed=bool(feat[2]))
 
+    def pair_features(self, q, bound: float, max_pairs: int = 4096):
+        """Enabled (link, object) pairs of configuration q closer than
+        `bound`: int array [n, 5] of (link, object, feature a, feature b,
+        signed flag) and their distances [n]."""
+        q = np.ascontiguousarray(q, dtype=np.float32).reshape(self.nl)
+        out = np.zeros((max_pairs, 5), np.int32)
+        dist = np.zeros(max_pairs, np.float64)
+        n = lib().orc_pair_features(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(self.masks),
+                                    _p(q), ctypes.c_double(bound), _p(out), _p(dist), ctypes.c_int(max_pairs))
+        assert n <= max_pairs, n
+        return out[:n].copy(), dist[:n].copy()
+
     def min_distance(self, q, cutoff: float, nthreads: int = 1, want_grad=True):
         q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, self.nl)
         B = q.shape[0]
@@ -243,15 +255,17 @@ def self_distance(oracle: "Oracle", q, cutoff: float = 1e3, nthreads: int = 1):
     return d, pair, cp, g
 
 
-def self_pair_distances(oracle: "Oracle", q, cutoff: float = 1e3, nthreads: int = 1):
-    """Each enabled self pair's own minimum distance: [B, L (L - 1) / 2] in
-    upper-triangle order, clamped at cutoff; -1 for pairs not queried."""
+def self_pair_distances(oracle: "Oracle", q, cutoff: float = 1e3, nthreads: int = 1, all_pairs: bool = False):
+    """Each self pair's own minimum distance: [B, L (L - 1) / 2] in
+    upper-triangle order, clamped at cutoff; -1 for pairs not queried (the
+    enabled self pairs, or with all_pairs every pair with geometry)."""
     L = oracle.nl
     q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, L)
     B = q.shape[0]
     out = np.zeros((B, L * (L - 1) // 2), np.float64)
     lib().orc_self_pair_distances(ctypes.c_void_p(oracle.robot), ctypes.c_void_p(oracle.env), _p(q), ctypes.c_int(B),
-                                  ctypes.c_double(cutoff), _p(out), ctypes.c_int(nthreads))
+                                  ctypes.c_double(cutoff), _p(out), ctypes.c_int(int(all_pairs)),
+                                  ctypes.c_int(nthreads))
     return out
 
 
@@ -297,3 +311,84 @@ def tri_tri(P, Q):
     cq = np.zeros(3, np.float64)
     hit = lib().orc_tri_tri(_p(P), _p(Q), _p(d2), _p(cp), _p(cq))
     return bool(hit), float(d2[0]), cp, cq
+
+
+def tri_tri_batch(P, Q) -> np.ndarray:
+    """The canonical FP64 separating-axis predicate on n pairs [n, 9]."""
+    P = np.ascontiguousarray(P, np.float64).reshape(-1, 9)
+    Q = np.ascontiguousarray(Q, np.float64).reshape(-1, 9)
+    out = np.zeros(len(P), np.uint8)
+    lib().orc_tri_tri_batch(_p(P), _p(Q), ctypes.c_int(len(P)), _p(out))
+    return out
+
+
+def tri_tri_exact(P, Q, nthreads: int = 1) -> np.ndarray:
+    """Independent exact test (oracle/exact_tri.cpp: feasibility of the
+    barycentric system in integer arithmetic) on n pairs of integer
+    triangles [n, 9], |coordinate| <= 1024."""
+    P = np.ascontiguousarray(P, np.int32).reshape(-1, 9)
+    Q = np.ascontiguousarray(Q, np.int32).reshape(-1, 9)
+    out = np.zeros(len(P), np.uint8)
+    r = lib().orc_tri_tri_exact(_p(P), _p(Q), ctypes.c_int(len(P)), _p(out), ctypes.c_int(nthreads))
+    if r != 0:
+        raise ValueError("coordinates must be integers of magnitude <= 1024")
+    return out
+
+
+class GeomPairOracle:
+    """FP64 oracle of the free-geometry pair queries: a two-link oracle robot
+    holding geometry a (link 0) and geometry b (link 1) with their margins,
+    placed by the caller's transforms."""
+
+    def __init__(self, mesh_a, mesh_b, margin_a: float = 0.0, margin_b: float = 0.0):
+        Va, Fa = (np.asarray(x) for x in mesh_a)
+        Vb, Fb = (np.asarray(x) for x in mesh_b)
+        eye = np.array([1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0], np.float64)
+        self._keep = dict(
+            parents=np.array([-1, -1], np.int32), jt=np.array([2, 2], np.int32), T0=np.concatenate([eye, eye]),
+            axes=np.array([0, 0, 1, 0, 0, 1], np.float64), qmin=np.zeros(2), qmax=np.zeros(2),
+            vo=np.array([0, len(Va), len(Va) + len(Vb)], np.int32),
+            V=np.ascontiguousarray(np.concatenate([Va, Vb]), np.float64).reshape(-1),
+            to=np.array([0, len(Fa), len(Fa) + len(Fb)], np.int32),
+            F=np.ascontiguousarray(np.concatenate([Fa, Fb]), np.int32).reshape(-1),
+            m=np.array([margin_a, margin_b], np.float64))
+        k = self._keep
+        self.robot = lib().orc_robot_create(ctypes.c_int(2), _p(k["parents"]), _p(k["jt"]), _p(k["T0"]), _p(k["axes"]),
+                                            _p(k["qmin"]), _p(k["qmax"]), _p(k["vo"]), _p(k["V"]), _p(k["to"]),
+                                            _p(k["F"]), _p(k["m"]), None)
+
+    def close(self):
+        if self.robot:
+            lib().orc_robot_destroy(ctypes.c_void_p(self.robot))
+            self.robot = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def _tf(Ta, Tb):
+        A = np.ascontiguousarray(Ta, np.float64).reshape(-1, 12)
+        B = np.ascontiguousarray(Tb, np.float64).reshape(-1, 12)
+        n = max(len(A), len(B))
+        flags = (1 if len(A) == 1 and n > 1 else 0) | (2 if len(B) == 1 and n > 1 else 0)
+        return A, B, n, flags
+
+    def collide(self, Ta, Tb, tol: float = 0.0, nthreads: int = 1) -> np.ndarray:
+        A, B, n, flags = self._tf(Ta, Tb)
+        hit = np.zeros(n, np.uint8)
+        lib().orc_geom_collide(ctypes.c_void_p(self.robot), _p(A), _p(B), ctypes.c_int(n), ctypes.c_int(flags),
+                               ctypes.c_double(tol), _p(hit), ctypes.c_int(nthreads))
+        return hit
+
+    def distance(self, Ta, Tb, upper_bound: float = float("inf"), nthreads: int = 1):
+        A, B, n, flags = self._tf(Ta, Tb)
+        d = np.zeros(n, np.float64)
+        cp = np.zeros((n, 6), np.float64)
+        elem = np.zeros((n, 2), np.int32)
+        dr = np.zeros((n, 3), np.float64)
+        lib().orc_geom_distance(ctypes.c_void_p(self.robot), _p(A), _p(B), ctypes.c_int(n), ctypes.c_int(flags),
+                                ctypes.c_double(upper_bound), _p(d), _p(cp), _p(elem), _p(dr), ctypes.c_int(nthreads))
+        return d, cp, elem, dr

@@ -84,41 +84,6 @@ def test_softmin_matches_oracle(cfg2):
         assert _grad_close(G[t], G_o[t]), (t, np.abs(G[t] - G_o[t]).max(), np.abs(G_o[t]).max())
 
 
-def test_softmin_finite_differences(cfg2):
-    """Central differences of the GPU soft-min (FP64 distances), h = 1e-5,
-    against the adjoint gradient."""
-    robot, env, q, w, o = cfg2
-    qt = q[4:6].copy()
-    T, Wn, L = qt.shape
-    _, G = w.softmin(qt, 0.01)
-    G = G.cpu().numpy().astype(np.float64)
-    h = 1e-5
-    plus, minus, steps = [], [], []
-    for t in range(T):
-        for wp in range(Wn):
-            for j in range(L):
-                a = qt[t].copy()
-                b = qt[t].copy()
-                a[wp, j] = np.float32(qt[t, wp, j] + h)
-                b[wp, j] = np.float32(qt[t, wp, j] - h)
-                plus.append(a)
-                minus.append(b)
-                steps.append(float(a[wp, j]) - float(b[wp, j]))
-    Lp, _ = w.softmin(np.stack(plus), 0.01, want_grad=False)
-    Lm, _ = w.softmin(np.stack(minus), 0.01, want_grad=False)
-    fd = (Lp.cpu().numpy() - Lm.cpu().numpy()) / np.asarray(steps)
-    fd = fd.reshape(T, Wn, L)
-    ok = 0
-    total = 0
-    for t in range(T):
-        scale = max(np.abs(G[t]).max(), 1e-6)
-        err = np.abs(fd[t] - G[t]) / scale
-        ok += int((err <= GRAD_RTOL).sum())
-        total += err.size
-    # kinks (a closest feature switching inside +-h) may spoil a few entries
-    assert ok >= 0.95 * total, (ok, total)
-
-
 @pytest.mark.parametrize("which", ["arm", "dual_arm", "humanoid"])
 def test_self_distance_matches_oracle(built, which):
     """Link-link minimum distance over the enabled self pairs: closest pair
@@ -203,8 +168,9 @@ def test_self_distance_empty_and_errors(built):
 
 
 def test_self_pair_distances_matches_oracle(built):
-    """Every enabled pair's own minimum bit for bit, disabled pairs -1, and the
-    sampled per-pair minima and maxima of RandomizedSelfCollisionDistances."""
+    """Every queried pair's own minimum bit for bit (enabled pairs, and every
+    pair with geometry), unqueried pairs -1, and the sampled per-pair minima
+    and maxima of RandomizedSelfCollisionDistances."""
     from klampt_gb300.engine import World
     from klampt_gb300 import klampt as kl
     from oracle.oracle_py import Oracle, self_pair_distances
@@ -214,22 +180,26 @@ def test_self_pair_distances_matches_oracle(built):
     o = Oracle(robot, env)
     rng = np.random.default_rng(53)
     q = (sc.uniform_configs(robot, 128, rng) * rng.uniform(0, 1, (128, 1))).astype(np.float32)
-    for cutoff in (1e3, 0.2):
-        dp_o = self_pair_distances(o, q, cutoff=cutoff, nthreads=NT)
-        dp = w.self_pair_distances(q, cutoff).cpu().numpy()
-        assert np.array_equal(dp, dp_o), np.argwhere(dp != dp_o)[:5]
-    assert (dp_o == 0).any() and (dp_o == 0.2).any() and ((dp_o > 0) & (dp_o < 0.2)).any()
+    for all_pairs in (False, True):
+        for cutoff in (1e3, 0.2):
+            dp_o = self_pair_distances(o, q, cutoff=cutoff, nthreads=NT, all_pairs=all_pairs)
+            dp = w.self_pair_distances(q, cutoff, all_pairs=all_pairs).cpu().numpy()
+            assert np.array_equal(dp, dp_o), (all_pairs, np.argwhere(dp != dp_o)[:5])
+        assert (dp_o == 0).any() and (dp_o == 0.2).any() and ((dp_o > 0) & (dp_o < 0.2)).any()
+        assert (dp_o < 0).any() != all_pairs
     w.close()
     wm = kl.WorldModel([robot], env)
     lo, hi = kl.RandomizedSelfCollisionDistances(wm.robot(0), 64, seed=3)
     Q = kl._sample_configs(wm.robot(0), 64, np.random.default_rng(3))
-    ref = self_pair_distances(o, Q, cutoff=1e3, nthreads=NT)
+    ref = self_pair_distances(o, Q, cutoff=1e3, nthreads=NT, all_pairs=True)
     L = robot.num_links
     iu, ju = np.triu_indices(L, 1)
     ok = (ref >= 0).all(0)
-    assert np.array_equal(lo[iu[ok], ju[ok]], ref[:, ok].min(0))
-    assert np.array_equal(hi[iu[ok], ju[ok]], ref[:, ok].max(0))
-    assert np.isinf(lo[iu[~ok], ju[~ok]]).all()
+    assert ok.all()
+    assert np.array_equal(lo[iu, ju], ref.min(0)) and np.array_equal(lo[ju, iu], ref.min(0))
+    assert np.array_equal(hi[iu, ju], ref.max(0)) and np.array_equal(hi[ju, iu], ref.max(0))
+    assert (np.diag(lo) == 0).all() and (np.diag(hi) == 0).all()
+    wm.close()
 
 
 def test_self_min_distance_autograd(built):
