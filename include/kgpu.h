@@ -63,6 +63,7 @@ typedef struct kgpu_robot_s* kgpu_robot;
 typedef struct kgpu_env_s* kgpu_env;
 typedef struct kgpu_world_s* kgpu_world;
 typedef struct kgpu_edge_plan_s* kgpu_edge_plan;
+typedef struct kgpu_config_plan_s* kgpu_config_plan;
 typedef void* kgpu_stream; /* cudaStream_t; NULL selects the legacy default stream */
 
 /* Robot model: links in topological order (parent index < link index, -1 =
@@ -290,6 +291,12 @@ kgpu_status kgpu_check_configs_plain64(kgpu_world world, int32_t robot, const fl
 kgpu_status kgpu_check_edges_plain64(kgpu_world world, int32_t robot, const float* qa,
                                      const float* qb, const int32_t* nsteps, int32_t E,
                                      int32_t* first_hit, kgpu_stream stream);
+/* The plain FP64 method with one thread per (edge, step): every
+ * configuration of every edge checked on its own (no in-order early exit),
+ * the smallest infeasible step kept; same outputs as kgpu_check_edges. */
+kgpu_status kgpu_check_edges_plain64_steps(kgpu_world world, int32_t robot, const float* qa,
+                                           const float* qb, const int32_t* nsteps, int32_t E,
+                                           int32_t* first_hit, kgpu_stream stream);
 
 /* Minimum signed link-obstacle distance per configuration, clamped at
  * `cutoff`, with its gradient d/dq.  Replaces the per-pair
@@ -436,6 +443,20 @@ kgpu_status kgpu_edge_plan_create(kgpu_world world, int32_t robot, const float* 
                                   int32_t* first_hit, kgpu_edge_plan* out);
 kgpu_status kgpu_edge_plan_launch(kgpu_edge_plan plan, kgpu_stream stream);
 kgpu_status kgpu_edge_plan_destroy(kgpu_edge_plan plan);
+
+/* ---- captured configuration-batch plans (CUDA-graph replay) -------------- */
+/* The configuration-batch check of kgpu_check_configs (robot >= 0) or, with
+ * robot = -1, of kgpu_check_configs_multi (robot_ids, q_stride) recorded for
+ * fixed device buffers into a CUDA graph with the world's current launch
+ * options; each launch replays it on `stream`.  Replaces, per batch, the
+ * WorldPlannerSettings::CheckCollision / RobotModel::selfCollides loop
+ * (Cpp/Planning/PlannerSettings.cpp:269-331, robotsim.cpp:5529-5539).  As
+ * for edge plans: destroy plans before their world. */
+kgpu_status kgpu_config_plan_create(kgpu_world world, int32_t robot, const int32_t* robot_ids, const float* q,
+                                    int32_t q_stride, int32_t B, uint8_t* env_hit, uint8_t* self_hit,
+                                    kgpu_config_plan* out);
+kgpu_status kgpu_config_plan_launch(kgpu_config_plan plan, kgpu_stream stream);
+kgpu_status kgpu_config_plan_destroy(kgpu_config_plan plan);
 
 /* ---- diagnostics ------------------------------------------------------------ */
 /* Last error message of the calling thread ("" when none). */

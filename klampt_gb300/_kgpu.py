@@ -93,6 +93,7 @@ _SIGS = {
     "kgpu_check_edges": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
     "kgpu_check_configs_plain64": [_c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
     "kgpu_check_edges_plain64": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
+    "kgpu_check_edges_plain64_steps": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
     "kgpu_distance": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p, _c_p, _c_p, _c_p],
     "kgpu_self_distance": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p, _c_p, _c_p, _c_p],
     "kgpu_self_pair_distances": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _i32, _c_p, _c_p],
@@ -116,6 +117,9 @@ _SIGS = {
     "kgpu_edge_plan_create": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
     "kgpu_edge_plan_launch": [_c_p, _c_p],
     "kgpu_edge_plan_destroy": [_c_p],
+    "kgpu_config_plan_create": [_c_p, _i32, _c_p, _c_p, _i32, _i32, _c_p, _c_p, _c_p],
+    "kgpu_config_plan_launch": [_c_p, _c_p],
+    "kgpu_config_plan_destroy": [_c_p],
 }
 _STR_FUNCS = ("kgpu_last_error", "kgpu_version")
 

@@ -86,3 +86,10 @@ def tune_edges(world: World, qa, qb, nsteps, robot: int = 0, reps: int = 3,
 def tune_configs(world: World, q, robot: int = 0, reps: int = 3):
     qd = torch.as_tensor(q).cuda()
     return tune(world, lambda: world.check_configs(qd, robot=robot, sync=False), reps)
+
+
+def tune_configs_multi(world: World, robot_ids, q, reps: int = 3, prep: Optional[Callable[[], None]] = None):
+    """The grid on a heterogeneous batch (robot_ids [B], q [B, max links])."""
+    ids = torch.as_tensor(robot_ids).cuda()
+    qd = torch.as_tensor(q).cuda()
+    return tune(world, lambda: world.check_configs_multi(ids, qd, sync=False), reps, GRID, prep)

@@ -961,6 +961,19 @@ kgpu_status kgpu_check_edges_plain64(kgpu_world w, int32_t robot, const float* q
                        "kgpu_check_edges_plain64");
 }
 
+kgpu_status kgpu_check_edges_plain64_steps(kgpu_world w, int32_t robot, const float* qa, const float* qb,
+                                           const int32_t* nsteps, int32_t E, int32_t* first_hit, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (E < 0 || E == INT32_MAX || (E > 0 && (!qa || !qb || !nsteps || !first_hit)))
+    return fail(KGPU_ERR_INVALID, "bad buffers");
+  if ((st = ensure_edge_scratch(w, E + 1))) return st;  // the step offsets
+  return launch_status(launch_plain64_edge_steps(w->dev, robot, qa, qb, nsteps, E, first_hit, w->scratch.edge_perm,
+                                                 w->num_sms, (cudaStream_t)s),
+                       "kgpu_check_edges_plain64_steps");
+}
+
 kgpu_status kgpu_distance(kgpu_world w, int32_t robot, const float* q, int32_t B, double cutoff, double* d,
                           int32_t* pair, double* cp, float* grad, kgpu_stream s)
 {
@@ -1190,6 +1203,65 @@ kgpu_status kgpu_edge_plan_launch(kgpu_edge_plan p, kgpu_stream s)
 }
 
 kgpu_status kgpu_edge_plan_destroy(kgpu_edge_plan p)
+{
+  if (!p) return KGPU_OK;
+  if (p->exec) {
+    cudaGraphExecDestroy(p->exec);
+    p->world->live_plans--;
+  }
+  if (p->graph) cudaGraphDestroy(p->graph);
+  delete p;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_config_plan_create(kgpu_world w, int32_t robot, const int32_t* robot_ids, const float* q,
+                                    int32_t q_stride, int32_t B, uint8_t* env_hit, uint8_t* self_hit,
+                                    kgpu_config_plan* out)
+{
+  if (!out) return fail(KGPU_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (!w) return fail(KGPU_ERR_INVALID, "null world");
+  kgpu_status st = robot >= 0 ? check_world(w, robot) : refresh_tables(w);
+  if (st) return st;
+  if (B <= 0 || !q || (!env_hit && !self_hit) || (robot < 0 && !robot_ids))
+    return fail(KGPU_ERR_INVALID, "bad buffers");
+  int maxl = 0;
+  for (auto R : w->robots) maxl = std::max(maxl, R->nlinks);
+  if (robot >= 0) q_stride = w->robots[robot]->nlinks;
+  else if (q_stride < maxl) return fail(KGPU_ERR_INVALID, "q_stride %d < max links %d", q_stride, maxl);
+  if (robot < 0 && (st = ensure_edge_scratch(w, B))) return st;  // the robot-sorted order
+  cudaStream_t cs;
+  CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  kgpu_config_plan p = new kgpu_config_plan_s();
+  p->world = w;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e == cudaSuccess) {
+    cudaError_t le = launch_check_configs(w->d_dev, engine_scratch(w, w->scratch), robot, robot < 0 ? robot_ids : nullptr,
+                                          q, q_stride, B, env_hit, self_hit, nullptr, grid_blocks(w), w->blocks_per_sm,
+                                          cs, w->grab, w->job_flush, w->fp64_inline,
+                                          robot < 0 ? (int)w->robots.size() : 0, robot < 0 ? w->d_status : nullptr);
+    e = cudaStreamEndCapture(cs, &p->graph);
+    if (e == cudaSuccess && le != cudaSuccess) e = le;
+  }
+  if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+  cudaStreamDestroy(cs);
+  if (e != cudaSuccess) {
+    kgpu_config_plan_destroy(p);
+    return cuda_fail(e, "configuration plan capture");
+  }
+  w->live_plans++;
+  *out = p;
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_config_plan_launch(kgpu_config_plan p, kgpu_stream s)
+{
+  if (!p || !p->exec) return fail(KGPU_ERR_INVALID, "null plan");
+  CK(cudaGraphLaunch(p->exec, (cudaStream_t)s));
+  return KGPU_OK;
+}
+
+kgpu_status kgpu_config_plan_destroy(kgpu_config_plan p)
 {
   if (!p) return KGPU_OK;
   if (p->exec) {

@@ -255,6 +255,12 @@ struct kgpu_edge_plan_s {
   cudaGraphExec_t exec = nullptr;
 };
 
+struct kgpu_config_plan_s {
+  kgpu_world world = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
 namespace kgpu {
 // launchers implemented in the .cu files (return a CUDA error code).  The
 // engine kernels read the world descriptor from device memory (Wd); the
@@ -279,6 +285,10 @@ cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q
 cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,
                                  const float* qb, const int* nsteps, int E, int* first_hit,
                                  cudaStream_t s);
+// one thread per (edge, step); off: E + 1 ints of scratch
+cudaError_t launch_plain64_edge_steps(const KWorldDev& W, int robot, const float* qa, const float* qb,
+                                      const int* nsteps, int E, int* first_hit, int* off, int num_sms,
+                                      cudaStream_t s);
 cudaError_t launch_ik(const KWorldDev* W, int robot, int B, float* q, const int* links, int link_all,
                       const float* plocal, const float* ptarget, const float* Rtarget, int max_iters, float tol,
                       uint8_t* ok, float* residual, int* iters, cudaStream_t s);

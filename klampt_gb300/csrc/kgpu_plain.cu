@@ -2,7 +2,7 @@
 // for the batched engine.
 //
 // One thread per configuration (or per edge, stepping through its
-// configurations in order), FP64 forward kinematics, FP64 BVH-vs-BVH
+// configurations in order, or per (edge, step)), FP64 forward kinematics, FP64 BVH-vs-BVH
 // traversal with a per-thread stack, and the canonical FP64 triangle test on
 // every candidate pair.  No warp cooperation, no FP32 filter, no work queue:
 // this is the straightforward port of the reference's serial loops
@@ -179,7 +179,96 @@ __global__ void k_plain_edges(KWorldDev W, int robot, const float* qa, const flo
   first_hit[e] = hit;
 }
 
+// The plain method with one thread per (edge, step): every configuration
+// of every edge is checked independently (no in-order early exit), the
+// smallest infeasible step of each edge kept by atomicMin.  off[e] = number
+// of steps of the edges before e (one block, a chunked scan).
+__global__ void k_plain_step_offsets(const int* nsteps, int E, int* off, int* status)
+{
+  __shared__ int carry;
+  __shared__ int part[1024];
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < E; base += 1024) {
+    const int e = base + threadIdx.x;
+    const int n = e < E ? nsteps[e] : 0;
+    int own = e < E ? n + 1 : 0;
+    if (e < E && (n < 1 || n > kMaxSteps)) {
+      set_status(status, KGPU_ERR_INVALID);
+      own = 0;  // an invalid edge has no steps (its result stays -1)
+    }
+    part[threadIdx.x] = own;
+    __syncthreads();
+    for (int o = 1; o < 1024; o <<= 1) {  // inclusive scan (Hillis-Steele)
+      const int v = threadIdx.x >= o ? part[threadIdx.x - o] : 0;
+      __syncthreads();
+      part[threadIdx.x] += v;
+      __syncthreads();
+    }
+    if (e < E) off[e] = carry + part[threadIdx.x] - own;
+    __syncthreads();
+    if (threadIdx.x == 0) carry += part[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) off[E] = carry;
+}
+
+__global__ void k_plain_edge_steps(KWorldDev W, int robot, const float* qa, const float* qb, const int* nsteps,
+                                   int E, const int* off, int* first_hit)
+{
+  const KRobotDev& R = W.robots[robot];
+  const int nl = R.nlinks;
+  const int total = off[E];
+  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < total; s += gridDim.x * blockDim.x) {
+    int lo = 0, hi = E - 1;  // the edge e with off[e] <= s < off[e + 1]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (off[mid] <= s) lo = mid; else hi = mid - 1;
+    }
+    const int e = lo, k = s - off[e], n = nsteps[e];
+    double qd[kMaxLinks];
+    bool ok = true, finite = true;
+    for (int i = 0; i < nl; ++i) {
+      qd[i] = kx_interp((double)qa[(size_t)e * nl + i], (double)qb[(size_t)e * nl + i], k, n);
+      if (!(fabs(qd[i]) < 1.0e6)) finite = false;
+      if (qd[i] < R.qmin64[i] || qd[i] > R.qmax64[i]) ok = false;
+    }
+    if (!finite) { set_status(W.status, KGPU_ERR_NOT_FINITE); continue; }
+    if (!ok) { atomicMin(first_hit + e, k); continue; }
+    double T[kMaxLinks][12];
+    fk64_all(R, qd, T);
+    const int r = plain_config(W, R, T, true, true, true);
+    if (r & 4) { set_status(W.status, KGPU_ERR_OVERFLOW); continue; }
+    if (r) atomicMin(first_hit + e, k);
+  }
+}
+
+__global__ void k_plain_fill(int* a, int n, int v)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) a[i] = v;
+}
+
+__global__ void k_plain_unset(int* a, int n)
+{
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && a[i] == INT_MAX) a[i] = -1;
+}
+
 }  // namespace
+
+cudaError_t launch_plain64_edge_steps(const KWorldDev& W, int robot, const float* qa, const float* qb,
+                                      const int* nsteps, int E, int* first_hit, int* off, int num_sms,
+                                      cudaStream_t s)
+{
+  if (E <= 0) return cudaSuccess;
+  const int tb = 256, gb = (E + tb - 1) / tb;
+  k_plain_fill<<<gb, tb, 0, s>>>(first_hit, E, INT_MAX);
+  k_plain_step_offsets<<<1, 1024, 0, s>>>(nsteps, E, off, W.status);
+  k_plain_edge_steps<<<num_sms * 16, 64, 0, s>>>(W, robot, qa, qb, nsteps, E, off, first_hit);
+  k_plain_unset<<<gb, tb, 0, s>>>(first_hit, E);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_plain64_configs(const KWorldDev& W, int robot, const float* q, int B,
                                    uint8_t* env_hit, uint8_t* self_hit, cudaStream_t s)

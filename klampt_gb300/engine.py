@@ -189,6 +189,36 @@ class EdgePlan:
             pass
 
 
+class ConfigPlan:
+    """A captured CUDA graph of one configuration-batch check over fixed
+    device buffers (one robot, or robot_ids for a heterogeneous batch)."""
+
+    def __init__(self, world: "World", q: torch.Tensor, env_hit: torch.Tensor, self_hit: torch.Tensor,
+                 robot: int = 0, robot_ids: Optional[torch.Tensor] = None):
+        self.world = world
+        self._keep = (q, env_hit, self_hit, robot_ids)
+        h = ctypes.c_void_p()
+        B = env_hit.shape[0]
+        stride = q.shape[-1] if q.dim() > 1 else 0
+        check(lib().kgpu_config_plan_create(world.handle, -1 if robot_ids is not None else robot, _dptr(robot_ids),
+                                            _dptr(q), stride, B, _dptr(env_hit), _dptr(self_hit), ctypes.byref(h)))
+        self.handle = h
+
+    def launch(self):
+        check(lib().kgpu_config_plan_launch(self.handle, _stream()))
+
+    def close(self):
+        if self.handle:
+            lib().kgpu_config_plan_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class World:
     """An environment plus robots on the current CUDA device."""
 
@@ -325,17 +355,26 @@ class World:
             self.sync()
         return eh, sh
 
-    def check_edges_plain64(self, qa, qb, nsteps, robot: int = 0, sync: bool = True) -> torch.Tensor:
+    def check_edges_plain64(self, qa, qb, nsteps, robot: int = 0, sync: bool = True,
+                            per_step: bool = False) -> torch.Tensor:
+        """The plain FP64 method: one thread per edge (in order), or with
+        per_step one thread per (edge, step)."""
         L = self.robots[robot].num_links
         a = _dev(qa, torch.float32).reshape(-1, L)
         b = _dev(qb, torch.float32).reshape(-1, L)
         n = _dev(nsteps, torch.int32).reshape(-1)
         out = torch.empty(a.shape[0], dtype=torch.int32, device="cuda")
-        check(lib().kgpu_check_edges_plain64(self.handle, robot, _dptr(a), _dptr(b), _dptr(n), a.shape[0],
-                                             _dptr(out), _stream()))
+        fn = lib().kgpu_check_edges_plain64_steps if per_step else lib().kgpu_check_edges_plain64
+        check(fn(self.handle, robot, _dptr(a), _dptr(b), _dptr(n), a.shape[0], _dptr(out), _stream()))
         if sync:
             self.sync()
         return out
+
+    def config_plan(self, q: torch.Tensor, env_hit: torch.Tensor, self_hit: torch.Tensor, robot: int = 0,
+                    robot_ids: Optional[torch.Tensor] = None) -> ConfigPlan:
+        """A CUDA-graph plan of check_configs (or, with robot_ids, of
+        check_configs_multi) over these device buffers."""
+        return ConfigPlan(self, q, env_hit, self_hit, robot, robot_ids)
 
     def edge_plan(self, qa: torch.Tensor, qb: torch.Tensor, nsteps: torch.Tensor, first_hit: torch.Tensor,
                   robot: int = 0) -> EdgePlan:

@@ -264,7 +264,10 @@ def _rob_items(path: str) -> List[Tuple[str, List[str]]]:
         if not line:
             continue
         tok = shlex.split(line)
-        items.append((tok[0], tok[1:]))
+        # item names are case-insensitive: the reference lower-cases them
+        # (Cpp/Modeling/Robot.cpp:313), and its own generators write TParent,
+        # qMin, qMax (Python/klampt/model/create/moving_base_robot.py:30-39)
+        items.append((tok[0].lower(), tok[1:]))
     return items
 
 
@@ -499,6 +502,49 @@ def load_urdf(path: str, name: Optional[str] = None) -> RobotSpec:
     return RobotSpec(name=name or root.get("name", os.path.splitext(os.path.basename(path))[0]),
                      parents=parents, joint_types=jt, T0_parent=T0, axes=axes, qmin=qmin, qmax=qmax,
                      meshes=meshes, margins=np.zeros(L), self_mask=mask)
+
+
+def load_rigid_object(path: str) -> Tuple[Mesh, np.ndarray]:
+    """Loads a Klamp't rigid-object file (Cpp/Modeling/RigidObject.cpp:
+    34-125): `mesh` (a geometry file relative to the object file),
+    `geomscale` (1 or 3 values) and `geomtranslate` applied to the geometry,
+    and the object's transform `T` (12 values: R row-major then t, or a 4x4
+    row-major matrix) or `position`.  Returns (the mesh in the world frame,
+    T as 12 numbers R row-major then t); mass and contact items are not
+    read."""
+    base_dir = os.path.dirname(os.path.abspath(path))
+    items: Dict[str, List[str]] = {}
+    with open(path, "r") as f:
+        for line in f.read().splitlines():
+            line = line.split("#", 1)[0].strip()
+            if line:
+                tok = shlex.split(line)
+                items[tok[0]] = tok[1:]
+    if "mesh" not in items or len(items["mesh"]) != 1:
+        raise ValueError(f"{path}: a rigid object needs one 'mesh' item")
+    V, F = load_mesh(os.path.join(base_dir, items["mesh"][0]))
+    V = np.asarray(V, np.float64)
+    if "geomscale" in items:
+        sc = [float(x) for x in items["geomscale"]]
+        if len(sc) not in (1, 3):
+            raise ValueError(f"{path}: geomscale needs 1 or 3 values")
+        V = V * np.asarray(sc if len(sc) == 3 else sc * 3)
+    if "geomtranslate" in items:
+        V = V + np.asarray([float(x) for x in items["geomtranslate"]], np.float64)
+    T = np.array([1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0], np.float64)
+    if "T" in items:
+        v = [float(x) for x in items["T"]]
+        if len(v) == 12:
+            T = np.asarray(v, np.float64)
+        elif len(v) == 16:
+            M = np.asarray(v, np.float64).reshape(4, 4)
+            T = np.concatenate([M[:3, :3].reshape(-1), M[:3, 3]])
+        else:
+            raise ValueError(f"{path}: T needs 12 or 16 values")
+    if "position" in items:
+        T[9:] = [float(x) for x in items["position"]]
+    W = V @ T[:9].reshape(3, 3).T + T[9:]
+    return (W, np.asarray(F, np.int32)), T
 
 
 def load_robot(path: str) -> RobotSpec:

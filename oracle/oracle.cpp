@@ -664,6 +664,19 @@ MinResult min_distance(Ctx& c, double bound)
   return m;
 }
 
+// per-thread counters summed into counters[3] = {node pairs, triangle pairs,
+// items} (when given)
+void sum_counters(const std::vector<Counters>& cs, long long* counters)
+{
+  if (!counters) return;
+  counters[0] = counters[1] = counters[2] = 0;
+  for (const auto& x : cs) {
+    counters[0] += x.node_pairs;
+    counters[1] += x.tri_pairs;
+    counters[2] += x.items;
+  }
+}
+
 template <class F>
 void parallel_for(int n, int nthreads, F&& fn)
 {
@@ -1088,13 +1101,16 @@ int orc_geom_distance(void* robot, const double* Ta, const double* Tb, int B, in
 /* minimum signed link-object distance of B configurations, clamped at
  * `cutoff`: d[B], pair[2B] (link, object or -1), cp[6B], grad[B*L] */
 int orc_min_distance(void* robot, void* env, const unsigned* masks, const float* q, int B,
-                     double cutoff, double* d, int* pair, double* cp, double* grad, int nthreads)
+                     double cutoff, double* d, int* pair, double* cp, double* grad, int nthreads,
+                     long long* counters)
 {
   Robot* R = (Robot*)robot;
   Env* E = (Env*)env;
-  parallel_for(B, nthreads, [&](int, int b0, int b1) {
+  std::vector<Counters> cs(std::max(1, nthreads));
+  parallel_for(B, nthreads, [&](int t, int b0, int b1) {
     Ctx c;
     c.init(R, E, masks);
+    c.cnt.items += b1 - b0;
     double qd[ORC_MAXL];
     for (int b = b0; b < b1; ++b) {
       for (int i = 0; i < R->L; ++i) qd[i] = (double)q[(size_t)b * R->L + i];
@@ -1114,7 +1130,11 @@ int orc_min_distance(void* robot, void* env, const unsigned* masks, const float*
         if (g) feature_gradient(c, m.link, m.pr.cp, m.pr.dir, 1.0, g);
       }
     }
+    cs[t].node_pairs += c.cnt.node_pairs;
+    cs[t].tri_pairs += c.cnt.tri_pairs;
+    cs[t].items += c.cnt.items;
   });
+  sum_counters(cs, counters);
   return 0;
 }
 
@@ -1125,14 +1145,16 @@ int orc_min_distance(void* robot, void* env, const unsigned* masks, const float*
  * chain rule through each pair's feature point.  q [T*W*L]; Lout [T]; grad
  * [T*W*L] or NULL. */
 int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, int T, int W,
-                double tau, double* Lout, double* grad, int nthreads)
+                double tau, double* Lout, double* grad, int nthreads, long long* counters)
 {
   Robot* R = (Robot*)robot;
   Env* E = (Env*)env;
   const double K = 30.0;
-  parallel_for(T, nthreads, [&](int, int t0, int t1) {
+  std::vector<Counters> cs(std::max(1, nthreads));
+  parallel_for(T, nthreads, [&](int th, int t0, int t1) {
     Ctx c;
     c.init(R, E, masks);
+    c.cnt.items += (long long)(t1 - t0) * W;
     double qd[ORC_MAXL];
     for (int t = t0; t < t1; ++t) {
       // pass 1: the trajectory minimum (distances searched up to 1000 m)
@@ -1169,7 +1191,11 @@ int orc_softmin(void* robot, void* env, const unsigned* masks, const float* q, i
         for (size_t k = 0; k < g.size(); ++k) grad[(size_t)t * W * R->L + k] = g[k] / sum;
       }
     }
+    cs[th].node_pairs += c.cnt.node_pairs;
+    cs[th].tri_pairs += c.cnt.tri_pairs;
+    cs[th].items += c.cnt.items;
   });
+  sum_counters(cs, counters);
   return 0;
 }
 

@@ -178,7 +178,9 @@ class Oracle:
         assert n <= max_pairs, n
         return out[:n].copy(), dist[:n].copy()
 
-    def min_distance(self, q, cutoff: float, nthreads: int = 1, want_grad=True):
+    def min_distance(self, q, cutoff: float, nthreads: int = 1, want_grad=True, counts=None):
+        """(d, pair, cp, grad); `counts`, an int64 array of 3, receives the
+        canonical traversal's (node pairs, triangle pairs, configurations)."""
         q = np.ascontiguousarray(q, dtype=np.float32).reshape(-1, self.nl)
         B = q.shape[0]
         d = np.zeros(B, np.float64)
@@ -187,17 +189,18 @@ class Oracle:
         grad = np.zeros((B, self.nl), np.float64) if want_grad else None
         lib().orc_min_distance(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(self.masks),
                                _p(q), ctypes.c_int(B), ctypes.c_double(cutoff), _p(d), _p(pair),
-                               _p(cp), _p(grad), ctypes.c_int(nthreads))
+                               _p(cp), _p(grad), ctypes.c_int(nthreads), _p(counts))
         return d, pair, cp, grad
 
-    def softmin(self, q, tau: float, nthreads: int = 1, want_grad=True):
+    def softmin(self, q, tau: float, nthreads: int = 1, want_grad=True, counts=None):
+        """(L, dL/dq); `counts` as for min_distance (items = waypoints)."""
         q = np.ascontiguousarray(q, dtype=np.float32)
         T, W = q.shape[0], q.shape[1]
         Lout = np.zeros(T, np.float64)
         grad = np.zeros((T, W, self.nl), np.float64) if want_grad else None
         lib().orc_softmin(ctypes.c_void_p(self.robot), ctypes.c_void_p(self.env), _p(self.masks),
                           _p(q), ctypes.c_int(T), ctypes.c_int(W), ctypes.c_double(tau),
-                          _p(Lout), _p(grad), ctypes.c_int(nthreads))
+                          _p(Lout), _p(grad), ctypes.c_int(nthreads), _p(counts))
         return Lout, grad
 
 

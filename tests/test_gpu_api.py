@@ -292,3 +292,43 @@ def test_batched_ik_matches_oracle_iteration():
         both = np.nonzero((ok == 1) & (oko == 1))[0]
         assert np.median(np.abs(q[both] - qo[both]).max(axis=1)) < 1e-2
     w.close()
+
+
+def test_config_plans_replay_and_autotune():
+    """Configuration batches replayed as CUDA graphs: one robot, and the
+    four-robot heterogeneous batch autotuned first; every replay equals the
+    eager call and the oracle."""
+    import torch
+    from klampt_gb300 import autotune
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robots, env, (ids, q) = sc.scene_cfg3(total=2048, n_spheres=70, n_boxes=870)
+    w = World(env, robots)
+    best, table = autotune.tune_configs_multi(w, ids, q, reps=1)
+    assert set(best) == {"blocks_per_sm", "grab", "job_flush", "fp64_inline"} and len(table) == 36
+    ids_d, q_d = torch.as_tensor(ids).cuda(), torch.as_tensor(q).cuda()
+    eh = torch.empty(len(ids), dtype=torch.uint8, device="cuda")
+    sh = torch.empty(len(ids), dtype=torch.uint8, device="cuda")
+    plan = w.config_plan(q_d, eh, sh, robot_ids=ids_d)
+    e_ref, s_ref = (x.cpu().numpy() for x in w.check_configs_multi(ids, q))
+    for _ in range(3):
+        eh.fill_(7)
+        plan.launch()
+        w.sync()
+        assert np.array_equal(eh.cpu().numpy(), e_ref) and np.array_equal(sh.cpu().numpy(), s_ref)
+    for r, spec in enumerate(robots):
+        sel = np.flatnonzero(ids == r)
+        eo, so, _ = Oracle(spec, env).check_configs(q[sel, :spec.num_links], nthreads=NT)
+        assert np.array_equal(e_ref[sel], eo) and np.array_equal(s_ref[sel], so)
+    plan.close()
+    # one robot
+    q1 = torch.as_tensor(q[ids == 1, :robots[1].num_links]).contiguous().cuda()
+    e1 = torch.empty(q1.shape[0], dtype=torch.uint8, device="cuda")
+    s1 = torch.empty(q1.shape[0], dtype=torch.uint8, device="cuda")
+    p1 = w.config_plan(q1, e1, s1, robot=1)
+    p1.launch()
+    w.sync()
+    ea, sa = w.check_configs(q1, robot=1)
+    assert torch.equal(e1, ea) and torch.equal(s1, sa)
+    p1.close()
+    w.close()

@@ -180,6 +180,9 @@ def test_cfg1_edges_plain64_exact(cfg1):
     fh_o, _ = o.check_edges(qa[sel], qb[sel], ns[sel], nthreads=NT)
     fh = w.check_edges_plain64(qa[sel], qb[sel], ns[sel]).cpu().numpy()
     assert np.array_equal(fh, fh_o)
+    # one thread per (edge, step): the same first hits
+    fs = w.check_edges_plain64(qa[sel], qb[sel], ns[sel], per_step=True).cpu().numpy()
+    assert np.array_equal(fs, fh_o)
 
 
 def test_cfg1_edges_host_and_graph(cfg1):

@@ -152,9 +152,9 @@ def test_min_distance_full_terrain(built):
     assert np.allclose(cp[nz], cp_o[nz], rtol=0, atol=1e-9)
     bad = [b for b in range(len(q)) if not _grad_close(g[b], g_o[b])]
     assert not bad, bad[:8]
-    # the sample covers contacts and clamped configurations (among the 500
-    # boxes the closest obstacle is always a box)
-    assert (d_o <= 0).any() and (~hit).any()
+    # among the 500 boxes in the 2 m cube every configuration has an obstacle
+    # within the cutoff (most are in contact); the closest is always a box
+    assert (d_o < 0).any()
     # the terrain alone (links masked to group 1): every closest pair is the
     # 1M-triangle terrain, parity as above
     from oracle.oracle_py import default_masks
@@ -171,7 +171,8 @@ def test_min_distance_full_terrain(built):
     assert np.allclose(cp[nz], cp_o[nz], rtol=0, atol=1e-9)
     bad = [b for b in range(len(q)) if not _grad_close(g[b], g_o[b])]
     assert not bad, bad[:8]
-    assert (p_o[:, 1] == 0).sum() > 50 and nz.any()
+    # terrain pairs within the cutoff, and clamped configurations
+    assert (p_o[:, 1] == 0).sum() > 50 and nz.any() and (p_o[:, 0] < 0).any()
     w.close()
 
 

@@ -123,3 +123,56 @@ def test_urdf_tree_limits_and_geometry(tmp_path):
 def test_load_robot_dispatch(tmp_path):
     with pytest.raises(ValueError):
         mio.load_robot(str(tmp_path / "x.dae"))
+
+
+def test_rob_item_names_are_case_insensitive(tmp_path):
+    """The reference lower-cases item names (Cpp/Modeling/Robot.cpp:313); its
+    moving-base generator writes TParent, qMin, qMax
+    (Python/klampt/model/create/moving_base_robot.py:30-39)."""
+    mio.save_off(str(tmp_path / "c.off"), sc.box_mesh((0, 0, 0), (0.05, 0.05, 0.05)))
+    (tmp_path / "m.rob").write_text(
+        "### a floating base in the generator's spelling\n"
+        "TParent 1 0 0   0 1 0   0 0 1   0 0 0  \\\n"
+        "1 0 0   0 1 0   0 0 1   0 0 0  \\\n"
+        "1 0 0   0 1 0   0 0 1   0 0 0  \\\n"
+        "1 0 0   0 1 0   0 0 1   0 0 0  \\\n"
+        "1 0 0   0 1 0   0 0 1   0 0 0  \\\n"
+        "1 0 0   0 1 0   0 0 1   0 0 0\n"
+        "Parents -1 0 1 2 3 4\n"
+        "axis 1 0 0   0 1 0    0 0 1     0 0 1     0 1 0     1 0 0\n"
+        "JointType p p p r r r\n"
+        "qMin -1 -1 -1  -inf -inf -inf\n"
+        "qMax  1  1  1   inf  inf  inf\n"
+        "Geometry \"\" \"\" \"\" \"\" \"\" \"c.off\"\n")
+    r = mio.load_rob(str(tmp_path / "m.rob"))
+    assert r.num_links == 6 and r.parents.tolist() == [-1, 0, 1, 2, 3, 4]
+    assert r.joint_types.tolist() == [1, 1, 1, 0, 0, 0]
+    assert r.qmin.tolist()[:3] == [-1, -1, -1] and r.qmax.tolist()[:3] == [1, 1, 1]
+    assert np.isinf(r.qmin[3:]).all() and np.isinf(r.qmax[3:]).all()
+    assert len(r.meshes[5][1]) == 12 and all(len(m[1]) == 0 for m in r.meshes[:5])
+
+
+REF_OBJECTS = "/root/reference/tests/objects"
+
+
+@pytest.mark.skipif(not os.path.isdir(REF_OBJECTS), reason="the reference's test fixtures are not mounted")
+def test_reference_fixtures_known_answers():
+    """The reference's own test objects: cube.off (the unit cube) and
+    block.obj (a rigid object: cube.off scaled by 0.4, moved by -0.2 and
+    placed at (1, 0, 0.3), tests/test_ODERigidObject.cpp:17), with known
+    overlap and distance answers from the oracle's pair queries."""
+    from oracle.oracle_py import GeomPairOracle
+    V, F = mio.load_off(os.path.join(REF_OBJECTS, "cube.off"))
+    assert V.shape == (8, 3) and F.shape == (12, 3)
+    assert V.min(0).tolist() == [0, 0, 0] and V.max(0).tolist() == [1, 1, 1]
+    (W, Fb), T = mio.load_rigid_object(os.path.join(REF_OBJECTS, "block.obj"))
+    assert np.allclose(T[9:], [1.0, 0.0, 0.3]) and np.allclose(T[:9], np.eye(3).reshape(-1))
+    assert np.allclose(W.min(0), [0.8, -0.2, 0.1]) and np.allclose(W.max(0), [1.2, 0.2, 0.5])
+    I12 = np.array([1, 0, 0, 0, 1, 0, 0, 0, 1, 0, 0, 0], np.float64)
+    o = GeomPairOracle((V, F), (W, Fb))
+    offs = [-0.3, -0.2, -0.1, 0.0, 0.25]   # the unit cube moved along x
+    Ta = np.stack([np.concatenate([I12[:9], [x, 0, 0]]) for x in offs])
+    hit = o.collide(Ta, I12[None])
+    assert hit.tolist() == [0, 1, 1, 1, 1]   # x = -0.2 touches the block's face at 0.8
+    d, _, _, _ = o.distance(Ta, I12[None])
+    assert np.allclose(d, [0.1, 0, 0, 0, 0], atol=1e-12)
