@@ -59,8 +59,13 @@ def parse():
     p.add_argument("--edges", type=int, default=16384)
     p.add_argument("--engine-only", action="store_true",
                    help="only warm-up + timed edge-plan launches (profiling runs); prints the device time")
+    p.add_argument("--set", action="append", default=[], metavar="NAME=VALUE",
+                   help="world option for --engine-only runs (e.g. blocks_per_sm=2)")
     p.add_argument("--dist-only", type=int, default=0, metavar="N",
-                   help="only N minimum-distance+gradient evaluations on the soft-min scene (profiling runs)")
+                   help="only N minimum-distance+gradient evaluations (profiling runs)")
+    p.add_argument("--dist-scene", default="softmin", choices=["softmin", "terrain"],
+                   help="--dist-only scene: the soft-min waypoints (icospheres, cutoff 1000 m) or the terrain "
+                        "and boxes (cutoff 0.2 m)")
     return p.parse_args()
 
 
@@ -70,14 +75,19 @@ def run_dist_only(args):
     kbuild.build()
     from klampt_gb300 import scenes as sc
     from klampt_gb300.engine import World
-    robot, env, q = sc.scene_cfg2(T=(args.dist_only + 31) // 32, W=32)
+    if args.dist_scene == "terrain":
+        robot, env, q = sc.scene_cfg4(n_configs=args.dist_only)
+        cutoff = 0.2
+    else:
+        robot, env, q = sc.scene_cfg2(T=(args.dist_only + 31) // 32, W=32)
+        cutoff = 1e3
     w = World(env, [robot])
     qd = torch.as_tensor(q.reshape(-1, robot.num_links)[:args.dist_only]).cuda()
     for _ in range(max(1, args.warmup)):
-        w.distance(qd, 1e3)
+        w.distance(qd, cutoff)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        w.distance(qd, 1e3, sync=False)
+        w.distance(qd, cutoff, sync=False)
     w.sync()
     print(json.dumps({"dist_only": args.dist_only, "ms_per_step": 1e3 * (time.perf_counter() - t0) / max(1, args.steps)}))
 
@@ -501,6 +511,9 @@ def main():
         # before each repetition as before each timed step
         ta, tb, tn = sc.random_edges(robot, args.edges, np.random.default_rng(2001))
         tuned, _ = autotune.tune_edges(w, ta, tb, tn, reps=3, prep=flush.zero_)
+    for kv in args.set:
+        k, v = kv.split("=", 1)
+        w.set_option(k, float(v))
     out = torch.empty(args.edges, dtype=torch.int32, device="cuda")
     plan = w.edge_plan(a, b, n, out)
     stream = torch.cuda.current_stream()

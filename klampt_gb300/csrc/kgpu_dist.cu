@@ -415,7 +415,15 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
     const float ed = dl + de + 32.f * kU * (fabsf(ob.a.x) + fabsf(ob.a.y) + fabsf(ob.a.z) + fabsf(ob.b.x) +
                                            fabsf(ob.b.y) + fabsf(ob.b.z) + 1.f);
     float lmax = -FLT_MAX;
-    // pass 1: FP32 depths, lane-local maximum
+    // pass 1: FP32 depths, lane-local maximum.  Each lane also keeps the (at
+    // most two) vertices whose pass-1 value lies within 2 ed of its running
+    // maximum: pass 1's value bounds a vertex's full FP32 minimum from
+    // above, and the global maximum is at least the lane's, so every vertex
+    // that pass 2 can accept is among them, unless more than two qualified
+    // (then the lane rescans all of its vertices)
+    int cv0 = 0, cv1 = 0, nc = 0;
+    float cd0 = 0.f, cd1 = 0.f;
+    bool rescan = false;
     for (int v = lane; v < vc; v += 32) {
       const float4 x = __ldg(W->lvert32 + vf + v);
       const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
@@ -431,6 +439,17 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
         dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
       }
       lmax = fmaxf(lmax, dmin);
+      const float thr = lmax - 2.f * ed;
+      if (dmin > -ed && dmin >= thr) {
+        if (nc == 2 && cd1 < thr) nc = 1;
+        if (nc >= 1 && cd0 < thr) {
+          if (nc == 2) { cv0 = cv1; cd0 = cd1; }
+          --nc;
+        }
+        if (nc == 0) { cv0 = v; cd0 = dmin; nc = 1; }
+        else if (nc == 1) { cv1 = v; cd1 = dmin; nc = 2; }
+        else rescan = true;
+      }
     }
     const float gmax = -warp_min(-lmax);
     if (gmax > -ed) {
@@ -438,19 +457,19 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
       // pass 2: FP64 depth of every vertex within the band of the deepest
       double bd = 0.0;
       int bv = INT_MAX, bf = -1;
-      for (int v = lane; v < vc; v += 32) {
+      auto depth64 = [&](int v) {
         const float4 x = __ldg(W->lvert32 + vf + v);
         const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
         if (fabsf(w.x - ob.a.x) > ob.b.x + tolb || fabsf(w.y - ob.a.y) > ob.b.y + tolb ||
             fabsf(w.z - ob.a.z) > ob.b.z + tolb)
-          continue;
+          return;
         const float stop = fmaxf(gmax - 2.f * ed, -ed);
         float dmin = FLT_MAX;
         for (int f = ff; f < ff + fc && dmin >= stop; ++f) {
           const float4 pl = __ldg(W->eface32 + f);
           dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
         }
-        if (dmin < gmax - 2.f * ed || dmin <= -ed) continue;
+        if (dmin < gmax - 2.f * ed || dmin <= -ed) return;
         double w64[3];
         kx_xform_point(T64[l], W->lvert64 + 3 * (size_t)(vf + v), w64);
         double dm = DBL_MAX;
@@ -462,6 +481,12 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
           if (dep < dm || (dep == dm && orig < fo)) { dm = dep; fm = f; fo = orig; }
         }
         if (dm > bd || (dm == bd && dm > 0.0 && v < bv)) { bd = dm; bv = v; bf = fm; }
+      };
+      if (rescan) {
+        for (int v = lane; v < vc; v += 32) depth64(v);
+      } else {
+        if (nc >= 1 && cd0 >= gmax - 2.f * ed) depth64(cv0);
+        if (nc >= 2 && cd1 >= gmax - 2.f * ed) depth64(cv1);
       }
       // warp maximum of (depth, -vertex)
       double wd = bd;

@@ -248,3 +248,45 @@ def test_softmin_finite_differences_64x32(cfg2_64):
     assert not unexplained, unexplained[:8]
     # the kinks are a small set (a sanity check on the test, not a tolerance)
     assert len(failing) <= 0.02 * err.size, (len(failing), err.size)
+
+
+def test_penetration_gradient_finite_differences(built):
+    """Penetrating configurations of the box field (d < 0: a link vertex
+    inside a convex box, depth to the box's nearest face plane): central
+    differences (h = 1e-5 on FP32 joint values) of the engine's distance
+    against its d/dq, every entry where the oracle shows the same deciding
+    feature (link, box, vertex, face) at q - h, q and q + h."""
+    from klampt_gb300.engine import World
+    from oracle.oracle_py import Oracle
+    robot, env, q = sc.scene_cfg4(n_configs=256, nx=64, ny=64, spacing=0.032)
+    w = World(env, [robot])
+    o = Oracle(robot, env)
+    d, p, _, g = (x.cpu().numpy() for x in w.distance(q, 0.2))
+    pen = np.flatnonzero(d < -1e-4)[:48]
+    assert len(pen) >= 24
+    L = robot.num_links
+    h = 1e-5
+    checked = 0
+    for b in pen:
+        qp = np.repeat(q[b][None], L, 0)
+        qm = qp.copy()
+        for j in range(L):
+            qp[j, j] = np.float32(q[b, j] + h)
+            qm[j, j] = np.float32(q[b, j] - h)
+        dp, pp, _, _ = (x.cpu().numpy() for x in w.distance(qp, 0.2))
+        dm, pm, _, _ = (x.cpu().numpy() for x in w.distance(qm, 0.2))
+        base = o.pair_features(q[b], 0.0)
+        for j in range(L):
+            if tuple(pp[j]) != tuple(p[b]) or tuple(pm[j]) != tuple(p[b]):
+                continue
+            fp, fm = o.pair_features(qp[j], 0.0), o.pair_features(qm[j], 0.0)
+            key = lambda F: {(int(r[0]), int(r[1])): tuple(int(x) for x in r[2:]) for r in F[0]}
+            kb, kp, km = key(base), key(fp), key(fm)
+            pair = (int(p[b, 0]), int(p[b, 1]))
+            if kb.get(pair) != kp.get(pair) or kb.get(pair) != km.get(pair):
+                continue  # the deciding vertex or face switches inside +-h
+            fd = (dp[j] - dm[j]) / (float(qp[j, j]) - float(qm[j, j]))
+            assert abs(fd - g[b, j]) <= 1e-4 * max(np.abs(g[b]).max(), 1e-6) + 1e-7, (b, j, fd, g[b, j])
+            checked += 1
+    assert checked >= 100
+    w.close()
