@@ -206,11 +206,26 @@ def _oracle_rate_and_bytes(counts, units: int, seconds: float, out_bytes_per_uni
     return units / seconds, per_unit
 
 
-def _roofline(bytes_per_unit: float, units_per_s: float) -> dict:
+def _roofline(bytes_per_unit: float, units_per_s: float, source: str, oracle_bytes_per_unit=None) -> dict:
     peak, kind = peaks()
     achieved = bytes_per_unit * units_per_s / 1e9
-    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": None, "peak_kind": kind, "algorithmic_bytes_per_unit": bytes_per_unit}
+    out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+           "traffic": None, "peak_kind": kind, "algorithmic_bytes_per_unit": bytes_per_unit, "bytes_source": source}
+    if oracle_bytes_per_unit is not None:
+        out["oracle_traversal_bytes_per_unit"] = oracle_bytes_per_unit
+    return out
+
+
+def _kernel_bytes_per_unit(stats: dict, units: int, io_bytes: float) -> float:
+    """Bytes the distance kernel's pruned traversal reads per unit, from its
+    own work counters: 32 B per node pair, 72 B per triangle pair (the
+    same per-item sizes as the oracle-based figure), plus input and output."""
+    return (stats["dist_node_pairs"] * NODE_BYTES + stats["dist_tri_pairs"] * TRI_PAIR_BYTES) / units + io_bytes
+
+
+DIST_BYTES_NOTE = ("the distance kernels' own node-pair and triangle-pair counters x (32 B, 72 B): the FP64 "
+                   "oracle's pair-by-pair traversal (no cross-pair bound, no triangle lower bounds) reads "
+                   "oracle_traversal_bytes_per_unit, which would overstate the fraction")
 
 
 def softmin_leg(reps: int = 2) -> dict:
@@ -227,7 +242,9 @@ def softmin_leg(reps: int = 2) -> dict:
     qd = torch.as_tensor(q).cuda()
     ms = _event_ms(lambda: w.softmin(qd, 0.01, sync=False), reps)
     w.sync()
+    w.reset_stats()
     Lg, Gg = (x.cpu().numpy() for x in w.softmin(qd, 0.01))
+    kbytes = _kernel_bytes_per_unit(w.stats(), T * Wn, 4 * L + 4 * L + 8.0 / Wn)
     w.close()
     ts = np.linspace(0, T - 1, 8).astype(int)
     o = Oracle(robot, env)
@@ -244,7 +261,7 @@ def softmin_leg(reps: int = 2) -> dict:
                       f"trajectory's minimum, tau 0.01 m), 2,000 icospheres",
             "max_rel_err": {"L": float(np.max(np.abs(Lg[ts] - L_o) / np.maximum(np.abs(L_o), 1e-12))),
                             "grad": gerr, "sample": f"{len(ts)} trajectories vs the FP64 oracle"},
-            "roofline": _roofline(bpu, value),
+            "roofline": _roofline(kbytes, value, DIST_BYTES_NOTE, bpu),
             "cpu_baseline": {"value": cpu_rate, "unit": "waypoint dist+grad evals/s", "cores": cores, "kind": "port",
                              "sample": f"the same {len(ts)} trajectories, FP64 oracle, std::thread over all cores"}}
 
@@ -263,7 +280,9 @@ def min_distance_leg(reps: int = 2) -> dict:
     qd = torch.as_tensor(q).cuda()
     ms = _event_ms(lambda: w.distance(qd, 0.2, sync=False), reps)
     w.sync()
+    w.reset_stats()
     d, p, _, g = (x.cpu().numpy() for x in w.distance(qd, 0.2))
+    kbytes = _kernel_bytes_per_unit(w.stats(), B, 4 * L + 8 + 8 + 48 + 4 * L)
     w.close()
     sel = np.arange(0, B, B // 2048)[:2048]
     o = Oracle(robot, env)
@@ -281,7 +300,7 @@ def min_distance_leg(reps: int = 2) -> dict:
             "max_rel_err": {"d": float(np.max(np.abs(d[sel] - d_o) / np.maximum(np.abs(d_o), 1e-12))),
                             "grad": gerr, "pair_mismatches": int((p[sel] != p_o).any(1).sum()),
                             "sample": f"{len(sel)} configurations (every {B // 2048}th) vs the FP64 oracle"},
-            "roofline": _roofline(bpu, value),
+            "roofline": _roofline(kbytes, value, DIST_BYTES_NOTE, bpu),
             "cpu_baseline": {"value": cpu_rate, "unit": "config dist+grad evals/s", "cores": cores, "kind": "port",
                              "sample": f"the same {len(sel)} configurations, FP64 oracle, std::thread over all cores"}}
 

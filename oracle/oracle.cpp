@@ -642,23 +642,35 @@ struct MinResult {
   PairResult pr;
 };
 
+// Pairs are visited nearest first by their box lower bound, as
+// DistanceLowerBound sorts its pairs (Cpp/Planning/PlannerSettings.cpp:
+// 543-567), so the running minimum prunes the rest early; the result is the
+// minimum with ties to the smallest (link, object), whatever the order.
 MinResult min_distance(Ctx& c, double bound)
 {
   MinResult m;
   m.d = bound;
   m.link = m.obj = -1;
+  std::vector<std::pair<double, int>> cand;  // (lower bound, l * N + o)
   for (int l = 0; l < c.R->L; ++l) {
     if (c.R->bvh[l].empty()) continue;
     for (int o = 0; o < c.E->N; ++o) {
       if (!pair_enabled(c, l, o)) continue;
-      // the box bound limits the unsigned distance; a pair can be negative
-      // only when its boxes meet (bound 0)
-      if (link_obj_lb(c, l, o) > std::max(m.d, 0.0) + 1e-9) continue;
-      // ties must reach the comparison: search with a bound slightly above m.d
-      PairResult pr = pair_distance(c, l, o, std::nextafter(m.d, 1e300));
-      if (pr.found && pr.d < m.d) {
-        m.d = pr.d; m.link = l; m.obj = o; m.pr = pr;
-      }
+      const double lb = link_obj_lb(c, l, o);
+      if (lb > std::max(bound, 0.0) + 1e-9) continue;
+      cand.push_back({lb, l * c.E->N + o});
+    }
+  }
+  std::sort(cand.begin(), cand.end());
+  for (const auto& x : cand) {
+    // the box bound limits the unsigned distance; a pair can be negative
+    // only when its boxes meet (bound 0)
+    if (x.first > std::max(m.d, 0.0) + 1e-9) break;
+    const int l = x.second / c.E->N, o = x.second % c.E->N;
+    // ties must reach the comparison: search with a bound slightly above m.d
+    PairResult pr = pair_distance(c, l, o, std::nextafter(m.d, 1e300));
+    if (pr.found && (pr.d < m.d || (pr.d == m.d && m.link >= 0 && (l < m.link || (l == m.link && o < m.obj))))) {
+      m.d = pr.d; m.link = l; m.obj = o; m.pr = pr;
     }
   }
   return m;
