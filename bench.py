@@ -571,6 +571,7 @@ def main():
         torch.distributed.barrier()
     clk = clocks.stop()
     w.sync()
+    fh_timed = out.cpu().numpy()  # the last timed step's first hits, checked below
     step_ms = [x.elapsed_time(y) for x, y in evs]
     t_dev = sum(step_ms) / 1e3
     if world > 1:
@@ -619,7 +620,10 @@ def main():
     c0 = time.perf_counter()
     fh_o, cnt = o.check_edges(qa, qb, ns, nthreads=cores)
     c_dt = time.perf_counter() - c0
-    mismatches = int((fh_o != fh).sum()) + sum(int((v[0] != fh_o[:sub]).sum()) for v in plain.values())
+    # the warm-up output, the last timed step's output, the last end-to-end
+    # call's output and both plain variants
+    mismatches = (int((fh_o != fh).sum()) + int((fh_o != fh_timed).sum()) + int((fh_o != fh_h).sum()) +
+                  sum(int((v[0] != fh_o[:sub]).sum()) for v in plain.values()))
     cpu_rate = checked_configs(fh_o, ns) / c_dt
     # the reference's serial path: one thread over a prefix of the edges
     n1 = min(len(ns), 2048)
