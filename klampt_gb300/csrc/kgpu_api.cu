@@ -483,6 +483,45 @@ kgpu_status kgpu_env_create_ex(const kgpu_env_desc* d, int32_t flags, kgpu_env* 
     E->group_root[g] = node_base;
     E->group_margin[g] = round_up_f(gm);
   }
+  // breadth-first order from the group roots: the top levels of every group
+  // tree become the first nodes of the array (the engine stages them in
+  // shared memory); siblings stay adjacent
+  {
+    const size_t nn = nodes.size();
+    std::vector<int> order, perm(nn, -1);
+    order.reserve(nn);
+    for (int g = 0; g < kMaxGroups; ++g)
+      if (E->group_root[g] >= 0) order.push_back(E->group_root[g]);
+    for (size_t h = 0; h < order.size(); ++h) {
+      const KNode& n = nodes[order[h]];
+      if (as_int(n.b.w) == 0) {  // internal: children c, c + 1
+        order.push_back(as_int(n.a.w));
+        order.push_back(as_int(n.a.w) + 1);
+      }
+    }
+    if (order.size() != nn) {
+      delete E;
+      return fail(KGPU_ERR_INVALID, "environment tree layout: %zu of %zu nodes reachable", order.size(), nn);
+    }
+    for (size_t k = 0; k < nn; ++k) perm[order[k]] = (int)k;
+    std::vector<KNode> n2(nn);
+    std::vector<double> n64(6 * nn);
+    std::vector<int> nobj(nn);
+    for (size_t k = 0; k < nn; ++k) {
+      KNode n = nodes[order[k]];
+      if (as_int(n.b.w) == 0) n.a.w = as_float(perm[as_int(n.a.w)]);
+      n2[k] = n;
+      for (int i = 0; i < 6; ++i) n64[6 * k + i] = node64[6 * (size_t)order[k] + i];
+      nobj[k] = node_obj[order[k]];
+    }
+    nodes.swap(n2);
+    node64.swap(n64);
+    node_obj.swap(nobj);
+    for (int g = 0; g < kMaxGroups; ++g)
+      if (E->group_root[g] >= 0) E->group_root[g] = perm[E->group_root[g]];
+    for (int o = 0; o < N; ++o)
+      if (obj_root[o] >= 0) obj_root[o] = perm[obj_root[o]];
+  }
   E->n_nodes = nodes.size();
   E->n_tris = leaf_tris.size();
   std::vector<float4> tri32(3 * leaf_tris.size());
@@ -700,6 +739,7 @@ kgpu_status kgpu_world_create(kgpu_env env, const kgpu_robot* robots, int32_t n,
     D.obj_leaf_count = env->d_obj_leaf_count;
     D.obj_tri_first = env->d_obj_tri_first;
     D.num_objects = env->nobj;
+    D.env_nodes = (int)env->n_nodes;
     for (int g = 0; g < kMaxGroups; ++g) {
       D.group_root[g] = env->group_root[g];
       D.group_margin[g] = env->group_margin[g];

@@ -43,7 +43,7 @@ namespace kgpu {
 
 namespace {
 
-constexpr int kStackCap = 384;
+constexpr int kStackCap = 256;
 constexpr int kJobCap = 96;
 constexpr int kGrab = 2;  // items taken from the queue per atomic
 constexpr int kWarps = 8; // warps per block
@@ -89,6 +89,18 @@ struct BlockShare {
   int flag[kWarps];
   int no_release;  // failure-path test switch (KWorldDev::share_no_release)
 };
+// The top levels of the environment trees are staged in shared memory by
+// every engine block: the node array is laid out breadth first from the
+// group roots, so its first nodes are the levels every traversal starts
+// with.  How many fit next to the warps' shared memory depends on the blocks
+// resident per SM (MINB): 1,024 nodes (32 KB) at 2, 512 at 3, none at 4.
+__host__ __device__ constexpr int stage_nodes_for(int minb) { return minb <= 2 ? 1024 : (minb == 3 ? 512 : 0); }
+constexpr size_t kStageOffset = (sizeof(WarpSmem) * kWarps + sizeof(BlockShare) + 15) / 16 * 16;
+// MINB blocks of this size (plus the 1 KB the hardware reserves per block)
+// fit in the 228 KB of shared memory of an SM
+static_assert(2 * (kStageOffset + 32 * stage_nodes_for(2) + 1024) <= 228 * 1024, "2 blocks per SM");
+static_assert(3 * (kStageOffset + 32 * stage_nodes_for(3) + 1024) <= 228 * 1024, "3 blocks per SM");
+static_assert(4 * (kStageOffset + 32 * stage_nodes_for(4) + 1024) <= 228 * 1024, "4 blocks per SM");
 constexpr int kDonateMin = 32;     // stack entries a warp needs before it shares
 constexpr int kShareSpins = 1 << 20;  // bound on a waiting warp's polls (~0.3 s)
 
@@ -351,7 +363,8 @@ __device__ __forceinline__ float pair_tol(const WarpSmem& S, int la, int tgt)
 
 __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __restrict__ W,
                                           const KRobotDev& R, uint2 e, uint2& c0, uint2& c1,
-                                          uint32_t& jA, uint32_t& jB, uint32_t& jM)
+                                          uint32_t& jA, uint32_t& jB, uint32_t& jM, const KNode* stage,
+                                          int nstage)
 {
   const int nodeA = e.y & 0xfffff;
   const int la = (e.y >> 20) & 31;
@@ -359,7 +372,10 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
   const int nodeB = (int)e.x;
   const bool self = tgt < 32;
   const KNode na = W->lnodes[nodeA];
-  const KNode nb = (self ? W->lnodes : W->enodes)[nodeB];
+  // environment nodes of the staged top levels come from shared memory (one
+  // generic load either way, so lanes do not diverge)
+  const KNode* pb = self ? W->lnodes + nodeB : (nodeB < nstage ? stage + nodeB : W->enodes + nodeB);
+  const KNode nb = *pb;
   float TA[12];
   load_row(S.T[la], TA);
   const Box32 A = xform_box(TA, na.a, na.b);
@@ -463,10 +479,11 @@ __device__ __noinline__ unsigned traverse(WarpSmem& S, const KWorldDev* __restri
                                           int qbase, int qcount, int lane, uint2* spill, int spill_cap,
                                           double (*T64)[12], int& fk64, const EngineArgs& A, int job_flush,
                                           Cnt& cnt, WarpSmem* all, int me, BlockShare& B, int preset, unsigned live,
-                                          int lgL)
+                                          int lgL, int nstage)
 {
   const unsigned lt = lanemask_lt();
   const int lmask = (1 << lgL) - 1;
+  const KNode* stage = reinterpret_cast<const KNode*>(reinterpret_cast<const unsigned char*>(all) + kStageOffset);
   int top = preset, njobs = 0, spill_top = 0;
   unsigned hits = 0;
   S.tol64[lane] = S.delta[lane] + W->eps_extra + R.link_margin[lane & lmask];
@@ -572,7 +589,7 @@ __device__ __noinline__ unsigned traverse(WarpSmem& S, const KWorldDev* __restri
     int outcome = 0;  // 1: two children, 2: leaf job
     uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
     uint32_t jA = 0, jB = 0, jM = 0;
-    if (have) outcome = test_entry(S, W, R, e, c0, c1, jA, jB, jM);
+    if (have) outcome = test_entry(S, W, R, e, c0, c1, jA, jB, jM, stage, nstage);
     cnt.node_pairs += have ? 1 : 0;
     const unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
     const unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
@@ -622,6 +639,14 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
     B.idle = 0;
     for (int w = 0; w < kWarps; ++w) B.flag[w] = 2;
     B.no_release = W->share_no_release;
+  }
+  // the environment tree's top levels into shared memory (coalesced 16-byte
+  // loads; 2 per node)
+  const int nstage = min(stage_nodes_for(MINB), W->env_nodes);
+  {
+    const float4* __restrict__ src = reinterpret_cast<const float4*>(W->enodes);
+    float4* dst = reinterpret_cast<float4*>(smem_raw + kStageOffset);
+    for (int i = threadIdx.x; i < 2 * nstage; i += blockDim.x) dst[i] = __ldg(src + i);
   }
   __syncthreads();
   // configurations of one robot go in groups of G = 32 / L (L = its link
@@ -797,16 +822,16 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           const int nq = R.nqueries_env + R.nqueries_self;
           if (nq > 0)
             env_hits = traverse<FP64, EDGES>(S, W, R, R.query_off, nq, lane, spill, spill_cap, T64, fk64, A,
-                                             job_flush, cnt, all, warp, B, 0, live, lgL);
+                                             job_flush, cnt, all, warp, B, 0, live, lgL, nstage);
         } else {
           // configurations report the environment and self verdicts apart
           if (A.env_hit != nullptr && R.nqueries_env > 0)
             env_hits = traverse<FP64, EDGES>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64,
-                                             fk64, A, job_flush, cnt, all, warp, B, 0, live, lgL);
+                                             fk64, A, job_flush, cnt, all, warp, B, 0, live, lgL, nstage);
           if (A.self_hit != nullptr && R.nqueries_self > 0)
             self_hits = traverse<FP64, EDGES>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane,
                                               spill, spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0, live,
-                                              lgL);
+                                              lgL, nstage);
         }
         if ((env_hits | self_hits) & kTrOverflow) {
           if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
@@ -868,7 +893,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           int fk64 = 0;
           const bool self = ((S.stack[0].y >> 25) & 63u) < 32u;
           const unsigned hits = traverse<FP64, EDGES>(S, W, R, 0, 0, lane, spill, spill_cap, T64, fk64, A, job_flush,
-                                                      cnt, all, warp, B, S.don_top, live, lgL);
+                                                      cnt, all, warp, B, S.don_top, live, lgL, nstage);
           if (lane == 0) {
             if (hits & kTrOverflow) {
               set_status(W->status, KGPU_ERR_OVERFLOW);
@@ -996,7 +1021,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) k_self_pairs(const KWorldDev* 
         if ((__shfl_sync(0xffffffffu, known, 0) >> tgt) & 1u) continue;
       }
       const unsigned hits = traverse<true, false>(S, W, R, qidx, 1, lane, spill, spill_cap, T64, fk64, A, job_flush,
-                                                  cnt, all, warp, B, 0, 1u, 5);
+                                                  cnt, all, warp, B, 0, 1u, 5, 0);
       if (hits & kTrOverflow) {
         if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
         found = 2;  // no verdict for this configuration
@@ -1400,7 +1425,7 @@ template <int MINB, bool FP64, bool EDGES>
 cudaError_t init_engine()
 {
   return cudaFuncSetAttribute(k_engine<MINB, FP64, EDGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)(sizeof(WarpSmem) * kWarps + sizeof(BlockShare)));
+                              (int)(kStageOffset + sizeof(KNode) * stage_nodes_for(MINB)));
 }
 
 // the shared-memory attribute is set once per process by engine_init(), so
@@ -1408,7 +1433,7 @@ cudaError_t init_engine()
 template <int MINB, bool FP64>
 cudaError_t launch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, cudaStream_t s)
 {
-  size_t smem = sizeof(WarpSmem) * kWarps + sizeof(BlockShare);
+  const size_t smem = kStageOffset + sizeof(KNode) * stage_nodes_for(MINB);
   if (A.mode == MODE_EDGES)
     k_engine<MINB, FP64, true><<<blocks, kWarps * 32, smem, s>>>(W, A);
   else

@@ -115,6 +115,7 @@ struct KWorldDev {
   int group_root[kMaxGroups];
   float group_margin[kMaxGroups];
   int num_objects;
+  int env_nodes;             // nodes in enodes (laid out breadth first from the group roots)
   // tolerances (m): the per-link FP32 error bounds come from warp_fk32; the
   // environment's FP32 coordinates are off by at most eps_env; eps_extra is
   // an optional additional inflation (world option, default 0)
