@@ -243,6 +243,7 @@ Scratch engine_scratch(kgpu_world w, Scratch S)
   if (w->pend_cap_opt > 0 && w->pend_cap_opt < S.pend_cap) S.pend_cap = w->pend_cap_opt;
   const size_t spill = (size_t)w->spill_cap_opt + (size_t)engine_scratch_doubles();
   if (w->spill_cap_opt > 0 && spill < S.spill_per_warp) S.spill_per_warp = spill;
+  S.stage_nodes = w->stage_nodes;
   return S;
 }
 }  // namespace kgpu
@@ -825,6 +826,9 @@ kgpu_status kgpu_world_set_option(kgpu_world w, const char* name, double v)
   } else if (!strcmp(name, "spill_cap")) {
     if (!(v >= 0 && v <= 1e9)) return fail(KGPU_ERR_INVALID, "spill_cap must be in [0, 1e9] (0: no cap)");
     w->spill_cap_opt = (int)v;
+  } else if (!strcmp(name, "stage_nodes")) {
+    if (!(v >= 0 && v <= 1024)) return fail(KGPU_ERR_INVALID, "stage_nodes must be in [0, 1024]");
+    w->stage_nodes = (int)v;
   } else if (!strcmp(name, "share_wait_polls")) {
     if (!(v >= 0 && v <= (double)(1 << 20))) return fail(KGPU_ERR_INVALID, "share_wait_polls must be in [0, 2^20]");
     w->dev.share_wait = (int)v;
@@ -854,6 +858,7 @@ kgpu_status kgpu_world_get_option(kgpu_world w, const char* name, double* v)
   else if (!strcmp(name, "fp64_inline")) *v = w->fp64_inline;
   else if (!strcmp(name, "num_sms")) *v = w->num_sms;
   else if (!strcmp(name, "pend_cap")) *v = w->pend_cap_opt;
+  else if (!strcmp(name, "stage_nodes")) *v = w->stage_nodes;
   else if (!strcmp(name, "spill_cap")) *v = w->spill_cap_opt;
   else if (!strcmp(name, "share_wait_polls")) *v = w->dev.share_wait;
   else if (!strcmp(name, "share_no_release")) *v = w->dev.share_no_release;

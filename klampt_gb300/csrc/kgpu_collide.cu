@@ -53,7 +53,8 @@ constexpr int kTailItemsPerWarp = 2;  // single-step rounds once fewer items tha
 
 enum Mode { MODE_CONFIGS = 0, MODE_FEASIBLE = 1, MODE_EDGES = 2 };
 
-// per-warp shared memory (~6.4 KB, so that up to 32 warps fit on an SM)
+// per-warp shared memory (~5.9 KB; with the staged environment nodes, 2 or 3
+// 8-warp blocks fit on an SM, 4 without them)
 struct __align__(16) WarpSmem {
   float T[kMaxLinks][12];     // first: every row starts on a 16-byte boundary
   uint2 stack[kStackCap];
@@ -159,6 +160,7 @@ struct EngineArgs {
   unsigned int* pend_count;
   int pend_cap;
   int inline64;          // 1: one pass with the FP64 test inline (no list)
+  int stage_nodes;       // environment nodes to stage in shared memory (capped per residency)
 };
 
 struct Cnt {
@@ -372,10 +374,8 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
   const int nodeB = (int)e.x;
   const bool self = tgt < 32;
   const KNode na = W->lnodes[nodeA];
-  // environment nodes of the staged top levels come from shared memory (one
-  // generic load either way, so lanes do not diverge)
-  const KNode* pb = self ? W->lnodes + nodeB : (nodeB < nstage ? stage + nodeB : W->enodes + nodeB);
-  const KNode nb = *pb;
+  // environment nodes of the staged top levels come from shared memory
+  const KNode nb = self ? W->lnodes[nodeB] : (nodeB < nstage ? stage[nodeB] : W->enodes[nodeB]);
   float TA[12];
   load_row(S.T[la], TA);
   const Box32 A = xform_box(TA, na.a, na.b);
@@ -642,7 +642,7 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
   }
   // the environment tree's top levels into shared memory (coalesced 16-byte
   // loads; 2 per node)
-  const int nstage = min(stage_nodes_for(MINB), W->env_nodes);
+  const int nstage = min(min(A.stage_nodes, stage_nodes_for(MINB)), W->env_nodes);
   {
     const float4* __restrict__ src = reinterpret_cast<const float4*>(W->enodes);
     float4* dst = reinterpret_cast<float4*>(smem_raw + kStageOffset);
@@ -1433,7 +1433,7 @@ cudaError_t init_engine()
 template <int MINB, bool FP64>
 cudaError_t launch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, cudaStream_t s)
 {
-  const size_t smem = kStageOffset + sizeof(KNode) * stage_nodes_for(MINB);
+  const size_t smem = kStageOffset + sizeof(KNode) * min(max(A.stage_nodes, 0), stage_nodes_for(MINB));
   if (A.mode == MODE_EDGES)
     k_engine<MINB, FP64, true><<<blocks, kWarps * 32, smem, s>>>(W, A);
   else
@@ -1456,6 +1456,7 @@ cudaError_t dispatch_engine(const KWorldDev* W, EngineArgs A, const Scratch& S, 
   A.pend_count = S.counters + 1;
   A.pend = S.pend;
   A.pend_cap = S.pend_cap;
+  A.stage_nodes = S.stage_nodes;
   if (A.inline64) return per_sm == 3 ? launch_engine<3, true>(W, A, blocks, s) : launch_engine<2, true>(W, A, blocks, s);
   switch (per_sm) {
     case 3: err = launch_engine<3, false>(W, A, blocks, s); break;

@@ -160,140 +160,6 @@ struct PairOut {
   float dir[3];
 };
 
-// Signed distance of a pair whose surfaces meet: for a convex object the
-// depth of the deepest link vertex inside it (d = -depth, FP32 screening,
-// canonical FP64 for the vertices within the band of the deepest), else 0.
-__device__ __noinline__ void contact_depth(DistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
-                                           double (*T64)[12], int& fk64, int lane, int l, int o, float dl, float de,
-                                           const float* TA, int certA, double bound, PairOut& out)
-{
-  int vbest = -1, fbest = -1;
-  double depth = 0.0;
-  if (W->obj_convex[o]) {
-    // deepest link vertex inside the convex object
-    const int vf = R.link_vert_first[l], vc = R.link_vert_count[l];
-    const KNode ob = W->enodes[W->obj_root[o]];
-    const float tolb = dl + de + 8.f * kU * (fabsf(ob.a.x) + fabsf(ob.a.y) + fabsf(ob.a.z) + 1.f);
-    const int ff = W->obj_leaf_first[o], fc = W->obj_leaf_count[o];
-    const float ed = dl + de + 32.f * kU * (fabsf(ob.a.x) + fabsf(ob.a.y) + fabsf(ob.a.z) + fabsf(ob.b.x) +
-                                           fabsf(ob.b.y) + fabsf(ob.b.z) + 1.f);
-    float lmax = -FLT_MAX;
-    // pass 1: FP32 depths, lane-local maximum.  Each lane also keeps the (at
-    // most two) vertices whose pass-1 value lies within 2 ed of its running
-    // maximum: pass 1's value bounds a vertex's full FP32 minimum from
-    // above, and the global maximum is at least the lane's, so every vertex
-    // that pass 2 can accept is among them, unless more than two qualified
-    // (then the lane rescans all of its vertices)
-    int cv0 = 0, cv1 = 0, nc = 0;
-    float cd0 = 0.f, cd1 = 0.f;
-    bool rescan = false;
-    for (int v = lane; v < vc; v += 32) {
-      const float4 x = __ldg(W->lvert32 + vf + v);
-      const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
-      if (fabsf(w.x - ob.a.x) > ob.b.x + tolb || fabsf(w.y - ob.a.y) > ob.b.y + tolb ||
-          fabsf(w.z - ob.a.z) > ob.b.z + tolb)
-        continue;
-      // a vertex stops counting once it is no deeper than the deepest so far
-      // (or outside the band): its final minimum can only be lower
-      const float stop = fmaxf(lmax, -ed);
-      float dmin = FLT_MAX;
-      for (int f = ff; f < ff + fc && dmin > stop; ++f) {
-        const float4 pl = __ldg(W->eface32 + f);
-        dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
-      }
-      lmax = fmaxf(lmax, dmin);
-      const float thr = lmax - 2.f * ed;
-      if (dmin > -ed && dmin >= thr) {
-        if (nc == 2 && cd1 < thr) nc = 1;
-        if (nc >= 1 && cd0 < thr) {
-          if (nc == 2) { cv0 = cv1; cd0 = cd1; }
-          --nc;
-        }
-        if (nc == 0) { cv0 = v; cd0 = dmin; nc = 1; }
-        else if (nc == 1) { cv1 = v; cd1 = dmin; nc = 2; }
-        else rescan = true;
-      }
-    }
-    const float gmax = -warp_min(-lmax);
-    if (gmax > -ed) {
-      dist_fk64(S, R, T64, lane, fk64);
-      // pass 2: FP64 depth of every vertex within the band of the deepest
-      double bd = 0.0;
-      int bv = INT_MAX, bf = -1;
-      auto depth64 = [&](int v) {
-        const float4 x = __ldg(W->lvert32 + vf + v);
-        const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
-        if (fabsf(w.x - ob.a.x) > ob.b.x + tolb || fabsf(w.y - ob.a.y) > ob.b.y + tolb ||
-            fabsf(w.z - ob.a.z) > ob.b.z + tolb)
-          return;
-        const float stop = fmaxf(gmax - 2.f * ed, -ed);
-        float dmin = FLT_MAX;
-        for (int f = ff; f < ff + fc && dmin >= stop; ++f) {
-          const float4 pl = __ldg(W->eface32 + f);
-          dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
-        }
-        if (dmin < gmax - 2.f * ed || dmin <= -ed) return;
-        double w64[3];
-        kx_xform_point(T64[l], W->lvert64 + 3 * (size_t)(vf + v), w64);
-        double dm = DBL_MAX;
-        int fm = -1, fo = INT_MAX;
-        for (int f = ff; f < ff + fc; ++f) {
-          const double* pl = W->eface64 + 4 * (size_t)f;
-          const double dep = kx_sub(pl[3], kx_dot3(pl, w64));
-          const int orig = W->etri_orig[f];
-          if (dep < dm || (dep == dm && orig < fo)) { dm = dep; fm = f; fo = orig; }
-        }
-        if (dm > bd || (dm == bd && dm > 0.0 && v < bv)) { bd = dm; bv = v; bf = fm; }
-      };
-      if (rescan) {
-        for (int v = lane; v < vc; v += 32) depth64(v);
-      } else {
-        if (nc >= 1 && cd0 >= gmax - 2.f * ed) depth64(cv0);
-        if (nc >= 2 && cd1 >= gmax - 2.f * ed) depth64(cv1);
-      }
-      // warp maximum of (depth, -vertex)
-      double wd = bd;
-      int wv = bd > 0.0 ? bv : INT_MAX, wf = bf, src = lane;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        const double od = __shfl_xor_sync(0xffffffffu, wd, off);
-        const int ov = __shfl_xor_sync(0xffffffffu, wv, off);
-        const int ofc = __shfl_xor_sync(0xffffffffu, wf, off);
-        const int os = __shfl_xor_sync(0xffffffffu, src, off);
-        if (od > wd || (od == wd && (ov < wv || (ov == wv && os < src)))) { wd = od; wv = ov; wf = ofc; src = os; }
-      }
-      if (wd > 0.0) {
-        depth = wd;
-        vbest = wv;
-        fbest = wf;
-      }
-    }
-  }
-  if (vbest >= 0) {
-    double w64[3];
-    kx_xform_point(T64[l], W->lvert64 + 3 * (size_t)(R.link_vert_first[l] + vbest), w64);
-    const double* pl = W->eface64 + 4 * (size_t)fbest;
-    out.d = -depth;
-    out.found = -depth < bound;
-    for (int i = 0; i < 3; ++i) {
-      out.cp[i] = w64[i];
-      out.cq[i] = kx_add(w64[i], kx_mul(depth, pl[i]));
-      out.dir[i] = (float)pl[i];
-    }
-    return;
-  }
-  // contact without a vertex inside (or a non-convex object): d = 0, no direction
-  out.d = 0.0;
-  out.found = 0.0 < bound;
-  float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (certA >= 0) x = __ldg(W->ltri32 + 3 * (size_t)certA);
-  const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
-  out.cp[0] = out.cq[0] = w.x;
-  out.cp[1] = out.cq[1] = w.y;
-  out.cp[2] = out.cq[2] = w.z;
-  out.dir[0] = out.dir[1] = out.dir[2] = 0.f;
-}
-
 // Signed distance of (link l, object o) below `bound` (found = d < bound).
 __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
                                        double (*T64)[12], int& fk64, int lane, int l, int o, double bound,
@@ -537,9 +403,132 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
     }
     return;
   }
-  // ---- surfaces meet (out of line: only contact pairs take it)
-  contact_depth(S, W, R, T64, fk64, lane, l, o, dl, de, TA, certA, bound, out);
-  return;
+  // ---- surfaces meet
+  int vbest = -1, fbest = -1;
+  double depth = 0.0;
+  if (W->obj_convex[o]) {
+    // deepest link vertex inside the convex object
+    const int vf = R.link_vert_first[l], vc = R.link_vert_count[l];
+    const KNode ob = W->enodes[W->obj_root[o]];
+    const float tolb = dl + de + 8.f * kU * (fabsf(ob.a.x) + fabsf(ob.a.y) + fabsf(ob.a.z) + 1.f);
+    const int ff = W->obj_leaf_first[o], fc = W->obj_leaf_count[o];
+    const float ed = dl + de + 32.f * kU * (fabsf(ob.a.x) + fabsf(ob.a.y) + fabsf(ob.a.z) + fabsf(ob.b.x) +
+                                           fabsf(ob.b.y) + fabsf(ob.b.z) + 1.f);
+    float lmax = -FLT_MAX;
+    // pass 1: FP32 depths, lane-local maximum.  Each lane also keeps the (at
+    // most two) vertices whose pass-1 value lies within 2 ed of its running
+    // maximum: pass 1's value bounds a vertex's full FP32 minimum from
+    // above, and the global maximum is at least the lane's, so every vertex
+    // that pass 2 can accept is among them, unless more than two qualified
+    // (then the lane rescans all of its vertices)
+    int cv0 = 0, cv1 = 0, nc = 0;
+    float cd0 = 0.f, cd1 = 0.f;
+    bool rescan = false;
+    for (int v = lane; v < vc; v += 32) {
+      const float4 x = __ldg(W->lvert32 + vf + v);
+      const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
+      if (fabsf(w.x - ob.a.x) > ob.b.x + tolb || fabsf(w.y - ob.a.y) > ob.b.y + tolb ||
+          fabsf(w.z - ob.a.z) > ob.b.z + tolb)
+        continue;
+      // a vertex stops counting once it is no deeper than the deepest so far
+      // (or outside the band): its final minimum can only be lower
+      const float stop = fmaxf(lmax, -ed);
+      float dmin = FLT_MAX;
+      for (int f = ff; f < ff + fc && dmin > stop; ++f) {
+        const float4 pl = __ldg(W->eface32 + f);
+        dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
+      }
+      lmax = fmaxf(lmax, dmin);
+      const float thr = lmax - 2.f * ed;
+      if (dmin > -ed && dmin >= thr) {
+        if (nc == 2 && cd1 < thr) nc = 1;
+        if (nc >= 1 && cd0 < thr) {
+          if (nc == 2) { cv0 = cv1; cd0 = cd1; }
+          --nc;
+        }
+        if (nc == 0) { cv0 = v; cd0 = dmin; nc = 1; }
+        else if (nc == 1) { cv1 = v; cd1 = dmin; nc = 2; }
+        else rescan = true;
+      }
+    }
+    const float gmax = -warp_min(-lmax);
+    if (gmax > -ed) {
+      dist_fk64(S, R, T64, lane, fk64);
+      // pass 2: FP64 depth of every vertex within the band of the deepest
+      double bd = 0.0;
+      int bv = INT_MAX, bf = -1;
+      auto depth64 = [&](int v) {
+        const float4 x = __ldg(W->lvert32 + vf + v);
+        const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
+        if (fabsf(w.x - ob.a.x) > ob.b.x + tolb || fabsf(w.y - ob.a.y) > ob.b.y + tolb ||
+            fabsf(w.z - ob.a.z) > ob.b.z + tolb)
+          return;
+        const float stop = fmaxf(gmax - 2.f * ed, -ed);
+        float dmin = FLT_MAX;
+        for (int f = ff; f < ff + fc && dmin >= stop; ++f) {
+          const float4 pl = __ldg(W->eface32 + f);
+          dmin = fminf(dmin, pl.w - (pl.x * w.x + pl.y * w.y + pl.z * w.z));
+        }
+        if (dmin < gmax - 2.f * ed || dmin <= -ed) return;
+        double w64[3];
+        kx_xform_point(T64[l], W->lvert64 + 3 * (size_t)(vf + v), w64);
+        double dm = DBL_MAX;
+        int fm = -1, fo = INT_MAX;
+        for (int f = ff; f < ff + fc; ++f) {
+          const double* pl = W->eface64 + 4 * (size_t)f;
+          const double dep = kx_sub(pl[3], kx_dot3(pl, w64));
+          const int orig = W->etri_orig[f];
+          if (dep < dm || (dep == dm && orig < fo)) { dm = dep; fm = f; fo = orig; }
+        }
+        if (dm > bd || (dm == bd && dm > 0.0 && v < bv)) { bd = dm; bv = v; bf = fm; }
+      };
+      if (rescan) {
+        for (int v = lane; v < vc; v += 32) depth64(v);
+      } else {
+        if (nc >= 1 && cd0 >= gmax - 2.f * ed) depth64(cv0);
+        if (nc >= 2 && cd1 >= gmax - 2.f * ed) depth64(cv1);
+      }
+      // warp maximum of (depth, -vertex)
+      double wd = bd;
+      int wv = bd > 0.0 ? bv : INT_MAX, wf = bf, src = lane;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const double od = __shfl_xor_sync(0xffffffffu, wd, off);
+        const int ov = __shfl_xor_sync(0xffffffffu, wv, off);
+        const int ofc = __shfl_xor_sync(0xffffffffu, wf, off);
+        const int os = __shfl_xor_sync(0xffffffffu, src, off);
+        if (od > wd || (od == wd && (ov < wv || (ov == wv && os < src)))) { wd = od; wv = ov; wf = ofc; src = os; }
+      }
+      if (wd > 0.0) {
+        depth = wd;
+        vbest = wv;
+        fbest = wf;
+      }
+    }
+  }
+  if (vbest >= 0) {
+    double w64[3];
+    kx_xform_point(T64[l], W->lvert64 + 3 * (size_t)(R.link_vert_first[l] + vbest), w64);
+    const double* pl = W->eface64 + 4 * (size_t)fbest;
+    out.d = -depth;
+    out.found = -depth < bound;
+    for (int i = 0; i < 3; ++i) {
+      out.cp[i] = w64[i];
+      out.cq[i] = kx_add(w64[i], kx_mul(depth, pl[i]));
+      out.dir[i] = (float)pl[i];
+    }
+    return;
+  }
+  // contact without a vertex inside (or a non-convex object): d = 0, no direction
+  out.d = 0.0;
+  out.found = 0.0 < bound;
+  float4 x = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (certA >= 0) x = __ldg(W->ltri32 + 3 * (size_t)certA);
+  const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
+  out.cp[0] = out.cq[0] = w.x;
+  out.cp[1] = out.cq[1] = w.y;
+  out.cp[2] = out.cq[2] = w.z;
+  out.dir[0] = out.dir[1] = out.dir[2] = 0.f;
 }
 
 // Gathers objects of group g whose root box is within `bound` of link l's
