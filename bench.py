@@ -53,7 +53,7 @@ TRI_PAIR_BYTES = 72
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=60)
+    p.add_argument("--steps", type=int, default=300)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="engine", choices=["engine", "reference"])
     p.add_argument("--edges", type=int, default=16384)
@@ -63,9 +63,11 @@ def parse():
                    help="world option for --engine-only runs (e.g. blocks_per_sm=2)")
     p.add_argument("--dist-only", type=int, default=0, metavar="N",
                    help="only N minimum-distance+gradient evaluations (profiling runs)")
-    p.add_argument("--dist-scene", default="softmin", choices=["softmin", "terrain"],
-                   help="--dist-only scene: the soft-min waypoints (icospheres, cutoff 1000 m) or the terrain "
-                        "and boxes (cutoff 0.2 m)")
+    p.add_argument("--dist-scene", default="softmin", choices=["softmin", "softmin_grad", "terrain", "self"],
+                   help="--dist-only scene: minimum distance over the soft-min waypoints (icospheres, cutoff "
+                        "1000 m), the soft-min and its gradient over those waypoints (N / 32 trajectories, tau "
+                        "0.01 m), the terrain and boxes (cutoff 0.2 m), or the humanoid's self distance "
+                        "(cutoff 1 m)")
     return p.parse_args()
 
 
@@ -75,19 +77,37 @@ def run_dist_only(args):
     kbuild.build()
     from klampt_gb300 import scenes as sc
     from klampt_gb300.engine import World
+    query = None
     if args.dist_scene == "terrain":
         robot, env, q = sc.scene_cfg4(n_configs=args.dist_only)
         cutoff = 0.2
+    elif args.dist_scene == "self":
+        # the bench's self-distance leg: humanoid configurations scaled
+        # towards zero (a third of them separated)
+        robot = sc.humanoid()
+        env = sc.env_from_objects("far", [sc.box_mesh((9, 9, 9), (0.1, 0.1, 0.1))])
+        rng = np.random.default_rng(2003)
+        q = (sc.uniform_configs(robot, args.dist_only, rng) * rng.uniform(0, 1, (args.dist_only, 1))).astype(np.float32)
+        cutoff = 1.0
+        query = "self"
     else:
         robot, env, q = sc.scene_cfg2(T=(args.dist_only + 31) // 32, W=32)
         cutoff = 1e3
+        if args.dist_scene == "softmin_grad":
+            query = "softmin"
     w = World(env, [robot])
-    qd = torch.as_tensor(q.reshape(-1, robot.num_links)[:args.dist_only]).cuda()
+    if query == "softmin":
+        qd = torch.as_tensor(q).cuda()   # [T, 32, L] waypoints
+        cutoff = 0.01                    # tau
+        run = w.softmin
+    else:
+        qd = torch.as_tensor(q.reshape(-1, robot.num_links)[:args.dist_only]).cuda()
+        run = w.self_distance if query == "self" else w.distance
     for _ in range(max(1, args.warmup)):
-        w.distance(qd, cutoff)
+        run(qd, cutoff)
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        w.distance(qd, cutoff, sync=False)
+        run(qd, cutoff, sync=False)
     w.sync()
     print(json.dumps({"dist_only": args.dist_only, "ms_per_step": 1e3 * (time.perf_counter() - t0) / max(1, args.steps)}))
 
@@ -110,6 +130,7 @@ class ClockSampler:
         self.index = index
         self.proc = None
         self.lines = []
+        self.skip = 0
 
     def start(self):
         try:
@@ -118,6 +139,12 @@ class ClockSampler:
                  "-lms", "100"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.thread = threading.Thread(target=self._read, daemon=True)
             self.thread.start()
+            # the timed region starts once sampling runs (nvidia-smi takes a
+            # moment to come up)
+            t0 = time.perf_counter()
+            while not self.lines and time.perf_counter() - t0 < 5.0 and self.proc.poll() is None:
+                time.sleep(0.01)
+            self.skip = len(self.lines)
         except Exception:
             self.proc = None
 
@@ -135,7 +162,9 @@ class ClockSampler:
             self.proc.kill()
         sm, smax, reasons = [], None, set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        # samples from inside the timed region (the one taken as sampling
+        # came up, if the region was too short for another)
+        for ln in self.lines[self.skip:] or self.lines[-1:]:
             parts = [x.strip() for x in ln.split(",")]
             if len(parts) < 9:
                 continue

@@ -173,8 +173,14 @@ kgpu_status kgpu_world_enable_self_pair(kgpu_world world, int32_t robot, int32_t
  * leave undecided get the FP64 test inside the traversal kernel; 0: they are
  * listed and decided by a second kernel, keeping FP64 code out of the
  * traversal kernel and letting configurations of one robot be checked in
- * groups; -1, the default: 0), read-only
- * "eps_env", "warps_per_block", "num_sms".  The autotuner
+ * groups; -1, the default: 0), "stage_nodes" (0..1024, default 0: at 2
+ * blocks per SM with the FP64 test deferred, each engine block copies this
+ * many top nodes of the breadth-first environment node array into shared
+ * memory and reads them there; results do not change), read-only
+ * "eps_env", "warps_per_block", "num_sms".  Test options that shrink a
+ * bound until it is reached: "pend_cap" (undecided-pair list records),
+ * "spill_cap" (spill entries per warp), "share_wait_polls" and
+ * "share_no_release" (the work-sharing wait).  The autotuner
  * (klampt_gb300/autotune.py) sets blocks_per_sm, grab, job_flush and
  * edge_chunk or fp64_inline.
  * Unknown names are KGPU_ERR_INVALID. */

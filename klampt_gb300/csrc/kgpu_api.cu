@@ -485,8 +485,8 @@ kgpu_status kgpu_env_create_ex(const kgpu_env_desc* d, int32_t flags, kgpu_env* 
     E->group_margin[g] = round_up_f(gm);
   }
   // breadth-first order from the group roots: the top levels of every group
-  // tree become the first nodes of the array (the engine stages them in
-  // shared memory); siblings stay adjacent
+  // tree, which every traversal visits, share the first cache lines of the
+  // array; siblings stay adjacent
   {
     const size_t nn = nodes.size();
     std::vector<int> order, perm(nn, -1);
@@ -858,8 +858,8 @@ kgpu_status kgpu_world_get_option(kgpu_world w, const char* name, double* v)
   else if (!strcmp(name, "fp64_inline")) *v = w->fp64_inline;
   else if (!strcmp(name, "num_sms")) *v = w->num_sms;
   else if (!strcmp(name, "pend_cap")) *v = w->pend_cap_opt;
-  else if (!strcmp(name, "stage_nodes")) *v = w->stage_nodes;
   else if (!strcmp(name, "spill_cap")) *v = w->spill_cap_opt;
+  else if (!strcmp(name, "stage_nodes")) *v = w->stage_nodes;
   else if (!strcmp(name, "share_wait_polls")) *v = w->dev.share_wait;
   else if (!strcmp(name, "share_no_release")) *v = w->dev.share_no_release;
   else return fail(KGPU_ERR_INVALID, "unknown option '%s'", name);

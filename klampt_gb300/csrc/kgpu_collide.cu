@@ -43,7 +43,7 @@ namespace kgpu {
 
 namespace {
 
-constexpr int kStackCap = 256;
+constexpr int kStackCap = 384;
 constexpr int kJobCap = 96;
 constexpr int kGrab = 2;  // items taken from the queue per atomic
 constexpr int kWarps = 8; // warps per block
@@ -53,8 +53,7 @@ constexpr int kTailItemsPerWarp = 2;  // single-step rounds once fewer items tha
 
 enum Mode { MODE_CONFIGS = 0, MODE_FEASIBLE = 1, MODE_EDGES = 2 };
 
-// per-warp shared memory (~5.9 KB; with the staged environment nodes, 2 or 3
-// 8-warp blocks fit on an SM, 4 without them)
+// per-warp shared memory (~6.4 KB, so that up to 32 warps fit on an SM)
 struct __align__(16) WarpSmem {
   float T[kMaxLinks][12];     // first: every row starts on a 16-byte boundary
   uint2 stack[kStackCap];
@@ -90,18 +89,17 @@ struct BlockShare {
   int flag[kWarps];
   int no_release;  // failure-path test switch (KWorldDev::share_no_release)
 };
-// The top levels of the environment trees are staged in shared memory by
-// every engine block: the node array is laid out breadth first from the
-// group roots, so its first nodes are the levels every traversal starts
-// with.  How many fit next to the warps' shared memory depends on the blocks
-// resident per SM (MINB): 1,024 nodes (32 KB) at 2, 512 at 3, none at 4.
-__host__ __device__ constexpr int stage_nodes_for(int minb) { return minb <= 2 ? 1024 : (minb == 3 ? 512 : 0); }
-constexpr size_t kStageOffset = (sizeof(WarpSmem) * kWarps + sizeof(BlockShare) + 15) / 16 * 16;
-// MINB blocks of this size (plus the 1 KB the hardware reserves per block)
-// fit in the 228 KB of shared memory of an SM
-static_assert(2 * (kStageOffset + 32 * stage_nodes_for(2) + 1024) <= 228 * 1024, "2 blocks per SM");
-static_assert(3 * (kStageOffset + 32 * stage_nodes_for(3) + 1024) <= 228 * 1024, "3 blocks per SM");
-static_assert(4 * (kStageOffset + 32 * stage_nodes_for(4) + 1024) <= 228 * 1024, "4 blocks per SM");
+constexpr size_t kBlockSmem = sizeof(WarpSmem) * kWarps + sizeof(BlockShare);
+// Optional (world option stage_nodes, 2 blocks per SM): the first nodes of
+// the environment node array, which is laid out breadth first from the group
+// roots, are the top levels every traversal starts with; a staged block
+// copies up to kStageNodes of them into shared memory and reads them there.
+constexpr int kStageNodes = 1024;
+constexpr size_t kStageOffset = (kBlockSmem + 15) / 16 * 16;
+// MINB blocks (plus the 1 KB the hardware reserves per block) fit in the
+// 228 KB of shared memory of an SM
+static_assert(4 * (kBlockSmem + 1024) <= 228 * 1024, "4 blocks per SM");
+static_assert(2 * (kStageOffset + 32 * kStageNodes + 1024) <= 228 * 1024, "2 staged blocks per SM");
 constexpr int kDonateMin = 32;     // stack entries a warp needs before it shares
 constexpr int kShareSpins = 1 << 20;  // bound on a waiting warp's polls (~0.3 s)
 
@@ -160,7 +158,7 @@ struct EngineArgs {
   unsigned int* pend_count;
   int pend_cap;
   int inline64;          // 1: one pass with the FP64 test inline (no list)
-  int stage_nodes;       // environment nodes to stage in shared memory (capped per residency)
+  int stage_nodes;       // environment nodes a staged block copies to shared memory
 };
 
 struct Cnt {
@@ -363,6 +361,7 @@ __device__ __forceinline__ float pair_tol(const WarpSmem& S, int la, int tgt)
   return (S.tol64[la] + S.tol64[tgt]) * (1.f + 16.f * kU);
 }
 
+template <bool STAGE>
 __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __restrict__ W,
                                           const KRobotDev& R, uint2 e, uint2& c0, uint2& c1,
                                           uint32_t& jA, uint32_t& jB, uint32_t& jM, const KNode* stage,
@@ -374,8 +373,7 @@ __device__ __forceinline__ int test_entry(const WarpSmem& S, const KWorldDev* __
   const int nodeB = (int)e.x;
   const bool self = tgt < 32;
   const KNode na = W->lnodes[nodeA];
-  // environment nodes of the staged top levels come from shared memory
-  const KNode nb = self ? W->lnodes[nodeB] : (nodeB < nstage ? stage[nodeB] : W->enodes[nodeB]);
+  const KNode nb = self ? W->lnodes[nodeB] : (STAGE && nodeB < nstage ? stage[nodeB] : W->enodes[nodeB]);
   float TA[12];
   load_row(S.T[la], TA);
   const Box32 A = xform_box(TA, na.a, na.b);
@@ -474,16 +472,17 @@ __device__ __noinline__ int share_stack(WarpSmem* all, int me, BlockShare& B, in
 // later steps).  Returns the steps found in contact (bits 0..3: a group has
 // at most 32 / 8 steps), plus kTrOverflow when the spill area ran out.
 // Warp-uniform control flow.
-template <bool FP64, bool EDGES>
+template <bool FP64, bool EDGES, bool STAGE = false>
 __device__ __noinline__ unsigned traverse(WarpSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
                                           int qbase, int qcount, int lane, uint2* spill, int spill_cap,
                                           double (*T64)[12], int& fk64, const EngineArgs& A, int job_flush,
                                           Cnt& cnt, WarpSmem* all, int me, BlockShare& B, int preset, unsigned live,
-                                          int lgL, int nstage)
+                                          int lgL, int nstage = 0)
 {
   const unsigned lt = lanemask_lt();
   const int lmask = (1 << lgL) - 1;
-  const KNode* stage = reinterpret_cast<const KNode*>(reinterpret_cast<const unsigned char*>(all) + kStageOffset);
+  const KNode* stage =
+      STAGE ? reinterpret_cast<const KNode*>(reinterpret_cast<const unsigned char*>(all) + kStageOffset) : nullptr;
   int top = preset, njobs = 0, spill_top = 0;
   unsigned hits = 0;
   S.tol64[lane] = S.delta[lane] + W->eps_extra + R.link_margin[lane & lmask];
@@ -589,7 +588,7 @@ __device__ __noinline__ unsigned traverse(WarpSmem& S, const KWorldDev* __restri
     int outcome = 0;  // 1: two children, 2: leaf job
     uint2 c0 = make_uint2(0, 0), c1 = make_uint2(0, 0);
     uint32_t jA = 0, jB = 0, jM = 0;
-    if (have) outcome = test_entry(S, W, R, e, c0, c1, jA, jB, jM, stage, nstage);
+    if (have) outcome = test_entry<STAGE>(S, W, R, e, c0, c1, jA, jB, jM, stage, nstage);
     cnt.node_pairs += have ? 1 : 0;
     const unsigned m1 = __ballot_sync(0xffffffffu, outcome == 1);
     const unsigned m2 = __ballot_sync(0xffffffffu, outcome == 2);
@@ -617,7 +616,7 @@ __device__ __noinline__ unsigned traverse(WarpSmem& S, const KWorldDev* __restri
 // pairs are common and an inline FP64 contact ends an item early) or as the
 // fallback after a main pass whose list overflowed (otherwise it returns at
 // once); its verdicts overwrite the main pass's.
-template <int MINB, bool FP64, bool EDGES>
+template <int MINB, bool FP64, bool EDGES, bool STAGE = false>
 __global__ void __launch_bounds__(kWarps * 32, MINB)
     k_engine(const KWorldDev* __restrict__ W, const EngineArgs A)
 {
@@ -640,10 +639,11 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
     for (int w = 0; w < kWarps; ++w) B.flag[w] = 2;
     B.no_release = W->share_no_release;
   }
-  // the environment tree's top levels into shared memory (coalesced 16-byte
-  // loads; 2 per node)
-  const int nstage = min(min(A.stage_nodes, stage_nodes_for(MINB)), W->env_nodes);
-  {
+  int nstage = 0;
+  if (STAGE) {
+    // the environment tree's top levels into shared memory (coalesced
+    // 16-byte loads, 2 per node)
+    nstage = min(min(A.stage_nodes, kStageNodes), W->env_nodes);
     const float4* __restrict__ src = reinterpret_cast<const float4*>(W->enodes);
     float4* dst = reinterpret_cast<float4*>(smem_raw + kStageOffset);
     for (int i = threadIdx.x; i < 2 * nstage; i += blockDim.x) dst[i] = __ldg(src + i);
@@ -821,17 +821,17 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
           // drain per group instead of two)
           const int nq = R.nqueries_env + R.nqueries_self;
           if (nq > 0)
-            env_hits = traverse<FP64, EDGES>(S, W, R, R.query_off, nq, lane, spill, spill_cap, T64, fk64, A,
-                                             job_flush, cnt, all, warp, B, 0, live, lgL, nstage);
+            env_hits = traverse<FP64, EDGES, STAGE>(S, W, R, R.query_off, nq, lane, spill, spill_cap, T64, fk64,
+                                                    A, job_flush, cnt, all, warp, B, 0, live, lgL, nstage);
         } else {
           // configurations report the environment and self verdicts apart
           if (A.env_hit != nullptr && R.nqueries_env > 0)
-            env_hits = traverse<FP64, EDGES>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap, T64,
-                                             fk64, A, job_flush, cnt, all, warp, B, 0, live, lgL, nstage);
+            env_hits = traverse<FP64, EDGES, STAGE>(S, W, R, R.query_off, R.nqueries_env, lane, spill, spill_cap,
+                                                    T64, fk64, A, job_flush, cnt, all, warp, B, 0, live, lgL, nstage);
           if (A.self_hit != nullptr && R.nqueries_self > 0)
-            self_hits = traverse<FP64, EDGES>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane,
-                                              spill, spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0, live,
-                                              lgL, nstage);
+            self_hits = traverse<FP64, EDGES, STAGE>(S, W, R, R.query_off + R.nqueries_env, R.nqueries_self, lane,
+                                                     spill, spill_cap, T64, fk64, A, job_flush, cnt, all, warp, B, 0,
+                                                     live, lgL, nstage);
         }
         if ((env_hits | self_hits) & kTrOverflow) {
           if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
@@ -892,8 +892,9 @@ __global__ void __launch_bounds__(kWarps * 32, MINB)
         if (live != 0) {
           int fk64 = 0;
           const bool self = ((S.stack[0].y >> 25) & 63u) < 32u;
-          const unsigned hits = traverse<FP64, EDGES>(S, W, R, 0, 0, lane, spill, spill_cap, T64, fk64, A, job_flush,
-                                                      cnt, all, warp, B, S.don_top, live, lgL, nstage);
+          const unsigned hits = traverse<FP64, EDGES, STAGE>(S, W, R, 0, 0, lane, spill, spill_cap, T64, fk64, A,
+                                                             job_flush, cnt, all, warp, B, S.don_top, live, lgL,
+                                                             nstage);
           if (lane == 0) {
             if (hits & kTrOverflow) {
               set_status(W->status, KGPU_ERR_OVERFLOW);
@@ -1021,7 +1022,7 @@ __global__ void __launch_bounds__(kWarps * 32, 2) k_self_pairs(const KWorldDev* 
         if ((__shfl_sync(0xffffffffu, known, 0) >> tgt) & 1u) continue;
       }
       const unsigned hits = traverse<true, false>(S, W, R, qidx, 1, lane, spill, spill_cap, T64, fk64, A, job_flush,
-                                                  cnt, all, warp, B, 0, 1u, 5, 0);
+                                                  cnt, all, warp, B, 0, 1u, 5);
       if (hits & kTrOverflow) {
         if (lane == 0) set_status(W->status, KGPU_ERR_OVERFLOW);
         found = 2;  // no verdict for this configuration
@@ -1421,23 +1422,26 @@ __global__ void k_jacobian(const KWorldDev* __restrict__ W, int robot, const flo
   }
 }
 
-template <int MINB, bool FP64, bool EDGES>
+template <bool STAGE>
+constexpr size_t engine_smem() { return STAGE ? kStageOffset + sizeof(KNode) * kStageNodes : kBlockSmem; }
+
+template <int MINB, bool FP64, bool EDGES, bool STAGE = false>
 cudaError_t init_engine()
 {
-  return cudaFuncSetAttribute(k_engine<MINB, FP64, EDGES>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)(kStageOffset + sizeof(KNode) * stage_nodes_for(MINB)));
+  return cudaFuncSetAttribute(k_engine<MINB, FP64, EDGES, STAGE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)engine_smem<STAGE>());
 }
 
 // the shared-memory attribute is set once per process by engine_init(), so
 // that launches can be captured into CUDA graphs
-template <int MINB, bool FP64>
+template <int MINB, bool FP64, bool STAGE = false>
 cudaError_t launch_engine(const KWorldDev* W, const EngineArgs& A, int blocks, cudaStream_t s)
 {
-  const size_t smem = kStageOffset + sizeof(KNode) * min(max(A.stage_nodes, 0), stage_nodes_for(MINB));
+  const size_t smem = engine_smem<STAGE>();
   if (A.mode == MODE_EDGES)
-    k_engine<MINB, FP64, true><<<blocks, kWarps * 32, smem, s>>>(W, A);
+    k_engine<MINB, FP64, true, STAGE><<<blocks, kWarps * 32, smem, s>>>(W, A);
   else
-    k_engine<MINB, FP64, false><<<blocks, kWarps * 32, smem, s>>>(W, A);
+    k_engine<MINB, FP64, false, STAGE><<<blocks, kWarps * 32, smem, s>>>(W, A);
   return cudaGetLastError();
 }
 
@@ -1461,7 +1465,9 @@ cudaError_t dispatch_engine(const KWorldDev* W, EngineArgs A, const Scratch& S, 
   switch (per_sm) {
     case 3: err = launch_engine<3, false>(W, A, blocks, s); break;
     case 4: err = launch_engine<4, false>(W, A, blocks, s); break;
-    default: err = launch_engine<2, false>(W, A, blocks, s); break;
+    default:
+      err = A.stage_nodes > 0 ? launch_engine<2, false, true>(W, A, blocks, s) : launch_engine<2, false>(W, A, blocks, s);
+      break;
   }
   if (err != cudaSuccess) return err;
   const int sms = per_sm > 0 && blocks / per_sm > 0 ? blocks / per_sm : 1;
@@ -1489,6 +1495,8 @@ cudaError_t engine_init()
   if (e == cudaSuccess) e = init_engine<4, false, false>();
   if (e == cudaSuccess) e = init_engine<2, true, false>();
   if (e == cudaSuccess) e = init_engine<3, true, false>();
+  if (e == cudaSuccess) e = init_engine<2, false, true, true>();
+  if (e == cudaSuccess) e = init_engine<2, false, false, true>();
   if (e == cudaSuccess)
     e = cudaFuncSetAttribute(k_self_pairs, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)(sizeof(WarpSmem) * kWarps + sizeof(BlockShare)));

@@ -173,7 +173,7 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
   float m32 = FLT_MAX;  // running FP32 minimum (warp-uniform)
   bool overlap = false;
   int top = 0, njobs = 0, ncand = 0;
-  int certA = -1, certB = -1;
+  int certA = -1;  // link triangle of the certified contact
   if (lane == 0) {
     S.b2 = DBL_MAX;
     S.bA = INT_MAX;
@@ -268,7 +268,6 @@ __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict_
           overlap = true;
           const int src = __ffs(mc) - 1;
           certA = __shfl_sync(0xffffffffu, tA, src);
-          certB = __shfl_sync(0xffffffffu, tB, src);
           break;
         }
         m32 = fminf(m32, warp_min(d32));
@@ -950,7 +949,7 @@ __device__ __noinline__ void sd_flush(SelfDistSmem& S, const KWorldDev* __restri
   }
 }
 
-__global__ void __launch_bounds__(kDW * 32, 1) k_self_dist(const KWorldDev* __restrict__ W, const SelfDistArgs A)
+__global__ void __launch_bounds__(kDW * 32, 2) k_self_dist(const KWorldDev* __restrict__ W, const SelfDistArgs A)
 {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

@@ -147,8 +147,8 @@ struct Scratch {
   size_t edge_cap = 0;
   double* dist_work = nullptr;       // soft-min per-waypoint minima, sums, trajectory minima
   size_t dist_work_cap = 0;
-  // launch setting carried with the scratch: environment nodes each engine
-  // block stages in shared memory (capped by what fits at its residency)
+  // launch setting carried with the scratch: environment nodes a staged
+  // engine block copies to shared memory (0: the unstaged kernels)
   int stage_nodes = 0;
 };
 
@@ -239,7 +239,7 @@ struct kgpu_world_s {
   // fallback pass and spill exhaustion in tests
   int pend_cap_opt = 0;
   int spill_cap_opt = 0;
-  int stage_nodes = 0;     // environment tree nodes staged in shared memory per engine block (0..1024)
+  int stage_nodes = 0;     // world option: environment nodes staged per engine block (0..1024; 2 blocks per SM)
   int num_sms = 0;
   bool tables_dirty = true;
   // pinned staging for the host-buffer entry points

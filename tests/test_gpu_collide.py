@@ -284,3 +284,40 @@ def test_nonfinite_config_reports_error(cfg0):
     with pytest.raises(KgpuError) as ei:
         w.check_configs(qq)
     assert ei.value.code == KGPU_ERR_NOT_FINITE
+
+
+@pytest.mark.parametrize("per_sm", [2, 3, 4])
+def test_every_residency_bit_exact(cfg1, per_sm):
+    """Each instantiation of the main pass (2, 3 or 4 blocks per SM: 128, 80
+    or 64 registers, more spilled stack at the lower budgets) gives the
+    oracle's edge and configuration results."""
+    robot, env, (qa, qb, ns), w, o = cfg1
+    fh_o, _ = o.check_edges(qa, qb, ns, nthreads=NT)
+    eo, so, _ = o.check_configs(qa, nthreads=NT)
+    w.set_option("blocks_per_sm", per_sm)
+    try:
+        assert np.array_equal(w.check_edges(qa, qb, ns).cpu().numpy(), fh_o)
+        eh, sh = (x.cpu().numpy() for x in w.check_configs(qa))
+        assert np.array_equal(eh, eo) and np.array_equal(sh, so)
+    finally:
+        w.set_option("blocks_per_sm", 3)
+
+
+@pytest.mark.parametrize("stage", [256, 1024])
+def test_staged_environment_levels_bit_exact(cfg1, stage):
+    """With the top levels of the environment tree staged in shared memory
+    (stage_nodes, the 2-blocks-per-SM kernels), edges and configurations
+    give the oracle's results."""
+    robot, env, (qa, qb, ns), w, o = cfg1
+    fh_o, _ = o.check_edges(qa, qb, ns, nthreads=NT)
+    eo, so, _ = o.check_configs(qa, nthreads=NT)
+    w.set_option("blocks_per_sm", 2)
+    w.set_option("stage_nodes", stage)
+    try:
+        assert w.get_option("stage_nodes") == stage
+        assert np.array_equal(w.check_edges(qa, qb, ns).cpu().numpy(), fh_o)
+        eh, sh = (x.cpu().numpy() for x in w.check_configs(qa))
+        assert np.array_equal(eh, eo) and np.array_equal(sh, so)
+    finally:
+        w.set_option("stage_nodes", 0)
+        w.set_option("blocks_per_sm", 3)
