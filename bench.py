@@ -14,10 +14,12 @@ Reported:
                 (kgpu_check_edges_host: pinned staging, H2D of the edges, D2H
                 of the first-hit indices inside the timed region)
   plain_fp64    the plain FP64 GPU method on the same edges (configs/s)
-  roofline      algorithmic bytes (FP64 oracle's canonical traversal counts:
-                32 B per BVH node pair, 72 B per triangle pair, plus q and the
-                output) per step / step time, against the measured HBM copy
-                bandwidth
+  roofline      of the dominant kernel (the main traversal pass): algorithmic
+                bytes (FP64 oracle's canonical traversal counts: 32 B per BVH
+                node pair, 72 B per triangle pair, plus q and the output) per
+                launch / the pass's own device time (events recorded around it
+                inside the edge plan), against the measured HBM copy
+                bandwidth; whole_plan divides by the step time instead
   cpu_baseline  the FP64 CPU oracle on all host cores over the same edges
   mismatches    first-hit indices that differ from the oracle's (must be 0)
 
@@ -191,15 +193,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def profiled_traffic():
-    """DRAM bytes per checked configuration of the engine kernel, from the
-    committed ncu summary (profiles/k_engine_edges.md), or None."""
-    path = os.path.join(ROOT, "profiles", "k_engine_edges.md")
+def profiled_traffic(name: str = "k_engine_edges.md", key: str = "dram_bytes_per_item"):
+    """DRAM bytes per work unit of a kernel, from its committed ncu summary
+    under profiles/ (a line "<key>: <bytes>"), or None."""
+    path = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(path):
         return None
     with open(path) as f:
         for line in f:
-            if line.startswith("dram_bytes_per_item:"):
+            if line.startswith(key + ":"):
                 try:
                     return float(line.split(":", 1)[1].strip())
                 except ValueError:
@@ -235,11 +237,16 @@ def _oracle_rate_and_bytes(counts, units: int, seconds: float, out_bytes_per_uni
     return units / seconds, per_unit
 
 
-def _roofline(bytes_per_unit: float, units_per_s: float, source: str, oracle_bytes_per_unit=None) -> dict:
+def _roofline(bytes_per_unit: float, units_per_s: float, source: str, oracle_bytes_per_unit=None,
+              traffic_per_unit=None) -> dict:
+    """Roofline of a distance leg per unit (waypoint or configuration):
+    algorithmic bytes x units/s against the measured HBM bandwidth; traffic
+    is the DRAM bytes per unit of the committed ncu capture."""
     peak, kind = peaks()
     achieved = bytes_per_unit * units_per_s / 1e9
     out = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-           "traffic": None, "peak_kind": kind, "algorithmic_bytes_per_unit": bytes_per_unit, "bytes_source": source}
+           "traffic": traffic_per_unit, "traffic_unit": "bytes per unit (ncu capture)", "peak_kind": kind,
+           "algorithmic_bytes_per_unit": bytes_per_unit, "bytes_source": source}
     if oracle_bytes_per_unit is not None:
         out["oracle_traversal_bytes_per_unit"] = oracle_bytes_per_unit
     return out
@@ -250,6 +257,12 @@ def _kernel_bytes_per_unit(stats: dict, units: int, io_bytes: float) -> float:
     own work counters: 32 B per node pair, 72 B per triangle pair (the
     same per-item sizes as the oracle-based figure), plus input and output."""
     return (stats["dist_node_pairs"] * NODE_BYTES + stats["dist_tri_pairs"] * TRI_PAIR_BYTES) / units + io_bytes
+
+
+def _work_per_unit(stats: dict, units: int) -> dict:
+    """The distance kernels' work counters per unit."""
+    return {"link_object_pairs": stats["dist_pairs"] / units, "node_pairs": stats["dist_node_pairs"] / units,
+            "triangle_pairs": stats["dist_tri_pairs"] / units, "fp64_triangle_pairs": stats["dist_fp64"] / units}
 
 
 DIST_BYTES_NOTE = ("the distance kernels' own node-pair and triangle-pair counters x (32 B, 72 B): the FP64 "
@@ -274,6 +287,7 @@ def softmin_leg(reps: int = 2) -> dict:
     w.reset_stats()
     Lg, Gg = (x.cpu().numpy() for x in w.softmin(qd, 0.01))
     kbytes = _kernel_bytes_per_unit(w.stats(), T * Wn, 4 * L + 4 * L + 8.0 / Wn)
+    work = _work_per_unit(w.stats(), T * Wn)
     w.close()
     ts = np.linspace(0, T - 1, 8).astype(int)
     o = Oracle(robot, env)
@@ -290,7 +304,9 @@ def softmin_leg(reps: int = 2) -> dict:
                       f"trajectory's minimum, tau 0.01 m), 2,000 icospheres",
             "max_rel_err": {"L": float(np.max(np.abs(Lg[ts] - L_o) / np.maximum(np.abs(L_o), 1e-12))),
                             "grad": gerr, "sample": f"{len(ts)} trajectories vs the FP64 oracle"},
-            "roofline": _roofline(kbytes, value, DIST_BYTES_NOTE, bpu),
+            "roofline": _roofline(kbytes, value, DIST_BYTES_NOTE, bpu,
+                                  profiled_traffic("k_dist_softmin.md", "dram_bytes_per_waypoint")),
+            "work_per_unit": work,
             "cpu_baseline": {"value": cpu_rate, "unit": "waypoint dist+grad evals/s", "cores": cores, "kind": "port",
                              "sample": f"the same {len(ts)} trajectories, FP64 oracle, std::thread over all cores"}}
 
@@ -312,6 +328,7 @@ def min_distance_leg(reps: int = 2) -> dict:
     w.reset_stats()
     d, p, _, g = (x.cpu().numpy() for x in w.distance(qd, 0.2))
     kbytes = _kernel_bytes_per_unit(w.stats(), B, 4 * L + 8 + 8 + 48 + 4 * L)
+    work = _work_per_unit(w.stats(), B)
     w.close()
     sel = np.arange(0, B, B // 2048)[:2048]
     o = Oracle(robot, env)
@@ -329,7 +346,9 @@ def min_distance_leg(reps: int = 2) -> dict:
             "max_rel_err": {"d": float(np.max(np.abs(d[sel] - d_o) / np.maximum(np.abs(d_o), 1e-12))),
                             "grad": gerr, "pair_mismatches": int((p[sel] != p_o).any(1).sum()),
                             "sample": f"{len(sel)} configurations (every {B // 2048}th) vs the FP64 oracle"},
-            "roofline": _roofline(kbytes, value, DIST_BYTES_NOTE, bpu),
+            "roofline": _roofline(kbytes, value, DIST_BYTES_NOTE, bpu,
+                                  profiled_traffic("k_dist_min_distance.md", "dram_bytes_per_terrain_config")),
+            "work_per_unit": work,
             "cpu_baseline": {"value": cpu_rate, "unit": "config dist+grad evals/s", "cores": cores, "kind": "port",
                              "sample": f"the same {len(sel)} configurations, FP64 oracle, std::thread over all cores"}}
 
@@ -555,10 +574,13 @@ def main():
     if not args.engine_only:
         from klampt_gb300 import autotune
         # tuned on a separately seeded batch of the same size and distribution
-        # (the timed edges are not used for tuning), with the same L2 flush
-        # before each repetition as before each timed step
+        # (the timed edges are not used for tuning), each setting timed as the
+        # CUDA-graph edge plan the timed steps replay, with the same L2 flush
+        # before each repetition as before each timed step; the six fastest
+        # are re-timed 15 times each
         ta, tb, tn = sc.random_edges(robot, args.edges, np.random.default_rng(2001))
-        tuned, _ = autotune.tune_edges(w, ta, tb, tn, reps=3, prep=flush.zero_)
+        tuned, _ = autotune.tune_edges(w, ta, tb, tn, reps=3, prep=flush.zero_, graph=True, finalists=6,
+                                       final_reps=15)
     for kv in args.set:
         k, v = kv.split("=", 1)
         w.set_option(k, float(v))
@@ -586,7 +608,7 @@ def main():
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
-    evs = []
+    evs, main_ms = [], []
     for _ in range(args.steps):
         flush.zero_()
         e0 = torch.cuda.Event(enable_timing=True)
@@ -595,6 +617,11 @@ def main():
         plan.launch()
         e1.record(stream)
         evs.append((e0, e1))
+        # the main pass's own device time, from the events the plan records
+        # around it (read before the next launch records them again; the
+        # wait falls between the timed intervals)
+        stream.synchronize()
+        main_ms.append(plan.main_pass_ms())
     torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
@@ -629,13 +656,13 @@ def main():
     # order), and one thread per (edge, step) (every step on its own) ------
     sub = args.edges
     plain = {}
-    for key, per_step in (("per_edge", False), ("per_step", True)):
-        w.check_edges_plain64(a[:sub], b[:sub], n[:sub], per_step=per_step)  # warm-up
+    for key, thread_per_step in (("per_edge", False), ("per_step", True)):
+        w.check_edges_plain64(a[:sub], b[:sub], n[:sub], per_step=thread_per_step)  # warm-up
         torch.cuda.synchronize()
         p0 = torch.cuda.Event(enable_timing=True)
         p1 = torch.cuda.Event(enable_timing=True)
         p0.record(stream)
-        fh_p = w.check_edges_plain64(a[:sub], b[:sub], n[:sub], sync=False, per_step=per_step)
+        fh_p = w.check_edges_plain64(a[:sub], b[:sub], n[:sub], sync=False, per_step=thread_per_step)
         p1.record(stream)
         w.sync()
         plain[key] = (fh_p.cpu().numpy(), checked_configs(fh_p.cpu().numpy(), ns[:sub]) / (p0.elapsed_time(p1) / 1e3))
@@ -661,7 +688,11 @@ def main():
     cpu_rate_1 = checked_configs(fh_1, ns[:n1]) / (time.perf_counter() - c0)
     items = int(cnt[2])
     alg_bytes = int(cnt[0]) * NODE_BYTES + int(cnt[1]) * TRI_PAIR_BYTES + items * (4 * robot.num_links) + 4 * len(ns)
-    achieved = alg_bytes / (t_dev / args.steps) / 1e9
+    # roofline of the dominant kernel: algorithmic bytes per launch over the
+    # main pass's average device time in the timed region
+    kernel_ms = float(np.mean(main_ms))
+    achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
+    achieved_plan = alg_bytes / (t_dev / args.steps) / 1e9
     peak, peak_kind = peaks()
     traffic_per_item = profiled_traffic()
     traffic = traffic_per_item * per_step if traffic_per_item is not None else None
@@ -686,7 +717,9 @@ def main():
         "mismatches": mismatches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_step": alg_bytes},
+                     "kernel": "k_engine main pass (CUDA events recorded around it inside the edge plan)",
+                     "kernel_ms": kernel_ms, "algorithmic_bytes_per_step": alg_bytes,
+                     "whole_plan": {"achieved": achieved_plan, "frac": achieved_plan / peak}},
         "cpu_baseline": {"value": cpu_rate, "unit": "configs/s", "cores": cores, "kind": "port",
                          "sample": f"all {len(ns)} edges, FP64 oracle, std::thread over all cores",
                          "single_thread": {"value": cpu_rate_1, "unit": "configs/s", "cores": 1,

@@ -448,6 +448,11 @@ kgpu_status kgpu_edge_plan_create(kgpu_world world, int32_t robot, const float* 
                                   const float* qb, const int32_t* nsteps, int32_t E,
                                   int32_t* first_hit, kgpu_edge_plan* out);
 kgpu_status kgpu_edge_plan_launch(kgpu_edge_plan plan, kgpu_stream stream);
+/* Device time (ms) of the main traversal pass of the plan's last launch,
+ * between two events the graph records around it; call after that launch
+ * has completed (the next launch records them again).  No reference
+ * counterpart: it exposes the timing the bench's roofline uses. */
+kgpu_status kgpu_edge_plan_main_pass_ms(kgpu_edge_plan plan, float* ms);
 kgpu_status kgpu_edge_plan_destroy(kgpu_edge_plan plan);
 
 /* ---- captured configuration-batch plans (CUDA-graph replay) -------------- */

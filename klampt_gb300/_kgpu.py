@@ -116,6 +116,7 @@ _SIGS = {
     "kgpu_check_edges_noalloc": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
     "kgpu_edge_plan_create": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
     "kgpu_edge_plan_launch": [_c_p, _c_p],
+    "kgpu_edge_plan_main_pass_ms": [_c_p, _c_p],
     "kgpu_edge_plan_destroy": [_c_p],
     "kgpu_config_plan_create": [_c_p, _i32, _c_p, _c_p, _i32, _i32, _c_p, _c_p, _c_p],
     "kgpu_config_plan_launch": [_c_p, _c_p],

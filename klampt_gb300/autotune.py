@@ -76,11 +76,32 @@ def tune(world: World, run: Callable[[], None], reps: int = 3,
 
 
 def tune_edges(world: World, qa, qb, nsteps, robot: int = 0, reps: int = 3,
-               prep: Optional[Callable[[], None]] = None):
+               prep: Optional[Callable[[], None]] = None, graph: bool = False,
+               finalists: int = 4, final_reps: int = 9):
+    """The edge grid on a sample batch.  graph=True times each setting as the
+    CUDA-graph edge plan it would be replayed as (one plan per setting,
+    recorded on first use and destroyed afterwards) instead of eager calls."""
     a = torch.as_tensor(qa).cuda()
     b = torch.as_tensor(qb).cuda()
     n = torch.as_tensor(nsteps).cuda()
-    return tune(world, lambda: world.check_edges(a, b, n, robot=robot, sync=False), reps, GRID_EDGES, prep)
+    if not graph:
+        return tune(world, lambda: world.check_edges(a, b, n, robot=robot, sync=False), reps, GRID_EDGES, prep,
+                    finalists, final_reps)
+    out = torch.empty(a.shape[0], dtype=torch.int32, device="cuda")
+    plans = {}
+
+    def run():
+        key = tuple(world.get_option(k) for k in GRID_EDGES)
+        if key not in plans:
+            plans[key] = world.edge_plan(a, b, n, out, robot=robot)
+        plans[key].launch()
+
+    try:
+        return tune(world, run, reps, GRID_EDGES, prep, finalists, final_reps)
+    finally:
+        world.sync()
+        for p in plans.values():
+            p.close()
 
 
 def tune_configs(world: World, q, robot: int = 0, reps: int = 3):

@@ -1222,9 +1222,14 @@ kgpu_status kgpu_edge_plan_create(kgpu_world w, int32_t robot, const float* qa, 
   CK(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   kgpu_edge_plan p = new kgpu_edge_plan_s();
   p->world = w;
-  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  cudaError_t e = cudaEventCreate(&p->ev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&p->ev[1]);
+  if (e == cudaSuccess) e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
   if (e == cudaSuccess) {
-    cudaError_t le = launch_check_edges(w->d_dev, w->d_status, engine_scratch(w, w->scratch), robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
+    Scratch S = engine_scratch(w, w->scratch);
+    S.main_pass_ev[0] = p->ev[0];
+    S.main_pass_ev[1] = p->ev[1];
+    cudaError_t le = launch_check_edges(w->d_dev, w->d_status, S, robot, qa, qb, nsteps, E, first_hit, grid_blocks(w),
                                         w->blocks_per_sm, cs, w->grab, w->job_flush, w->edge_chunk, w->fp64_inline);
     e = cudaStreamEndCapture(cs, &p->graph);
     if (e == cudaSuccess && le != cudaSuccess) e = le;
@@ -1247,6 +1252,13 @@ kgpu_status kgpu_edge_plan_launch(kgpu_edge_plan p, kgpu_stream s)
   return KGPU_OK;
 }
 
+kgpu_status kgpu_edge_plan_main_pass_ms(kgpu_edge_plan p, float* ms)
+{
+  if (!p || !p->exec || !ms) return fail(KGPU_ERR_INVALID, "null argument");
+  CK(cudaEventElapsedTime(ms, p->ev[0], p->ev[1]));
+  return KGPU_OK;
+}
+
 kgpu_status kgpu_edge_plan_destroy(kgpu_edge_plan p)
 {
   if (!p) return KGPU_OK;
@@ -1255,6 +1267,8 @@ kgpu_status kgpu_edge_plan_destroy(kgpu_edge_plan p)
     p->world->live_plans--;
   }
   if (p->graph) cudaGraphDestroy(p->graph);
+  for (cudaEvent_t ev : p->ev)
+    if (ev) cudaEventDestroy(ev);
   delete p;
   return KGPU_OK;
 }

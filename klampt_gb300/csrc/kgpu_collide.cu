@@ -1461,6 +1461,9 @@ cudaError_t dispatch_engine(const KWorldDev* W, EngineArgs A, const Scratch& S, 
   A.pend = S.pend;
   A.pend_cap = S.pend_cap;
   A.stage_nodes = S.stage_nodes;
+  if (S.main_pass_ev[0] != nullptr &&
+      (err = cudaEventRecordWithFlags(S.main_pass_ev[0], s, cudaEventRecordExternal)) != cudaSuccess)
+    return err;
   if (A.inline64) return per_sm == 3 ? launch_engine<3, true>(W, A, blocks, s) : launch_engine<2, true>(W, A, blocks, s);
   switch (per_sm) {
     case 3: err = launch_engine<3, false>(W, A, blocks, s); break;
@@ -1470,6 +1473,9 @@ cudaError_t dispatch_engine(const KWorldDev* W, EngineArgs A, const Scratch& S, 
       break;
   }
   if (err != cudaSuccess) return err;
+  if (S.main_pass_ev[1] != nullptr &&
+      (err = cudaEventRecordWithFlags(S.main_pass_ev[1], s, cudaEventRecordExternal)) != cudaSuccess)
+    return err;
   const int sms = per_sm > 0 && blocks / per_sm > 0 ? blocks / per_sm : 1;
   k_band<<<2 * sms, kWarps * 32, 0, s>>>(W, A);
   if ((err = cudaGetLastError()) != cudaSuccess) return err;

@@ -150,6 +150,9 @@ struct Scratch {
   // launch setting carried with the scratch: environment nodes a staged
   // engine block copies to shared memory (0: the unstaged kernels)
   int stage_nodes = 0;
+  // edge plans: events recorded (as graph nodes) around the main pass, so
+  // that its own device time can be read after a launch
+  cudaEvent_t main_pass_ev[2] = {nullptr, nullptr};
 };
 
 }  // namespace kgpu
@@ -258,6 +261,7 @@ struct kgpu_edge_plan_s {
   kgpu_world world = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};  // around the main pass
 };
 
 struct kgpu_config_plan_s {

@@ -177,6 +177,13 @@ class EdgePlan:
     def launch(self):
         check(lib().kgpu_edge_plan_launch(self.handle, _stream()))
 
+    def main_pass_ms(self) -> float:
+        """Device time of the last launch's main traversal pass (call after
+        that launch has completed)."""
+        ms = ctypes.c_float()
+        check(lib().kgpu_edge_plan_main_pass_ms(self.handle, ctypes.byref(ms)))
+        return float(ms.value)
+
     def close(self):
         if self.handle:
             lib().kgpu_edge_plan_destroy(self.handle)

@@ -156,6 +156,20 @@ def test_autotuner_keeps_results(world0):
     assert all(np.array_equal(x.cpu().numpy(), y.cpu().numpy()) for x, y in zip(before, after))
 
 
+def test_edge_autotuner_graph_mode_keeps_results(world0):
+    """Edge tuning with every setting timed as its CUDA-graph plan leaves the
+    fastest setting in the world, destroys its plans, and changes no result."""
+    from klampt_gb300 import autotune
+    W, robot, env, q, o = world0
+    w = W.engine
+    qa, qb, ns = sc.random_edges(robot, 256, np.random.default_rng(77))
+    before = w.check_edges(qa, qb, ns).cpu().numpy()
+    best, table = autotune.tune_edges(w, qa, qb, ns, reps=1, graph=True, finalists=2, final_reps=2)
+    assert len(table) == 54 and set(best) == {"blocks_per_sm", "grab", "job_flush", "fp64_inline", "edge_chunk"}
+    assert all(w.get_option(k) == v for k, v in best.items())
+    assert np.array_equal(w.check_edges(qa, qb, ns).cpu().numpy(), before)
+
+
 def test_heterogeneous_batch_matches_oracle():
     """Four robots (6-DOF, 7-DOF, 12-DOF dual arm, 30-DOF humanoid) in one
     launch, every configuration checked against its own robot's oracle."""

@@ -198,9 +198,17 @@ def test_cfg1_edges_host_and_graph(cfg1):
     plan = w.edge_plan(a, b, n, out)
     for _ in range(3):
         out.fill_(-7)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
         plan.launch()
+        e1.record()
         w.sync()
         assert np.array_equal(out.cpu().numpy(), ref)
+        # the main pass's own time, from the events inside the graph, lies
+        # within the whole launch's
+        main_ms = plan.main_pass_ms()
+        assert 0.0 < main_ms <= e0.elapsed_time(e1)
     plan.close()
 
 
