@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--edges", type=int, default=16384)
     p.add_argument("--engine-only", action="store_true",
                    help="only warm-up + timed edge-plan launches (profiling runs); prints the device time")
+    p.add_argument("--host-only", action="store_true",
+                   help="with --engine-only: time the end-to-end call with host buffers instead of the plan")
     p.add_argument("--set", action="append", default=[], metavar="NAME=VALUE",
                    help="world option for --engine-only runs (e.g. blocks_per_sm=2)")
     p.add_argument("--dist-only", type=int, default=0, metavar="N",
@@ -596,7 +598,10 @@ def main():
     if args.engine_only:
         t0 = time.perf_counter()
         for _ in range(args.steps):
-            plan.launch()
+            if args.host_only:
+                w.check_edges_host(qa, qb, ns)
+            else:
+                plan.launch()
         w.sync()
         print(json.dumps({"engine_only": True, "edges": args.edges, "configs_checked_per_step": per_step,
                           "ms_per_step": 1e3 * (time.perf_counter() - t0) / max(1, args.steps)}), flush=True)
