@@ -866,12 +866,10 @@ kgpu_status kgpu_world_get_option(kgpu_world w, const char* name, double* v)
   return KGPU_OK;
 }
 
-kgpu_status kgpu_world_sync(kgpu_world w, kgpu_stream stream)
+// The status word a sync read: 0, or the code the kernels set (then cleared
+// on the device and reported with its message).
+static kgpu_status status_result(kgpu_world w, int st)
 {
-  if (!w) return fail(KGPU_ERR_INVALID, "null world");
-  CK(cudaStreamSynchronize((cudaStream_t)stream));
-  int st = 0;
-  CK(cudaMemcpy(&st, w->d_status, sizeof(int), cudaMemcpyDeviceToHost));
   if (st != 0) {
     CK(cudaMemset(w->d_status, 0, sizeof(int)));
     const char* what = st == KGPU_ERR_NOT_FINITE ? "non-finite or out-of-range configuration value"
@@ -882,6 +880,25 @@ kgpu_status kgpu_world_sync(kgpu_world w, kgpu_stream stream)
     return fail(st, "device status: %s", what);
   }
   return KGPU_OK;
+}
+
+kgpu_status kgpu_world_sync(kgpu_world w, kgpu_stream stream)
+{
+  if (!w) return fail(KGPU_ERR_INVALID, "null world");
+  CK(cudaStreamSynchronize((cudaStream_t)stream));
+  int st = 0;
+  CK(cudaMemcpy(&st, w->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  return status_result(w, st);
+}
+
+// kgpu_world_sync for the host-buffer calls: the status word is copied into
+// pinned memory on the call's stream behind its results, so that one wait
+// returns both
+static kgpu_status sync_status_pinned(kgpu_world w, cudaStream_t s, int* pinned_status)
+{
+  CK(cudaMemcpyAsync(pinned_status, w->d_status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return status_result(w, *pinned_status);
 }
 
 kgpu_status kgpu_world_get_stats(kgpu_world w, kgpu_stats* out)
@@ -1164,7 +1181,7 @@ kgpu_status kgpu_check_configs_host(kgpu_world w, int32_t robot, const float* q,
   if (B < 0 || (B > 0 && !q)) return fail(KGPU_ERR_INVALID, "bad buffers");
   int L = w->robots[robot]->nlinks;
   size_t qb = al((size_t)B * L * sizeof(float)), ob = al((size_t)B);
-  if ((st = ensure_stage(w, qb + 2 * ob))) return st;
+  if ((st = ensure_stage(w, qb + 2 * ob + al(sizeof(int))))) return st;
   char* hp = (char*)w->pinned;
   char* dp = (char*)w->dstage;
   cudaStream_t s = w->host_stream;
@@ -1175,7 +1192,7 @@ kgpu_status kgpu_check_configs_host(kgpu_world w, int32_t robot, const float* q,
   if (st) return st;
   if (env_hit) CK(cudaMemcpyAsync(hp + qb, dp + qb, B, cudaMemcpyDeviceToHost, s));
   if (self_hit) CK(cudaMemcpyAsync(hp + qb + ob, dp + qb + ob, B, cudaMemcpyDeviceToHost, s));
-  if ((st = kgpu_world_sync(w, s))) return st;
+  if ((st = sync_status_pinned(w, s, (int*)(hp + qb + 2 * ob)))) return st;
   if (env_hit) memcpy(env_hit, hp + qb, B);
   if (self_hit) memcpy(self_hit, hp + qb + ob, B);
   return KGPU_OK;
@@ -1190,7 +1207,7 @@ kgpu_status kgpu_check_edges_host(kgpu_world w, int32_t robot, const float* qa, 
   int L = w->robots[robot]->nlinks;
   size_t qbytes = (size_t)E * L * sizeof(float);
   size_t o1 = al(qbytes), o2 = o1 + al(qbytes), o3 = o2 + al((size_t)E * 4);
-  size_t total = o3 + al((size_t)E * 4);
+  size_t o4 = o3 + al((size_t)E * 4), total = o4 + al(sizeof(int));
   if ((st = ensure_stage(w, total))) return st;
   char* hp = (char*)w->pinned;
   char* dp = (char*)w->dstage;
@@ -1203,7 +1220,7 @@ kgpu_status kgpu_check_edges_host(kgpu_world w, int32_t robot, const float* qa, 
                         (int32_t*)(dp + o3), s);
   if (st) return st;
   CK(cudaMemcpyAsync(hp + o3, dp + o3, (size_t)E * 4, cudaMemcpyDeviceToHost, s));
-  if ((st = kgpu_world_sync(w, s))) return st;
+  if ((st = sync_status_pinned(w, s, (int*)(hp + o4)))) return st;
   memcpy(first_hit, hp + o3, (size_t)E * 4);
   return KGPU_OK;
 }

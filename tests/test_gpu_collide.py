@@ -292,6 +292,21 @@ def test_nonfinite_config_reports_error(cfg0):
     with pytest.raises(KgpuError) as ei:
         w.check_configs(qq)
     assert ei.value.code == KGPU_ERR_NOT_FINITE
+    # the host-buffer calls report the device status with their results, and
+    # the world stays usable
+    with pytest.raises(KgpuError) as ei:
+        w.check_configs_host(qq)
+    assert ei.value.code == KGPU_ERR_NOT_FINITE
+    qb = q[16:32].copy()
+    ns = np.full(16, 5, np.int32)
+    with pytest.raises(KgpuError) as ei:
+        w.check_edges_host(qq, qb, ns)
+    assert ei.value.code == KGPU_ERR_NOT_FINITE
+    eo, so, _ = o.check_configs(q[:16], nthreads=NT)
+    eh, sh = w.check_configs_host(q[:16])
+    assert np.array_equal(eh, eo.astype(bool)) and np.array_equal(sh, so.astype(bool))
+    fo, _ = o.check_edges(q[:16], qb, ns, nthreads=NT)
+    assert np.array_equal(w.check_edges_host(q[:16], qb, ns), fo)
 
 
 @pytest.mark.parametrize("per_sm", [2, 3, 4])
