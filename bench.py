@@ -439,6 +439,8 @@ def secondary_metrics(reps: int = 2) -> dict:
     # configuration batches of one robot (environment and self verdicts, and
     # feasibility) on the same scene
     q1 = torch.as_tensor(sc.uniform_configs(robot1, 262144, np.random.default_rng(2003))).cuda()
+    # launch options tuned on a separately seeded batch of the same size
+    tuned1, _ = autotune.tune_configs(w1, sc.uniform_configs(robot1, 262144, np.random.default_rng(2004)), reps=2)
     ms_c = _event_ms(lambda: w1.check_configs(q1, sync=False), reps)
     ms_f = _event_ms(lambda: w1.is_feasible(q1, sync=False), reps)
     ms_p = _event_ms(lambda: w1.check_configs_plain64(q1, sync=False), 1)
@@ -448,6 +450,7 @@ def secondary_metrics(reps: int = 2) -> dict:
     out["configs"] = {"value": q1.shape[0] / (ms_c / 1e3), "unit": "configs/s",
                       "sample": "262,144 uniform configurations of the 7-DOF arm among 2,000 icospheres; "
                                 "environment and self verdicts apart",
+                      "autotuned": tuned1,
                       "feasibility": {"value": q1.shape[0] / (ms_f / 1e3), "unit": "configs/s"},
                       "plain_fp64": {"value": q1.shape[0] / (ms_p / 1e3), "unit": "configs/s",
                                      "method": "one thread per configuration, FP64 FK and traversal",
