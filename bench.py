@@ -664,13 +664,13 @@ def main():
     # order), and one thread per (edge, step) (every step on its own) ------
     sub = args.edges
     plain = {}
-    for key, thread_per_step in (("per_edge", False), ("per_step", True)):
-        w.check_edges_plain64(a[:sub], b[:sub], n[:sub], per_step=thread_per_step)  # warm-up
+    for key, grain in (("per_edge", {}), ("per_step", {"per_step": True}), ("per_pair", {"per_pair": True})):
+        w.check_edges_plain64(a[:sub], b[:sub], n[:sub], **grain)  # warm-up
         torch.cuda.synchronize()
         p0 = torch.cuda.Event(enable_timing=True)
         p1 = torch.cuda.Event(enable_timing=True)
         p0.record(stream)
-        fh_p = w.check_edges_plain64(a[:sub], b[:sub], n[:sub], sync=False, per_step=thread_per_step)
+        fh_p = w.check_edges_plain64(a[:sub], b[:sub], n[:sub], sync=False, **grain)
         p1.record(stream)
         w.sync()
         plain[key] = (fh_p.cpu().numpy(), checked_configs(fh_p.cpu().numpy(), ns[:sub]) / (p0.elapsed_time(p1) / 1e3))
@@ -720,8 +720,10 @@ def main():
         "gpu_launches": 7 * args.steps,  # per edge plan: 3 prep kernels, main pass, k_band, fallback, finalize
         "plain_fp64": {"value": plain_rate, "unit": "configs/s", "edges": sub, "speedup": value / plain_rate,
                        "per_edge": plain["per_edge"][1], "per_step": plain["per_step"][1],
+                       "per_pair": plain["per_pair"][1],
                        "method": "FP64 FK, FP64 BVH traversal and triangle tests per thread; value = the "
-                                 "faster of one thread per edge (in order) and one per (edge, step)"},
+                                 "fastest of one thread per edge (in order), one per (edge, step) and one per "
+                                 "(edge, step, link-group or link-link query)"},
         "mismatches": mismatches,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "peak_kind": peak_kind,

@@ -303,6 +303,13 @@ kgpu_status kgpu_check_edges_plain64(kgpu_world world, int32_t robot, const floa
 kgpu_status kgpu_check_edges_plain64_steps(kgpu_world world, int32_t robot, const float* qa,
                                            const float* qb, const int32_t* nsteps, int32_t E,
                                            int32_t* first_hit, kgpu_stream stream);
+/* The plain FP64 method with one thread per (edge, step, query): each
+ * thread forms its step's FP64 transforms and checks one link-group or
+ * link-link pair (the per-pair loop of PlannerSettings.cpp:269-331 split
+ * across threads); same outputs as kgpu_check_edges. */
+kgpu_status kgpu_check_edges_plain64_pairs(kgpu_world world, int32_t robot, const float* qa,
+                                           const float* qb, const int32_t* nsteps, int32_t E,
+                                           int32_t* first_hit, kgpu_stream stream);
 
 /* Minimum signed link-obstacle distance per configuration, clamped at
  * `cutoff`, with its gradient d/dq.  Replaces the per-pair

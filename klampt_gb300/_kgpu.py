@@ -94,6 +94,7 @@ _SIGS = {
     "kgpu_check_configs_plain64": [_c_p, _i32, _c_p, _i32, _c_p, _c_p, _c_p],
     "kgpu_check_edges_plain64": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
     "kgpu_check_edges_plain64_steps": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
+    "kgpu_check_edges_plain64_pairs": [_c_p, _i32, _c_p, _c_p, _c_p, _i32, _c_p, _c_p],
     "kgpu_distance": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p, _c_p, _c_p, _c_p],
     "kgpu_self_distance": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _c_p, _c_p, _c_p, _c_p, _c_p],
     "kgpu_self_pair_distances": [_c_p, _i32, _c_p, _i32, ctypes.c_double, _i32, _c_p, _c_p],

@@ -1036,6 +1036,19 @@ kgpu_status kgpu_check_edges_plain64_steps(kgpu_world w, int32_t robot, const fl
                        "kgpu_check_edges_plain64_steps");
 }
 
+kgpu_status kgpu_check_edges_plain64_pairs(kgpu_world w, int32_t robot, const float* qa, const float* qb,
+                                           const int32_t* nsteps, int32_t E, int32_t* first_hit, kgpu_stream s)
+{
+  kgpu_status st = check_world(w, robot);
+  if (st) return st;
+  if (E < 0 || E == INT32_MAX || (E > 0 && (!qa || !qb || !nsteps || !first_hit)))
+    return fail(KGPU_ERR_INVALID, "bad buffers");
+  if ((st = ensure_edge_scratch(w, E + 1))) return st;  // the step offsets
+  return launch_status(launch_plain64_edge_pairs(w->dev, robot, qa, qb, nsteps, E, first_hit, w->scratch.edge_perm,
+                                                 w->num_sms, (cudaStream_t)s),
+                       "kgpu_check_edges_plain64_pairs");
+}
+
 kgpu_status kgpu_distance(kgpu_world w, int32_t robot, const float* q, int32_t B, double cutoff, double* d,
                           int32_t* pair, double* cp, float* grad, kgpu_stream s)
 {

@@ -295,6 +295,9 @@ cudaError_t launch_plain64_edges(const KWorldDev& W, int robot, const float* qa,
                                  const float* qb, const int* nsteps, int E, int* first_hit,
                                  cudaStream_t s);
 // one thread per (edge, step); off: E + 1 ints of scratch
+cudaError_t launch_plain64_edge_pairs(const KWorldDev& W, int robot, const float* qa, const float* qb,
+                                      const int* nsteps, int E, int* first_hit, int* off, int num_sms,
+                                      cudaStream_t s);
 cudaError_t launch_plain64_edge_steps(const KWorldDev& W, int robot, const float* qa, const float* qb,
                                       const int* nsteps, int E, int* first_hit, int* off, int num_sms,
                                       cudaStream_t s);

@@ -243,6 +243,46 @@ __global__ void k_plain_edge_steps(KWorldDev W, int robot, const float* qa, cons
   }
 }
 
+// The plain method with one thread per (edge, step, query): each thread
+// forms its step's FP64 transforms itself and traverses one (link, group)
+// or (link, link) query; a contact or a joint-limit violation records the
+// step by atomicMin.  The finest grain the plain method has (a configuration
+// check split into its pair checks).
+__global__ void k_plain_edge_pairs(KWorldDev W, int robot, const float* qa, const float* qb, const int* nsteps,
+                                   int E, const int* off, int* first_hit)
+{
+  const KRobotDev& R = W.robots[robot];
+  const int nl = R.nlinks;
+  const int nq = R.nqueries_env + R.nqueries_self;
+  if (nq <= 0) return;
+  const long long total = (long long)off[E] * nq;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int s = (int)(t / nq), qi = (int)(t - (long long)s * nq);
+    int lo = 0, hi = E - 1;  // the edge e with off[e] <= s < off[e + 1]
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (off[mid] <= s) lo = mid; else hi = mid - 1;
+    }
+    const int e = lo, k = s - off[e], n = nsteps[e];
+    double qd[kMaxLinks];
+    bool ok = true, finite = true;
+    for (int i = 0; i < nl; ++i) {
+      qd[i] = kx_interp((double)qa[(size_t)e * nl + i], (double)qb[(size_t)e * nl + i], k, n);
+      if (!(fabs(qd[i]) < 1.0e6)) finite = false;
+      if (qd[i] < R.qmin64[i] || qd[i] > R.qmax64[i]) ok = false;
+    }
+    if (!finite) { set_status(W.status, KGPU_ERR_NOT_FINITE); continue; }
+    if (!ok) { atomicMin(first_hit + e, k); continue; }
+    double T[kMaxLinks][12];
+    fk64_all(R, qd, T);
+    const uint32_t qw = W.queries[R.query_off + qi];
+    const int r = plain_query(W, R, T, qw & 0xff, (qw >> 8) & 0xff);
+    if (r == 2) { set_status(W.status, KGPU_ERR_OVERFLOW); continue; }
+    if (r == 1) atomicMin(first_hit + e, k);
+  }
+}
+
 __global__ void k_plain_fill(int* a, int n, int v)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -266,6 +306,19 @@ cudaError_t launch_plain64_edge_steps(const KWorldDev& W, int robot, const float
   k_plain_fill<<<gb, tb, 0, s>>>(first_hit, E, INT_MAX);
   k_plain_step_offsets<<<1, 1024, 0, s>>>(nsteps, E, off, W.status);
   k_plain_edge_steps<<<num_sms * 16, 64, 0, s>>>(W, robot, qa, qb, nsteps, E, off, first_hit);
+  k_plain_unset<<<gb, tb, 0, s>>>(first_hit, E);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_plain64_edge_pairs(const KWorldDev& W, int robot, const float* qa, const float* qb,
+                                      const int* nsteps, int E, int* first_hit, int* off, int num_sms,
+                                      cudaStream_t s)
+{
+  if (E <= 0) return cudaSuccess;
+  const int tb = 256, gb = (E + tb - 1) / tb;
+  k_plain_fill<<<gb, tb, 0, s>>>(first_hit, E, INT_MAX);
+  k_plain_step_offsets<<<1, 1024, 0, s>>>(nsteps, E, off, W.status);
+  k_plain_edge_pairs<<<num_sms * 16, 64, 0, s>>>(W, robot, qa, qb, nsteps, E, off, first_hit);
   k_plain_unset<<<gb, tb, 0, s>>>(first_hit, E);
   return cudaGetLastError();
 }

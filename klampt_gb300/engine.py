@@ -363,15 +363,17 @@ class World:
         return eh, sh
 
     def check_edges_plain64(self, qa, qb, nsteps, robot: int = 0, sync: bool = True,
-                            per_step: bool = False) -> torch.Tensor:
-        """The plain FP64 method: one thread per edge (in order), or with
-        per_step one thread per (edge, step)."""
+                            per_step: bool = False, per_pair: bool = False) -> torch.Tensor:
+        """The plain FP64 method: one thread per edge (in order), with
+        per_step one thread per (edge, step), with per_pair one thread per
+        (edge, step, query)."""
         L = self.robots[robot].num_links
         a = _dev(qa, torch.float32).reshape(-1, L)
         b = _dev(qb, torch.float32).reshape(-1, L)
         n = _dev(nsteps, torch.int32).reshape(-1)
         out = torch.empty(a.shape[0], dtype=torch.int32, device="cuda")
-        fn = lib().kgpu_check_edges_plain64_steps if per_step else lib().kgpu_check_edges_plain64
+        fn = (lib().kgpu_check_edges_plain64_pairs if per_pair else
+              lib().kgpu_check_edges_plain64_steps if per_step else lib().kgpu_check_edges_plain64)
         check(fn(self.handle, robot, _dptr(a), _dptr(b), _dptr(n), a.shape[0], _dptr(out), _stream()))
         if sync:
             self.sync()

@@ -183,6 +183,9 @@ def test_cfg1_edges_plain64_exact(cfg1):
     # one thread per (edge, step): the same first hits
     fs = w.check_edges_plain64(qa[sel], qb[sel], ns[sel], per_step=True).cpu().numpy()
     assert np.array_equal(fs, fh_o)
+    # one thread per (edge, step, query)
+    fp = w.check_edges_plain64(qa[sel], qb[sel], ns[sel], per_pair=True).cpu().numpy()
+    assert np.array_equal(fp, fh_o)
 
 
 def test_cfg1_edges_host_and_graph(cfg1):
