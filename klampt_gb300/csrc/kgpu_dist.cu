@@ -153,6 +153,46 @@ __device__ __noinline__ void flush_cands(DistSmem& S, const KWorldDev* __restric
   }
 }
 
+// An upper bound on the distance between the surfaces of link l and object
+// o: the link vertex nearest the centre of o's box and the vertex of o (the
+// first vertex of each of its triangles) nearest that link vertex are both
+// surface points; widened by the FP32 placement bounds and rounding.  Seeds
+// a pair's running minimum, so that its traversal prunes from the start.
+constexpr int kSeedMaxTris = 4096;  // objects up to this size are scanned for a seed
+
+__device__ __noinline__ float pair_seed(DistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R, int lane,
+                                        int l, int o)
+{
+  const KNode ob = W->enodes[W->obj_root[o]];
+  const float* TA = S.T[l];
+  const int vf = R.link_vert_first[l], vc = R.link_vert_count[l];
+  float bd = FLT_MAX;
+  float3 bv = make_float3(ob.a.x, ob.a.y, ob.a.z);
+  for (int v = lane; v < vc; v += 32) {
+    const float4 x = __ldg(W->lvert32 + vf + v);
+    const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
+    const float dx = w.x - ob.a.x, dy = w.y - ob.a.y, dz = w.z - ob.a.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 < bd) { bd = d2; bv = w; }
+  }
+  const float m = warp_min(bd);
+  const unsigned mm = __ballot_sync(0xffffffffu, bd == m);
+  const int src = mm ? __ffs(mm) - 1 : 0;
+  bv = make_float3(__shfl_sync(0xffffffffu, bv.x, src), __shfl_sync(0xffffffffu, bv.y, src),
+                   __shfl_sync(0xffffffffu, bv.z, src));
+  const int ff = W->obj_leaf_first[o], fc = W->obj_leaf_count[o];
+  if (fc > kSeedMaxTris) return FLT_MAX;  // large objects (terrains): no seed
+  float bo = FLT_MAX;
+  for (int t = lane; t < fc; t += 32) {
+    const float4 y = __ldg(W->etri32 + 3 * (size_t)(ff + t));
+    const float dx = y.x - bv.x, dy = y.y - bv.y, dz = y.z - bv.z;
+    bo = fminf(bo, dx * dx + dy * dy + dz * dz);
+  }
+  bo = warp_min(bo);
+  if (!(bo < FLT_MAX)) return FLT_MAX;
+  return sqrtf(bo) * (1.f + 1e-5f) + 2.f * (S.delta[l] + W->eps_env + 2.f * W->eps_extra) + 1e-6f;
+}
+
 struct PairOut {
   int found;
   double d;
@@ -163,14 +203,14 @@ struct PairOut {
 // Signed distance of (link l, object o) below `bound` (found = d < bound).
 __device__ __noinline__ void eval_pair(DistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
                                        double (*T64)[12], int& fk64, int lane, int l, int o, double bound,
-                                       PairOut& out, DCnt& cnt)
+                                       PairOut& out, DCnt& cnt, float seed = FLT_MAX)
 {
   cnt.pairs++;
   const unsigned lt = lanemask_lt();
   const float dl = S.delta[l] + W->eps_extra;
   const float de = W->eps_env + W->eps_extra;
   const float fb = bound > 0.0 ? (bound < 1e30 ? (float)bound * 1.000001f + 1e-7f : FLT_MAX) : 0.f;
-  float m32 = FLT_MAX;  // running FP32 minimum (warp-uniform)
+  float m32 = seed;  // running FP32 minimum (warp-uniform); seed: an upper bound known in advance
   bool overlap = false;
   int top = 0, njobs = 0, ncand = 0;
   int certA = -1;  // link triangle of the certified contact
@@ -797,7 +837,8 @@ __global__ void __launch_bounds__(kDW * 32, 2) k_dist(const KWorldDev* __restric
             const int np = gather_objects(S, W, R, lane, l, fbnd, -1.f, 0, top);
             for (int k = 0; k < np; ++k) {
               PairOut po;
-              eval_pair(S, W, R, T64, fk64, lane, l, S.pobj[k], bnd, po, cnt);
+              const int o = S.pobj[k];
+              eval_pair(S, W, R, T64, fk64, lane, l, o, bnd, po, cnt, pair_seed(S, W, R, lane, l, o));
               if (!po.found) continue;
               const double e = exp(-(po.d - m) / A.tau);
               sum += e;
