@@ -767,7 +767,9 @@ __global__ void __launch_bounds__(kDW * 32, 2) k_dist(const KWorldDev* __restric
           if (vm > (float)fmax(best, 0.0) * 1.00001f + 1e-6f) break;
           const int o = S.pobj[k], l = S.plink[k];
           PairOut po;
-          eval_pair(S, W, R, T64, fk64, lane, l, o, nextafter(best, 1e300), po, cnt);
+          // the first pair has no running bound to prune with yet: seed it
+          eval_pair(S, W, R, T64, fk64, lane, l, o, nextafter(best, 1e300), po, cnt,
+                    bl < 0 ? pair_seed(S, W, R, lane, l, o) : FLT_MAX);
           if (po.found && (po.d < best || (po.d == best && (l < bl || (l == bl && o < bo))))) {
             best = po.d;
             bl = l;
@@ -916,6 +918,10 @@ constexpr int kSDStack = 512;
 constexpr int kSDJobs = 64;
 constexpr int kSDCand = 128;
 
+struct __align__(16) SelfDistSmem;
+__device__ __noinline__ float link_pair_seed(SelfDistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                             int lane, int i, int j);
+
 struct __align__(16) SelfDistSmem {
   float T[kMaxLinks][12];
   float delta[kMaxLinks];
@@ -944,6 +950,47 @@ struct SelfDistArgs {
   double* dpair;   // per-pair mode: [B, L (L - 1) / 2], each pair's own minimum
   int all_pairs;   // per-pair mode: every pair i < j whose links have geometry, enabled or not
 };
+
+// An upper bound on the distance between the surfaces of links i and j:
+// the vertex of i nearest the centre of j's root box and the vertex of j
+// nearest that vertex (both surface points), widened by the links' FP32
+// placement bounds and rounding.
+__device__ __noinline__ float link_pair_seed(SelfDistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R,
+                                             int lane, int i, int j)
+{
+  const KNode nj = W->lnodes[R.link_root[j]];
+  const float3 cj = xform32(S.T[j], make_float3(nj.a.x, nj.a.y, nj.a.z));
+  float bd = FLT_MAX;
+  float3 bv = cj;
+  {
+    const int vf = R.link_vert_first[i], vc = R.link_vert_count[i];
+    for (int v = lane; v < vc; v += 32) {
+      const float4 x = __ldg(W->lvert32 + vf + v);
+      const float3 w = xform32(S.T[i], make_float3(x.x, x.y, x.z));
+      const float dx = w.x - cj.x, dy = w.y - cj.y, dz = w.z - cj.z;
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      if (d2 < bd) { bd = d2; bv = w; }
+    }
+  }
+  const float m = warp_min(bd);
+  const unsigned mm = __ballot_sync(0xffffffffu, bd == m);
+  const int src = mm ? __ffs(mm) - 1 : 0;
+  bv = make_float3(__shfl_sync(0xffffffffu, bv.x, src), __shfl_sync(0xffffffffu, bv.y, src),
+                   __shfl_sync(0xffffffffu, bv.z, src));
+  float bo = FLT_MAX;
+  {
+    const int vf = R.link_vert_first[j], vc = R.link_vert_count[j];
+    for (int v = lane; v < vc; v += 32) {
+      const float4 x = __ldg(W->lvert32 + vf + v);
+      const float3 w = xform32(S.T[j], make_float3(x.x, x.y, x.z));
+      const float dx = w.x - bv.x, dy = w.y - bv.y, dz = w.z - bv.z;
+      bo = fminf(bo, dx * dx + dy * dy + dz * dz);
+    }
+  }
+  bo = warp_min(bo);
+  if (!(bo < FLT_MAX)) return FLT_MAX;
+  return sqrtf(bo) * (1.f + 1e-5f) + 2.f * (S.delta[i] + S.delta[j]) + 1e-6f;
+}
 
 // FP64 finalisation of candidates of pair (i, j), merged into the pair's
 // best: the lexicographic minimum (squared distance, triangle of i, triangle
@@ -1051,6 +1098,11 @@ __global__ void __launch_bounds__(kDW * 32, 2) k_self_dist(const KWorldDev* __re
       int top = 1, njobs = 0, ncand = 0;
       bool pc = false;  // certified contact of this pair
       if (per_pair) m32 = fcut;  // every pair on its own
+      // a pair without a running bound to prune with (the first, or every
+      // pair in per-pair mode) starts from a vertex-pair upper bound of its
+      // own distance (>= the running minimum including it, so the bound
+      // stays valid for the later pairs)
+      if (m32 >= fcut) m32 = fminf(m32, link_pair_seed(S, W, R, lane, i, j));
       if (lane == 0) {
         if (per_pair) S.bd = A.cutoff;
         S.stack[0] = make_uint2((uint32_t)R.link_root[i], (uint32_t)R.link_root[j]);
