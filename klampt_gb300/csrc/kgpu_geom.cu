@@ -131,6 +131,44 @@ __device__ __forceinline__ float placement_err32(const float* T, float r)
 // FP64 finalisation of distance candidates into the running lexicographic
 // best (pb2, pA, pB): pairs whose squared distance is below the bound, or
 // equal to the best with smaller (triangle of a, triangle of b)
+constexpr int kSeedMaxTris = 4096;  // geometries up to this size are scanned for a seed
+
+// An upper bound on the distance between the two placed surfaces: A's
+// vertex nearest the centre of B's root box, then B's vertex nearest that
+// vertex (the first vertex of each triangle), widened by the placement
+// bounds and rounding.  Seeds the running minimum, so that the traversal
+// prunes from the start.
+__device__ __noinline__ float geom_seed(const GeomDev& GA, const GeomDev& GB, const float* TA, const float* TB,
+                                        int lane, float dd)
+{
+  if (GA.ntri > kSeedMaxTris || GB.ntri > kSeedMaxTris) return FLT_MAX;
+  const float3 cb = xform32(TB, make_float3(GB.nodes[0].a.x, GB.nodes[0].a.y, GB.nodes[0].a.z));
+  float bd = FLT_MAX;
+  float3 bv = cb;
+  for (int t = lane; t < GA.ntri; t += 32) {
+    const float4 x = __ldg(GA.tri32 + 3 * (size_t)t);
+    const float3 w = xform32(TA, make_float3(x.x, x.y, x.z));
+    const float dx = w.x - cb.x, dy = w.y - cb.y, dz = w.z - cb.z;
+    const float d2 = dx * dx + dy * dy + dz * dz;
+    if (d2 < bd) { bd = d2; bv = w; }
+  }
+  const float m = warp_min(bd);
+  const unsigned mm = __ballot_sync(0xffffffffu, bd == m);
+  const int src = mm ? __ffs(mm) - 1 : 0;
+  bv = make_float3(__shfl_sync(0xffffffffu, bv.x, src), __shfl_sync(0xffffffffu, bv.y, src),
+                   __shfl_sync(0xffffffffu, bv.z, src));
+  float bo = FLT_MAX;
+  for (int t = lane; t < GB.ntri; t += 32) {
+    const float4 y = __ldg(GB.tri32 + 3 * (size_t)t);
+    const float3 w = xform32(TB, make_float3(y.x, y.y, y.z));
+    const float dx = w.x - bv.x, dy = w.y - bv.y, dz = w.z - bv.z;
+    bo = fminf(bo, dx * dx + dy * dy + dz * dz);
+  }
+  bo = warp_min(bo);
+  if (!(bo < FLT_MAX)) return FLT_MAX;
+  return sqrtf(bo) * (1.f + 1e-5f) + 2.f * dd + 1e-6f;
+}
+
 __device__ __noinline__ void geom_flush(GeomSmem& S, const GeomDev& GA, const GeomDev& GB, int lane, int ncand,
                                         float lim)
 {
@@ -205,6 +243,7 @@ __global__ void __launch_bounds__(kGW * 32) k_geom(const GeomDev GA, const GeomD
     int top = (GA.ntri > 0 && GB.ntri > 0) ? 1 : 0, njobs = 0, ncand = 0;
     bool hit = false;
     float run = fcut;  // distance: FP32 upper bound on the minimum (warp-uniform)
+    if (DIST && top > 0) run = fminf(run, geom_seed(GA, GB, TA, TB, lane, dd));
 #pragma unroll 1
     while ((top > 0 || njobs > 0) && !hit) {
       if (njobs >= 16 || (top == 0 && njobs > 0)) {
