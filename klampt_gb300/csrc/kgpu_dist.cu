@@ -163,6 +163,8 @@ constexpr int kSeedMaxTris = 4096;  // objects up to this size are scanned for a
 __device__ __noinline__ float pair_seed(DistSmem& S, const KWorldDev* __restrict__ W, const KRobotDev& R, int lane,
                                         int l, int o)
 {
+  const int ff = W->obj_leaf_first[o], fc = W->obj_leaf_count[o];
+  if (fc > kSeedMaxTris) return FLT_MAX;  // large objects (terrains): no seed
   const KNode ob = W->enodes[W->obj_root[o]];
   const float* TA = S.T[l];
   const int vf = R.link_vert_first[l], vc = R.link_vert_count[l];
@@ -180,8 +182,6 @@ __device__ __noinline__ float pair_seed(DistSmem& S, const KWorldDev* __restrict
   const int src = mm ? __ffs(mm) - 1 : 0;
   bv = make_float3(__shfl_sync(0xffffffffu, bv.x, src), __shfl_sync(0xffffffffu, bv.y, src),
                    __shfl_sync(0xffffffffu, bv.z, src));
-  const int ff = W->obj_leaf_first[o], fc = W->obj_leaf_count[o];
-  if (fc > kSeedMaxTris) return FLT_MAX;  // large objects (terrains): no seed
   float bo = FLT_MAX;
   for (int t = lane; t < fc; t += 32) {
     const float4 y = __ldg(W->etri32 + 3 * (size_t)(ff + t));
