@@ -432,13 +432,15 @@ kgpu_status kgpu_check_edges_host(kgpu_world world, int32_t robot, const float* 
  * planning or control loop that cannot afford cudaMalloc's device-wide
  * synchronisation, or a host application that hands all device memory to its
  * own pool — this variant of kgpu_check_edges gives the same results but
- * works only inside one fixed 20 MiB file-scope device array, which every
+ * works only inside one fixed 32 MiB file-scope device array, which every
  * GPU that loads the library keeps until the process exits.  At most
- * KGPU_NOALLOC_MAX_EDGES edges per call (larger E: KGPU_ERR_INVALID).  The
- * first call on a device looks up the array's address (make it before any
- * stream capture); each call clears the parts that must start at zero, and
- * calls that overlap on the GPU race on the shared array, so serialise them.
- * The world's collision masks must not have changed since its last regular
+ * KGPU_NOALLOC_MAX_EDGES edges per call (larger E: KGPU_ERR_INVALID).
+ * kgpu_world_create looks the array up (and so loads it) on the world's
+ * device, so no call allocates; each call clears the parts that must start
+ * at zero, and calls that overlap on the GPU race on the shared array, so
+ * serialise them.  It uses the world's launch options, with blocks_per_sm
+ * capped at what the array's per-warp regions serve (2560 warps).  The
+ * world's collision masks must not have changed since its last regular
  * query (re-uploading them would allocate). */
 #define KGPU_NOALLOC_MAX_EDGES 65536
 kgpu_status kgpu_check_edges_noalloc(kgpu_world world, int32_t robot, const float* qa,
