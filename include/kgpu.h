@@ -133,7 +133,7 @@ kgpu_status kgpu_env_create(const kgpu_env_desc* desc, kgpu_env* out);
 
 /* kgpu_env_create with build flags.  KGPU_ENV_BUILD_GPU builds the
  * environment trees on the current GPU (linear BVH: Morton-code radix sort
- * and radix tree, boxes bottom up) instead of the host median-split builder;
+ * and radix tree, boxes bottom up) instead of the host surface-area builder;
  * the layout, the results of every query and the FP32 conservativeness are
  * the same, the tree shape (and so the traversal cost) differs.  The host
  * builder stands in for the PQP precompute InitCollisions runs

@@ -1,5 +1,5 @@
 // kgpu_lbvh.cu — environment BVH built on the GPU (linear BVH), the
-// alternative to the host median-split builder (bvh.cpp) for large scenes.
+// alternative to the host surface-area builder (bvh.cpp) for large scenes.
 //
 // Replaces the PQP hierarchy precompute Klamp't runs in InitCollisions
 // (Cpp/Modeling/World.cpp:266-274, Python/klampt/src/robotsim.cpp:
