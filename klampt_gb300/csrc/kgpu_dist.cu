@@ -178,8 +178,9 @@ __device__ __noinline__ float pair_seed(DistSmem& S, const KWorldDev* __restrict
     if (d2 < bd) { bd = d2; bv = w; }
   }
   const float m = warp_min(bd);
+  if (!(m < FLT_MAX)) return FLT_MAX;  // no vertex: no surface point, no seed
   const unsigned mm = __ballot_sync(0xffffffffu, bd == m);
-  const int src = mm ? __ffs(mm) - 1 : 0;
+  const int src = __ffs(mm) - 1;
   bv = make_float3(__shfl_sync(0xffffffffu, bv.x, src), __shfl_sync(0xffffffffu, bv.y, src),
                    __shfl_sync(0xffffffffu, bv.z, src));
   float bo = FLT_MAX;
@@ -973,8 +974,9 @@ __device__ __noinline__ float link_pair_seed(SelfDistSmem& S, const KWorldDev* _
     }
   }
   const float m = warp_min(bd);
+  if (!(m < FLT_MAX)) return FLT_MAX;  // no vertex: no surface point, no seed
   const unsigned mm = __ballot_sync(0xffffffffu, bd == m);
-  const int src = mm ? __ffs(mm) - 1 : 0;
+  const int src = __ffs(mm) - 1;
   bv = make_float3(__shfl_sync(0xffffffffu, bv.x, src), __shfl_sync(0xffffffffu, bv.y, src),
                    __shfl_sync(0xffffffffu, bv.z, src));
   float bo = FLT_MAX;
