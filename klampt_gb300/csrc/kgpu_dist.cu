@@ -767,6 +767,16 @@ __global__ void __launch_bounds__(kDW * 32, 2) k_dist(const KWorldDev* __restric
           __syncwarp();
           if (vm > (float)fmax(best, 0.0) * 1.00001f + 1e-6f) break;
           const int o = S.pobj[k], l = S.plink[k];
+          // a pair cannot go below 0 unless its object is convex, and then
+          // not below minus the smallest half-extent of the object's box
+          // (no point lies deeper inside a convex body that fits in the
+          // box): once the best is at or under that, the pair can at most
+          // tie, which only a smaller (link, object) would win
+          const double dlow = W->obj_convex[o] ? -(double)fminf(fminf(W->enodes[W->obj_root[o]].b.x,
+                                                                       W->enodes[W->obj_root[o]].b.y),
+                                                                 W->enodes[W->obj_root[o]].b.z)
+                                               : 0.0;
+          if (bl >= 0 && (dlow > best || (dlow == best && !(l < bl || (l == bl && o < bo))))) continue;
           PairOut po;
           // the first pair has no running bound to prune with yet: seed it
           eval_pair(S, W, R, T64, fk64, lane, l, o, nextafter(best, 1e300), po, cnt,
