@@ -667,6 +667,15 @@ MinResult min_distance(Ctx& c, double bound)
     // only when its boxes meet (bound 0)
     if (x.first > std::max(m.d, 0.0) + 1e-9) break;
     const int l = x.second / c.E->N, o = x.second % c.E->N;
+    // a pair's distance is at least 0 unless its object is convex, and then
+    // at least minus the smallest half-extent of the object's box; a pair
+    // that cannot go below the best, and could at most tie without winning
+    // the tie, cannot change the result
+    if (m.link >= 0) {
+      const double* h = &c.E->obj_h[3 * (size_t)o];
+      const double dlow = c.E->convex[o] ? -std::min(h[0], std::min(h[1], h[2])) : 0.0;
+      if (dlow > m.d || (dlow == m.d && !(l < m.link || (l == m.link && o < m.obj)))) continue;
+    }
     // ties must reach the comparison: search with a bound slightly above m.d
     PairResult pr = pair_distance(c, l, o, std::nextafter(m.d, 1e300));
     if (pr.found && (pr.d < m.d || (pr.d == m.d && m.link >= 0 && (l < m.link || (l == m.link && o < m.obj))))) {
